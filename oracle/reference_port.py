@@ -1,0 +1,300 @@
+"""CPU oracle: the reference's numpy GAP/ADMM path, restated.
+
+TEST INFRASTRUCTURE ONLY.  Nothing in the product imports this module; only
+``tests/``, ``__graft_entry__.smoke()`` and the CPU-baseline leg of
+``bench.py`` use it, and only as the checker.
+
+Each function restates one reference function with the same numpy operation
+order, so that a float64 run is bit-identical to the reference's own code.
+That identity is pinned: ``tests/golden/make_golden.py`` imports the
+reference modules themselves (``PnP_SCI/python/utils.py``,
+``PnP_SCI/python/pnp_sci_algo.py``) with the third-party imports replaced by
+``oracle.tv_chambolle`` and the metric restatements below, runs them on
+seeded inputs and stores the outputs; ``tests/test_oracle.py`` checks this
+port against those fixtures bit for bit.
+
+Extensions over the reference, used by the large configurations and marked
+where they appear: ``tv_weight`` and ``_lambda`` may be per-iteration
+sequences (a schedule); ``eps`` of the TV may be passed through.
+"""
+import math
+import time
+
+import numpy as np
+from scipy.ndimage import uniform_filter
+
+from .tv_chambolle import denoise_tv_chambolle
+
+
+# ---------------------------------------------------------------- L1 operators
+def A_(x, Phi):
+    """``PnP_SCI/python/utils.py:10-15``: y = sum_b x[..., b] * Phi[..., b]."""
+    return np.sum(x * Phi, axis=2)
+
+
+def At_(y, Phi):
+    """``PnP_SCI/python/utils.py:17-26``: x[..., b] = y * Phi[..., b]."""
+    return np.multiply(np.repeat(y[:, :, np.newaxis], Phi.shape[2], axis=2), Phi)
+
+
+def psnr(ref, img):
+    """``PnP_SCI/python/utils.py:28-36`` (peak 1, returns 100 when equal)."""
+    mse = np.mean((ref - img) ** 2)
+    if mse == 0:
+        return 100
+    return 20 * math.log10(1.0 / math.sqrt(mse))
+
+
+# ------------------------------------------------------- third-party metrics
+def compare_psnr(im_true, im_test, data_range=None):
+    """scikit-image 0.16 ``measure.compare_psnr``: 10 log10(R^2 / MSE).
+
+    Called per frame at ``pnp_sci_algo.py:704`` and ``:862`` with
+    ``data_range=1``.  The MSE is taken in float64.
+    """
+    im_true = np.asarray(im_true, dtype=np.float64)
+    im_test = np.asarray(im_test, dtype=np.float64)
+    err = np.mean(np.square(im_true - im_test), dtype=np.float64)
+    return 10 * np.log10((data_range ** 2) / err)
+
+
+def compare_ssim(X, Y, win_size=None, data_range=None, multichannel=False,
+                 **_unused):
+    """scikit-image 0.16 ``measure.compare_ssim`` with its default options.
+
+    Wang et al. (2004) SSIM with a 7 x 7 uniform window
+    (``scipy.ndimage.uniform_filter``, mode 'reflect'), sample covariance
+    (N / (N - 1)), K1 = 0.01, K2 = 0.03, and the mean taken over the image
+    cropped by (win_size - 1) // 2 on every side.  The reference calls it
+    per frame with ``data_range=1`` (``pnp_sci_algo.py:705``, ``:863``).
+    """
+    X = np.asarray(X, dtype=np.float64)
+    Y = np.asarray(Y, dtype=np.float64)
+    if multichannel:
+        return float(np.mean([compare_ssim(X[..., c], Y[..., c], win_size,
+                                           data_range) for c in range(X.shape[-1])]))
+    win = 7 if win_size is None else win_size
+    ndim = X.ndim
+    npix = win ** ndim
+    cov_norm = npix / (npix - 1.0)
+    ux = uniform_filter(X, size=win)
+    uy = uniform_filter(Y, size=win)
+    uxx = uniform_filter(X * X, size=win)
+    uyy = uniform_filter(Y * Y, size=win)
+    uxy = uniform_filter(X * Y, size=win)
+    vx = cov_norm * (uxx - ux * ux)
+    vy = cov_norm * (uyy - uy * uy)
+    vxy = cov_norm * (uxy - ux * uy)
+    R = data_range
+    C1 = (0.01 * R) ** 2
+    C2 = (0.03 * R) ** 2
+    A1, A2, B1, B2 = (2 * ux * uy + C1, 2 * vxy + C2,
+                      ux ** 2 + uy ** 2 + C1, vx + vy + C2)
+    S = (A1 * A2) / (B1 * B2)
+    pad = (win - 1) // 2
+    crop = tuple(slice(pad, s - pad) for s in S.shape)
+    return float(S[crop].mean())
+
+
+# ---------------------------------------------------------------- schedules
+def _at(seq_or_scalar, k):
+    """Value of a per-iteration schedule at iteration k (extension)."""
+    if np.ndim(seq_or_scalar) == 0:
+        return seq_or_scalar
+    return seq_or_scalar[k]
+
+
+def annealed_weights(w0, w1, n):
+    """Geometric tv_weight schedule w_k = w0 (w1/w0)^(k/(n-1)).
+
+    Extends the multiplicative annealing of ``ADMM_TV_rec``
+    (``pnp_sci_algo.py:898``: ``weight = 0.999*weight`` per iteration) to
+    fixed end points; used for the 2048 x 2048 x 24 configuration
+    (0.2 -> 0.05 over 60 iterations).
+    """
+    if n == 1:
+        return np.array([w0], dtype=np.float64)
+    k = np.arange(n, dtype=np.float64)
+    return w0 * (w1 / w0) ** (k / (n - 1))
+
+
+# ---------------------------------------------------------------- L2 solvers
+def gap_denoise(y, Phi_sum, A, At, _lambda=1, accelerate=True,
+                denoiser='tv', iter_max=50, noise_estimate=False, sigma=None,
+                tv_weight=0.1, tv_iter_max=5, multichannel=True, x0=None,
+                X_orig=None, model=None, show_iqa=True, tvm='tv_chambolle',
+                eps=2.e-4, verbose=False):
+    """``PnP_SCI/python/pnp_sci_algo.py:536-706`` with ``denoiser='tv'``.
+
+    GAP (``:645``) or accelerated GAP (``:641-643``) projection, then the
+    Chambolle TV (``:650``).  ``tv_weight`` / ``_lambda`` may also be
+    sequences indexed by the global iteration (extension).  Only the
+    'tv' / 'tv_chambolle' plug-in exists here.
+    """
+    if denoiser.lower() != 'tv' or tvm != 'tv_chambolle':
+        raise ValueError('oracle supports denoiser="tv", tvm="tv_chambolle"')
+    if x0 is None:
+        x0 = At(y)
+    if not isinstance(sigma, list):
+        sigma = [sigma]
+    if not isinstance(iter_max, list):
+        iter_max = [iter_max] * len(sigma)
+    y1 = np.zeros_like(y)
+    x = x0
+    psnr_all = []
+    k = 0
+    for idx, nsig in enumerate(sigma):
+        for it in range(iter_max[idx]):
+            lam = _at(_lambda, k)
+            w = _at(tv_weight, k)
+            yb = A(x)
+            if accelerate:
+                y1 = y1 + (y - yb)
+                x = x + lam * (At((y1 - yb) / Phi_sum))
+            else:
+                x = x + lam * (At((y - yb) / Phi_sum))
+            x = denoise_tv_chambolle(x, w, eps=eps, n_iter_max=tv_iter_max,
+                                     multichannel=multichannel)
+            if show_iqa and X_orig is not None:
+                psnr_all.append(psnr(X_orig, x))
+                if verbose and (k + 1) % 5 == 0:
+                    print('  GAP-TV iteration {: 3d}, PSNR {:2.2f} dB.'.format(
+                        k + 1, psnr_all[k]))
+            k = k + 1
+    psnr_, ssim_ = [], []
+    nmask = x.shape[-1]
+    if X_orig is not None:
+        for imask in range(nmask):
+            psnr_.append(compare_psnr(X_orig[..., imask], x[..., imask], data_range=1.))
+            ssim_.append(compare_ssim(X_orig[..., imask], x[..., imask], data_range=1.,
+                                      multichannel=x[..., imask].ndim > 2))
+    return x, psnr_, ssim_, psnr_all
+
+
+def admm_denoise(y, Phi_sum, A, At, _lambda=1, gamma=0.01,
+                 denoiser='tv', iter_max=50, noise_estimate=False, sigma=None,
+                 tv_weight=0.1, tv_iter_max=5, multichannel=True, x0=None,
+                 model=None, X_orig=None, show_iqa=True, eps=2.e-4,
+                 verbose=False):
+    """``PnP_SCI/python/pnp_sci_algo.py:708-864`` with ``denoiser='tv'``.
+
+    yb = A(theta + b); x = theta + b + lambda At((y - yb)/(Phi_sum + gamma))
+    (``:808-809``); theta = TV(x - b) (``:812-813``); b = b - (x - theta)
+    (``:836``).  Returns x, not theta (``:864``).
+    """
+    if denoiser.lower() != 'tv':
+        raise ValueError('oracle supports denoiser="tv"')
+    if x0 is None:
+        x0 = At(y)
+    if not isinstance(sigma, list):
+        sigma = [sigma]
+    if not isinstance(iter_max, list):
+        iter_max = [iter_max] * len(sigma)
+    x = x0
+    theta = x0
+    b = np.zeros_like(x0)
+    psnr_all = []
+    k = 0
+    for idx, nsig in enumerate(sigma):
+        for it in range(iter_max[idx]):
+            lam = _at(_lambda, k)
+            w = _at(tv_weight, k)
+            yb = A(theta + b)
+            x = (theta + b) + lam * (At((y - yb) / (Phi_sum + gamma)))
+            theta = denoise_tv_chambolle(x - b, w, eps=eps, n_iter_max=tv_iter_max,
+                                         multichannel=multichannel)
+            b = b - (x - theta)
+            if show_iqa and X_orig is not None:
+                psnr_all.append(psnr(X_orig, x))
+                if verbose and (k + 1) % 5 == 0:
+                    print('  ADMM-TV iteration {: 3d}, PSNR {:2.2f} dB.'.format(
+                        k + 1, psnr_all[k]))
+            k = k + 1
+    psnr_, ssim_ = [], []
+    nmask = x.shape[2]
+    if X_orig is not None:
+        for imask in range(nmask):
+            psnr_.append(compare_psnr(X_orig[:, :, imask], x[:, :, imask], data_range=1.))
+            ssim_.append(compare_ssim(X_orig[:, :, imask], x[:, :, imask], data_range=1.))
+    return x, psnr_, ssim_, psnr_all
+
+
+def admmdenoise_cacti(meas, mask, A, At, projmeth='admm', v0=None, orig=None,
+                      iframe=0, nframe=1, MAXB=1., maskdirection='plain',
+                      **args):
+    """``PnP_SCI/python/pnp_sci_algo.py:479-534``: the frame-block driver.
+
+    Phi_sum with zeros replaced by 1 (``:491-492``), per-block scaling by
+    MAXB (``:501-503``), v0 flips for 'updown'/'downup' masks
+    (``:506-510``, ``:521-527``).  An unknown ``projmeth`` raises
+    ValueError (the reference only prints, ``:518-519``).
+    """
+    nmask = mask.shape[-1]
+    mask_sum = np.sum(mask, axis=tuple(range(2, mask.ndim)))
+    mask_sum[mask_sum == 0] = 1
+    x_ = np.zeros((*mask.shape[:-1], nmask * nframe), dtype=np.float32)
+    psnr_, ssim_, psnrall_ = [], [], []
+    begin_time = time.time()
+    orig_k = None
+    for kf in range(nframe):
+        if orig is not None:
+            orig_k = orig[..., (kf + iframe) * nmask:(kf + iframe + 1) * nmask] / MAXB
+        meas_k = meas[..., kf + iframe] / MAXB
+        if v0 is None:
+            v0_k = None
+        else:
+            v0_k = v0[:, :, kf * nmask:(kf + 1) * nmask]
+            if (maskdirection.lower() == 'updown' and (kf + iframe) % 2 == 1) or \
+               (maskdirection.lower() == 'downup' and (kf + iframe) % 2 == 0):
+                v0_k = v0_k[..., ::-1]
+        if projmeth.lower() == 'admm':
+            x_k, psnr_k, ssim_k, psnrall_k = admm_denoise(
+                meas_k, mask_sum, A, At, x0=v0_k, X_orig=orig_k, **args)
+        elif projmeth.lower() == 'gap':
+            x_k, psnr_k, ssim_k, psnrall_k = gap_denoise(
+                meas_k, mask_sum, A, At, x0=v0_k, X_orig=orig_k, **args)
+        else:
+            raise ValueError('Unsupported projection method %s' % projmeth.upper())
+        if (maskdirection.lower() == 'updown' and (kf + iframe) % 2 == 1) or \
+           (maskdirection.lower() == 'downup' and (kf + iframe) % 2 == 0):
+            x_k = x_k[..., ::-1]
+            psnr_k = psnr_k[::-1]
+            ssim_k = ssim_k[::-1]
+            psnrall_k = psnrall_k[::-1]
+        t_ = time.time() - begin_time
+        x_[..., kf * nmask:(kf + 1) * nmask] = x_k
+        psnr_.extend(psnr_k)
+        ssim_.extend(ssim_k)
+        psnrall_.append(psnrall_k)
+    return x_, t_, psnr_, ssim_, psnrall_
+
+
+# ------------------------------------------------------------- legacy loops
+def GAP_TV_rec(y, Phi, A, At, Phi_sum, maxiter, step_size, weight, row, col,
+               ColT, X_ori, tv_n_iter=30):
+    """``PnP_SCI/python/pnp_sci_algo.py:866-882`` (two-argument A/At)."""
+    y1 = np.zeros((row, col))
+    f = At(y, Phi)
+    for ni in range(maxiter):
+        fb = A(f, Phi)
+        y1 = y1 + (y - fb)
+        f = f + np.multiply(step_size, At(np.divide(y1 - fb, Phi_sum), Phi))
+        f = denoise_tv_chambolle(f, weight, n_iter_max=tv_n_iter, multichannel=True)
+    return f
+
+
+def ADMM_TV_rec(y, Phi, A, At, Phi_sum, maxiter, step_size, weight, row, col,
+                ColT, eta, X_ori, tv_n_iter=30):
+    """``PnP_SCI/python/pnp_sci_algo.py:884-907``; anneals weight *= 0.999
+    and eta *= 0.998 every iteration (``:898-899``)."""
+    theta = At(y, Phi)
+    v = theta
+    b = np.zeros((row, col, ColT))
+    for ni in range(maxiter):
+        yb = A(theta + b, Phi)
+        v = (theta + b) + np.multiply(step_size, At(np.divide(y - yb, Phi_sum + eta), Phi))
+        theta = denoise_tv_chambolle(v - b, weight, n_iter_max=tv_n_iter, multichannel=True)
+        b = b - (v - theta)
+        weight = 0.999 * weight
+        eta = 0.998 * eta
+    return v

@@ -1,0 +1,166 @@
+"""The oracle pinned against the reference's own outputs (no GPU needed).
+
+Fixtures come from ``tests/golden/make_golden.py``, which ran the
+reference's ``utils.py`` / ``pnp_sci_algo.py`` themselves.  The numpy port
+must reproduce them bit for bit; the C oracle must agree with the numpy
+port to 1e-12 relative.  The third-party TV restatement is checked through
+known-answer properties (its parity with scikit-image is unpinned).
+"""
+import json
+
+import numpy as np
+import pytest
+
+from oracle import reference_port as port
+from oracle import c_oracle
+from oracle.tv_chambolle import (denoise_tv_chambolle, tv_chambolle_frames,
+                                 tv_cham_itv2d_matlab, _tv_chambolle_nd)
+import sci_algorithms_gb300.datasets as ds
+
+
+def _cacti_args(g):
+    return json.loads(str(g["args_json"]))
+
+
+def _run_port_cacti(g):
+    mask, meas, orig = g["mask"], g["meas"], g["orig"]
+    A = lambda x: port.A_(x, mask)  # noqa: E731
+    At = lambda y: port.At_(y, mask)  # noqa: E731
+    v0 = g["v0"] if "v0" in g else None
+    return port.admmdenoise_cacti(
+        meas, mask, A, At, projmeth=str(g["projmeth"]), v0=v0, orig=orig,
+        iframe=int(g["iframe"]), nframe=int(g["nframe"]), MAXB=float(g["MAXB"]),
+        maskdirection=str(g["maskdirection"]), **_cacti_args(g))
+
+
+def test_ops_bit_exact(golden):
+    g = golden("ops")
+    assert np.array_equal(port.A_(g["x"], g["phi"]), g["A"])
+    assert np.array_equal(port.At_(g["y"], g["phi"]), g["At"])
+    assert port.psnr(g["x"], g["x"] + 0.01 * g["y"][..., None]) == g["psnr"]
+    assert port.psnr(g["x"], g["x"]) == 100 == g["psnr_equal"]
+
+
+@pytest.mark.parametrize("case", ["gap_acc", "gap_plain", "gap_tv30", "admm",
+                                  "gap_updown", "admm_downup"])
+def test_driver_bit_exact(golden, case):
+    g = golden(case)
+    x_, _t, psnr_, ssim_, psnrall_ = _run_port_cacti(g)
+    assert np.array_equal(x_.astype(np.float64), g["x"])
+    assert np.array_equal(np.array(psnr_), g["psnr"])
+    assert np.array_equal(np.array(ssim_), g["ssim"])
+    assert np.array_equal(np.array(psnrall_), g["psnrall"])
+
+
+def test_legacy_loops_bit_exact(golden):
+    g = golden("legacy")
+    msum = np.sum(g["mask"], axis=2)
+    msum[msum == 0] = 1
+    v = port.ADMM_TV_rec(g["meas"], g["mask"], port.A_, port.At_, msum, 6, 1.0,
+                         0.1, 20, 20, 4, 0.01, g["orig"])
+    f = port.GAP_TV_rec(g["meas"], g["mask"], port.A_, port.At_, msum, 5, 1.0,
+                        0.1, 20, 20, 4, g["orig"])
+    assert np.array_equal(v, g["admm"])
+    assert np.array_equal(f, g["gap"])
+
+
+def test_config0_inputs_and_digest(golden):
+    import hashlib
+    g = golden("config0")
+    orig, mask, meas = ds.config0()
+
+    def dg(a):
+        return hashlib.sha256(np.ascontiguousarray(a, dtype=np.float64).tobytes()).hexdigest()
+    assert dg(orig) == str(g["orig_digest"])
+    assert dg(mask) == str(g["mask_digest"])
+    assert dg(meas) == str(g["meas_digest"])
+
+
+# ------------------------------------------------------------ TV properties
+def test_tv_constant_frame_unchanged():
+    f = np.full((17, 23, 3), 0.37)
+    u = denoise_tv_chambolle(f, 0.2, n_iter_max=7, multichannel=True)
+    assert np.array_equal(u, f)
+
+
+def test_tv_single_step_is_identity():
+    rng = np.random.default_rng(3)
+    f = rng.random((19, 11, 2))
+    assert np.array_equal(denoise_tv_chambolle(f, 0.3, n_iter_max=1, multichannel=True), f)
+
+
+def test_tv_stop_rule():
+    rng = np.random.default_rng(4)
+    f = rng.random((40, 33))
+    _, n, e = _tv_chambolle_nd(f, 0.1, 2e-4, 400)
+    assert n < 400  # the stop test fires
+    assert len(e) == n
+    # (E_k is scikit-image's stopping heuristic, not a monotone objective:
+    # it dips after the first step and then rises towards its limit.)
+    # stop at the first k with |E_{k-1}-E_k| < eps E_0
+    k_stop = next(k for k in range(1, len(e)) if abs(e[k - 1] - e[k]) < 2e-4 * e[0])
+    assert n == k_stop + 1
+
+
+def test_tv_matches_matlab_variant_in_the_interior():
+    """Same ROF problem as tvdenoise_cham_ITV2D.m with lambda = 1/weight:
+    after convergence both agree away from the first row/column (where the
+    MATLAB divergence differs)."""
+    rng = np.random.default_rng(5)
+    f = np.cumsum(np.cumsum(rng.standard_normal((28, 28)), 0), 1)
+    f = (f - f.min()) / (f.max() - f.min())
+    w = 0.08
+    u_sk = _tv_chambolle_nd(f, w, 0.0, 3000)[0]
+    u_ml = tv_cham_itv2d_matlab(f, 1.0 / w, 6000)
+    inner = (slice(10, None), slice(10, None))
+    assert np.max(np.abs(u_sk[inner] - u_ml[inner])) < 1e-5
+    # ... and the first-row/column divergence is where they differ
+    assert np.max(np.abs(u_sk[:2] - u_ml[:2])) > 1e-4
+
+
+def test_tv_frames_diagnostics_match_wrapper():
+    rng = np.random.default_rng(6)
+    f = rng.random((15, 14, 4))
+    u1 = denoise_tv_chambolle(f, 0.15, n_iter_max=60, multichannel=True)
+    u2, steps, _ = tv_chambolle_frames(f, 0.15, n_iter_max=60)
+    assert np.array_equal(u1, u2)
+    assert all(1 <= s <= 60 for s in steps)
+
+
+# ---------------------------------------------------------------- C oracle
+def test_c_oracle_tv_matches_port():
+    rng = np.random.default_rng(8)
+    f = rng.random((21, 18, 5))
+    for n_iter in (1, 2, 5, 40):
+        ref, steps, _ = tv_chambolle_frames(f, 0.12, n_iter_max=n_iter)
+        u, csteps, _ = c_oracle.tv_chambolle(c_oracle.planar(f), 0.12, n_iter)
+        assert list(csteps) == steps
+        np.testing.assert_allclose(c_oracle.unplanar(u), ref, rtol=0, atol=1e-13)
+
+
+@pytest.mark.parametrize("case", ["gap_acc", "gap_plain", "admm"])
+def test_c_oracle_solver_matches_golden(golden, case):
+    g = golden(case)
+    args = _cacti_args(g)
+    mask, meas, orig = g["mask"], g["meas"][..., 0], g["orig"]
+    msum = mask.sum(axis=2)
+    msum[msum == 0] = 1
+    iters = args["iter_max"]
+    iters = sum(iters) if isinstance(iters, list) else iters
+    x0 = c_oracle.planar(port.At_(meas, mask))
+    if str(g["projmeth"]) == "gap":
+        x, pa = c_oracle.gap_tv(meas, c_oracle.planar(mask), msum, x0, iters,
+                                lambdas=args["_lambda"], weights=args["tv_weight"],
+                                tv_iter_max=args["tv_iter_max"],
+                                accelerate=args["accelerate"],
+                                orig_bhw=c_oracle.planar(orig))
+    else:
+        x, pa = c_oracle.admm_tv(meas, c_oracle.planar(mask), msum, x0, iters,
+                                 lambdas=args["_lambda"], weights=args["tv_weight"],
+                                 gamma=args["gamma"], tv_iter_max=args["tv_iter_max"],
+                                 orig_bhw=c_oracle.planar(orig))
+    ref = g["x"]
+    rel = np.linalg.norm(c_oracle.unplanar(x) - ref) / np.linalg.norm(ref)
+    # x_ of the driver is stored as float32 (pnp_sci_algo.py:494)
+    assert rel < 1e-7
+    np.testing.assert_allclose(pa, g["psnrall"][0], rtol=1e-6)
