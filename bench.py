@@ -1,0 +1,310 @@
+"""Benchmark: GAP-TV reconstruction at 2048 x 2048 x 24 on one GB300.
+
+One step = one full GAP-TV solve of the 2048 x 2048 x 24 workload (Bernoulli
+0.5 mask, noise 0.01 max y, 60 iterations, tv_weight annealed 0.2 -> 0.05,
+tv_iter_max 5), inputs resident in HBM.  ``value`` is GAP-TV iterations per
+second over the whole job (N replicas for N GPUs: the path has no
+cross-measurement exchange, so ranks solve independent measurements).
+
+Also reported on the same JSON line:
+  roofline      the dominant kernel (the Chambolle TV pass) timed alone with
+                CUDA events, algorithmic bytes / duration vs measured HBM peak
+  e2e           the same metric through Solver.run_host: pinned host
+                measurement in, host result out, copies inside the timed region
+  cpu_baseline  the numpy port of the reference path on a bounded sample
+  admm          ADMM-TV iterations per second on the same workload
+
+``--impl reference`` times the reference's CPU implementation (the numpy
+port in oracle/, the reference being Python) on a bounded sample instead.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, REPO)
+
+H, W, B, ITERS, TV_ITERS = 2048, 2048, 24, 60, 5
+METRIC = "GAP-TV iter/s & HBM GB/s vs peak; unrolled fwd+bwd ms vs autograd at 1e-4 rel"
+WORKLOAD = "gap_tv_2048x2048x24"
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def base_config():
+    return {"workload": WORKLOAD, "H": H, "W": W, "B": B, "iters": ITERS,
+            "tv_iter_max": TV_ITERS, "tv_weight": "0.2->0.05 geometric", "lambda": 1.0,
+            "accelerate": True, "mask": "Bernoulli(0.5), packed 1 bit/frame/pixel",
+            "noise": "sigma = 0.01 max(y)",
+            "l2": "inputs larger than L2 (402.7 MB frame stack vs 129 MB L2); no flush"}
+
+
+def load_peaks():
+    p = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def ncu_traffic(kernel):
+    """dram bytes per launch from the committed ncu summary, or None."""
+    p = os.path.join(REPO, "profiles", "traffic.txt")
+    if not os.path.exists(p):
+        return None
+    for line in open(p):
+        parts = line.split()
+        if len(parts) >= 2 and parts[0] == kernel:
+            return float(parts[1])
+    return None
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.Q,
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.p.terminate()
+        out, _ = self.p.communicate(timeout=10)
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in out.strip().splitlines():
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                smax.append(float(f[1]))
+            except ValueError:
+                continue
+            for n, v in zip(names, f[4:8]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def cpu_sample(crop=1024, iters=2):
+    """The reference numpy path (oracle port, float64) on a crop of the
+    workload; returns full-size iterations/s (scaled by area) and a note."""
+    from oracle import reference_port as port
+    import sci_algorithms_gb300.datasets as ds
+    orig, mask, meas = ds.video_config(crop, crop, B, noise_rel=0.01)
+    msum = mask.sum(axis=2)
+    msum[msum == 0] = 1
+    w = port.annealed_weights(0.2, 0.05, ITERS)[:iters]
+    t0 = time.perf_counter()
+    port.gap_denoise(meas, msum, lambda x: port.A_(x, mask), lambda y: port.At_(y, mask),
+                     _lambda=1, accelerate=True, iter_max=iters, tv_weight=w,
+                     tv_iter_max=TV_ITERS, show_iqa=False)
+    dt = time.perf_counter() - t0
+    scale = (H * W) / float(crop * crop)
+    value = iters / (dt * scale)
+    note = ("numpy float64 port of gap_denoise (pnp_sci_algo.py:536-706) + Chambolle TV, "
+            "%d iterations on a %dx%dx%d crop (%.1f s), scaled by area x%.0f; "
+            "numpy elementwise kernels use 1 core" % (iters, crop, crop, B, dt, scale))
+    return value, note, dt
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    vals = []
+    for i in range(args.warmup + args.steps):
+        v, note, dt = cpu_sample(crop=args.ref_crop, iters=1)
+        if i >= args.warmup:
+            vals.append((v, dt))
+    value = float(np.mean([v for v, _ in vals]))
+    ms = float(np.mean([dt for _, dt in vals])) * 1e3 * (H * W) / args.ref_crop ** 2 * ITERS
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": "iter/s",
+            "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": base_config(),
+            "cpu_baseline": {"value": value, "unit": "iter/s", "cores": 1, "kind": "port",
+                             "sample": note},
+            "e2e": {"value": value, "unit": "iter/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+
+
+def run_gpu(args):
+    import torch
+    import sci_algorithms_gb300 as sci
+    from sci_algorithms_gb300 import _dev
+    from sci_algorithms_gb300._lib import call
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    dev = torch.device("cuda", local)
+
+    # replicas solve independent measurements: seed by rank
+    seeds = (1000 * rank, 1000 * rank + 1, 1000 * rank + 2)
+    orig, mask, meas = sci.datasets.video_config(H, W, B, noise_rel=0.01, seeds=seeds)
+    del orig
+    op = sci.MaskOperator(mask)
+    del mask
+    y = _dev.plane(meas, dev)
+    weights = np.array([0.2 * 0.25 ** (k / (ITERS - 1)) for k in range(ITERS)], np.float32)
+    gap = sci.Solver(op, "gap", ITERS, 1.0, weights, TV_ITERS, accelerate=True)
+    admm = sci.Solver(op, "admm", ITERS, 1.0, weights, TV_ITERS, gamma=0.01)
+    stream = torch.cuda.current_stream()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+        torch.cuda.synchronize()
+
+    def timed(fn, steps, warmup):
+        for _ in range(warmup):
+            fn()
+        barrier()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(steps):
+            fn()
+        e1.record(stream)
+        barrier()
+        ms = e0.elapsed_time(e1) / steps
+        if world > 1:
+            t = torch.tensor([ms], device=dev)
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms = float(t.item())
+        return ms
+
+    clocks = Clocks(local)
+    clocks.start()
+    ms_gap = timed(lambda: gap.run(y), args.steps, args.warmup)
+    clk = clocks.stop()
+    ms_admm = timed(lambda: admm.run(y), max(2, args.steps // 2), 1)
+
+    # dominant kernel alone: the TV pass on the frame stack (CUDA events on
+    # the launching stream), and the fused projection for the share
+    n = B * H * W
+    xin = gap.x.clone()
+    xout = torch.empty_like(xin)
+    ws = sci.tv.tv_workspace(B, H, W, TV_ITERS, dev)
+    y1 = torch.zeros((H, W), dtype=torch.float32, device=dev)
+
+    def tv_once():
+        call("sci_tv_chambolle", xin.data_ptr(), xout.data_ptr(), None, B, H, W, 0.1, 2e-4,
+             TV_ITERS, None, None, ws.data_ptr(), ws.numel(), stream.cuda_stream)
+
+    def proj_once():
+        call("sci_proj_gap", xin.data_ptr(), None, op.bits.data_ptr(), y.data_ptr(),
+             y1.data_ptr(), op.phisum.data_ptr(), xout.data_ptr(), 1.0, 1, B, H, W,
+             stream.cuda_stream)
+
+    ms_tv = timed(tv_once, 20, 3)
+    ms_proj = timed(proj_once, 20, 3)
+    peak, peak_kind = load_peaks()
+    tv_bytes = 8.0 * n                      # read x, write u (p stays on chip)
+    proj_bytes = 8.0 * n + 4.0 * H * W + 16.0 * H * W  # x r/w, mask words, y/y1/phisum/y1
+    tv_gbs = tv_bytes / (ms_tv * 1e-3) / 1e9
+    proj_gbs = proj_bytes / (ms_proj * 1e-3) / 1e9
+
+    # end to end through the public API with host buffers
+    y_host = torch.from_numpy(meas.astype(np.float32)).pin_memory()
+    x_host = torch.empty((B, H, W), dtype=torch.float32).pin_memory()
+    for _ in range(2):
+        gap.run_host(y_host, x_host)
+    barrier()
+    t0 = time.perf_counter()
+    e2e_steps = max(3, args.steps // 2)
+    for _ in range(e2e_steps):
+        gap.run_host(y_host, x_host)
+    barrier()
+    ms_e2e = (time.perf_counter() - t0) * 1e3 / e2e_steps
+    if world > 1:
+        t = torch.tensor([ms_e2e], device=dev)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_e2e = float(t.item())
+
+    if rank == 0:
+        cpu_v, cpu_note, _ = (None, None, None)
+        if world == 1 and not args.no_cpu:
+            cpu_v, cpu_note, _ = cpu_sample(crop=args.ref_crop, iters=2)
+        per_iter_bytes = proj_bytes + tv_bytes
+        line = {
+            "metric": METRIC, "value": world * ITERS * 1e3 / ms_gap, "unit": "iter/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": ms_gap, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+            "config": base_config(),
+            "roofline": {"bound": "hbm", "kernel": "k_tv_main<4> (Chambolle TV pass)",
+                         "achieved": tv_gbs, "peak": peak, "unit": "GB/s",
+                         "frac": tv_gbs / peak, "peak_kind": peak_kind,
+                         "traffic": ncu_traffic("k_tv_main"),
+                         "algorithmic_bytes_per_launch": tv_bytes, "ms_per_launch": ms_tv},
+            "kernels": {"tv_ms": ms_tv, "tv_gbs": tv_gbs, "proj_ms": ms_proj,
+                        "proj_gbs": proj_gbs, "proj_frac": proj_gbs / peak,
+                        "per_iteration_algorithmic_bytes": per_iter_bytes,
+                        "per_iteration_gbs": per_iter_bytes * ITERS / (ms_gap * 1e-3) / 1e9},
+            "admm": {"value": world * ITERS * 1e3 / ms_admm, "unit": "iter/s",
+                     "ms_per_step": ms_admm},
+            "e2e": {"value": world * ITERS * 1e3 / ms_e2e, "unit": "iter/s",
+                    "h2d_bytes_per_step": 4 * H * W, "d2h_bytes_per_step": 4 * n,
+                    "ms_per_step": ms_e2e},
+            "gpu_launches": args.steps * ITERS * 4,
+            "clocks": clk,
+        }
+        if cpu_v is not None:
+            line["cpu_baseline"] = {"value": cpu_v, "unit": "iter/s", "cores": 1,
+                                    "kind": "port", "sample": cpu_note}
+        print(json.dumps(line))
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--ref-crop", type=int, default=1024)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.warmup < 3:
+        args.warmup = 3
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

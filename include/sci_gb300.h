@@ -1,0 +1,160 @@
+/*
+ * sci_gb300.h -- C ABI of the GB300-native GAP-TV / ADMM-TV library
+ * (libsci_gb300.so, built from sci-algorithms_gb300/csrc for sm_103a).
+ *
+ * Conventions
+ *   - Every array argument is a DEVICE pointer to float32 data in the planar
+ *     layout B x H x W (frame-major, W fastest) unless stated otherwise.
+ *     The reference keeps frames last (H x W x B, numpy C order,
+ *     PnP_SCI/python/utils.py:15,26); callers convert once at the boundary.
+ *   - 2-D maps (measurement y, Phi_sum, y1) are H x W.
+ *   - `stream` is a cudaStream_t (NULL = legacy default stream).  All work is
+ *     stream-ordered; no call synchronises the device unless stated.
+ *   - Ownership: the caller allocates every buffer, including the workspace
+ *     whose size the *_workspace_bytes queries return.  The library keeps
+ *     no device memory of its own apart from cached CUDA graphs.
+ *   - Errors: every function returns SCI_OK (0) or a negative SCI_ERR_*
+ *     code; sci_last_error() returns the message of the last failure on the
+ *     calling thread.  No kernel traps; device-side waits are bounded.
+ *   - Inputs are never modified unless the argument is documented in/out.
+ */
+#ifndef SCI_GB300_H
+#define SCI_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SCI_OK 0
+#define SCI_ERR_INVALID_ARG -1
+#define SCI_ERR_CUDA -2
+#define SCI_ERR_UNSUPPORTED -3
+#define SCI_ERR_WORKSPACE -4
+#define SCI_ERR_TIMEOUT -5
+
+/* Library version (major*10000 + minor*100 + patch). */
+int sci_version(void);
+
+/* Copies the last error message of this thread into buf (NUL-terminated,
+ * truncated to n bytes).  Returns the full message length. */
+int sci_last_error(char *buf, size_t n);
+
+/* ---------------------------------------------------------- L1 operators */
+
+/* y = sum_b phi_b .* x_b.
+ * Replaces A_(x, Phi)            PnP_SCI/python/utils.py:10-15 */
+int sci_A(const float *x, const float *phi, float *y,
+          int64_t B, int64_t H, int64_t W, void *stream);
+
+/* x_b = phi_b .* y.
+ * Replaces At_(y, Phi)           PnP_SCI/python/utils.py:17-26 */
+int sci_At(const float *y, const float *phi, float *x,
+           int64_t B, int64_t H, int64_t W, void *stream);
+
+/* phisum = sum_b phi_b, entries equal to 0 replaced by 1 when guard_zero.
+ * Replaces the mask_sum lines    PnP_SCI/python/pnp_sci_algo.py:491-492 */
+int sci_phisum(const float *phi, float *phisum, int64_t B, int64_t H,
+               int64_t W, int guard_zero, void *stream);
+
+/* Packs a binary mask (every entry exactly 0 or 1) into one uint32 word per
+ * pixel, bit b = phi_b (B <= 32).  Returns SCI_ERR_INVALID_ARG through
+ * *nonbinary_flag (device int, set to 1) if an entry is neither 0 nor 1;
+ * the caller must then use the float mask.  No reference counterpart: a
+ * storage format for binary coded apertures (pnp_sci_test_orig.py:135-137
+ * masks are 0/1 after normalisation). */
+int sci_pack_mask(const float *phi, uint32_t *bits, int *nonbinary_flag,
+                  int64_t B, int64_t H, int64_t W, void *stream);
+
+/* ------------------------------------------------ projections (fused K1) */
+
+/* One GAP projection over the B-frame stack in a single pass:
+ *   yb = A(x); accelerate: y1 += y - yb, r = (y1 - yb)/phisum;
+ *   else r = (y - yb)/phisum;   x_out = x + lambda * At(r).
+ * y1 is in/out (ignored when accelerate == 0).  mask_bits (nullable) is
+ * the packed form of phi; when given, phi may be NULL.
+ * Replaces pnp_sci_algo.py:640-645 (gap_denoise, GAP and GAP_acc). */
+int sci_proj_gap(const float *x, const float *phi, const uint32_t *mask_bits,
+                 const float *y, float *y1, const float *phisum, float *x_out,
+                 float lambda, int accelerate,
+                 int64_t B, int64_t H, int64_t W, void *stream);
+
+/* One ADMM projection:  t = theta + b; yb = A(t);
+ *   x = t + lambda * At((y - yb)/(phisum + gamma));  v = x - b.
+ * Writes v (the TV input) and, when x_out is non-NULL, x.
+ * Replaces pnp_sci_algo.py:808-809 (admm_denoise) and the x - b of :812. */
+int sci_proj_admm(const float *theta, const float *b, const float *phi,
+                  const uint32_t *mask_bits, const float *y,
+                  const float *phisum, float *v, float *x_out, float lambda,
+                  float gamma, int64_t B, int64_t H, int64_t W, void *stream);
+
+/* ------------------------------------------------------ Chambolle TV (K2) */
+
+/* Bytes of device workspace sci_tv_chambolle needs for these sizes. */
+int sci_tv_workspace_bytes(int64_t nframes, int64_t H, int64_t W,
+                           int n_iter_max, size_t *bytes);
+
+/* Per-frame Chambolle TV (scikit-image 0.16 denoise_tv_chambolle
+ * semantics, including its energy stop test with eps) of nframes H x W
+ * frames: u = TV(f).  resid (nullable) receives u - f (the ADMM multiplier
+ * update b = theta - v).  steps (nullable, device int[nframes]) receives
+ * the number of executed Chambolle steps per frame.  energy (nullable,
+ * device double[nframes * n_iter_max * 2]) receives per-frame sums
+ * (sum (div p_k)^2, sum |grad u_k|) of the steps it evaluates.
+ * Replaces denoise_tv_chambolle(x, weight, n_iter_max, multichannel=True)
+ * as called at PnP_SCI/python/pnp_sci_algo.py:650 and :812-813. */
+int sci_tv_chambolle(const float *f, float *u, float *resid, int64_t nframes,
+                     int64_t H, int64_t W, float weight, float eps,
+                     int n_iter_max, int *steps, double *energy,
+                     void *workspace, size_t workspace_bytes, void *stream);
+
+/* -------------------------------------------------- metrics (diagnostics) */
+
+/* out[0] += sum_i (a_i - b_i)^2 in float64 (PSNR numerator for
+ * psnr()/compare_psnr, PnP_SCI/python/utils.py:28-36). */
+int sci_sqerr_accum(const float *a, const float *b, int64_t n, double *out,
+                    void *stream);
+
+/* ------------------------------------------------------ solvers (L2 loop) */
+
+/* Options shared by the solvers. */
+typedef struct sci_solve_opts {
+    int iters;               /* total GAP/ADMM iterations                   */
+    const float *lambdas;    /* HOST array [iters]: lambda_k                */
+    const float *weights;    /* HOST array [iters]: tv_weight_k             */
+    int tv_iter_max;         /* Chambolle steps per TV call (n_iter_max)    */
+    float eps;               /* TV stop tolerance (scikit-image eps)        */
+    int accelerate;          /* GAP: 1 = GAP_acc                            */
+    float gamma;             /* ADMM: gamma                                 */
+    const float *gammas;     /* nullable HOST array [iters]: gamma_k        */
+    const float *orig;       /* nullable: ground truth for PSNR per iter    */
+    double *sqerr;           /* nullable device double[iters]: sum sq. err. */
+    int *tv_steps;           /* nullable device int[iters * B]              */
+    int use_graph;           /* 1: capture the loop in a CUDA graph (cached) */
+} sci_solve_opts;
+
+/* Workspace bytes for sci_gap_tv / sci_admm_tv. */
+int sci_solver_workspace_bytes(int64_t B, int64_t H, int64_t W,
+                               const sci_solve_opts *opts, size_t *bytes);
+
+/* GAP-TV: x_out = gap_denoise(y, phisum, A, At, x0=x0, ...).x for
+ * denoiser='tv' (PnP_SCI/python/pnp_sci_algo.py:536-706).  x0 and x_out may
+ * alias.  phi or mask_bits (one may be NULL). */
+int sci_gap_tv(const float *y, const float *phi, const uint32_t *mask_bits,
+               const float *phisum, const float *x0, float *x_out,
+               int64_t B, int64_t H, int64_t W, const sci_solve_opts *opts,
+               void *workspace, size_t workspace_bytes, void *stream);
+
+/* ADMM-TV: x_out = admm_denoise(y, phisum, A, At, x0=x0, ...).x
+ * (PnP_SCI/python/pnp_sci_algo.py:708-864); returns x, not theta. */
+int sci_admm_tv(const float *y, const float *phi, const uint32_t *mask_bits,
+                const float *phisum, const float *x0, float *x_out,
+                int64_t B, int64_t H, int64_t W, const sci_solve_opts *opts,
+                void *workspace, size_t workspace_bytes, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SCI_GB300_H */

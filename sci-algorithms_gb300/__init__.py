@@ -1,1 +1,16 @@
-"""GB300-native GAP-TV / ADMM-TV reconstruction for snapshot compressive imaging."""
+"""GB300-native GAP-TV / ADMM-TV reconstruction for snapshot compressive imaging.
+
+A drop-in for the TV path of Scientific-Research-Resource/SCI-algorithms
+``PnP_SCI/python``: the ``A_`` / ``At_`` mask operators, the Chambolle TV
+denoiser and the ``admmdenoise_cacti`` / ``gap_denoise`` / ``admm_denoise``
+drivers, with the same names and arguments.  Compute runs in hand-written
+sm_103a CUDA kernels behind the C ABI of ``include/sci_gb300.h``
+(``libsci_gb300.so``); there is no CPU fallback.
+"""
+from .buildlib import build  # noqa: F401
+from .utils import A_, At_, psnr, make_ops, MaskOperator  # noqa: F401
+from .tv import denoise_tv_chambolle, tv_frames  # noqa: F401
+from .pnp_sci_algo import (admmdenoise_cacti, gap_denoise, admm_denoise,  # noqa: F401
+                           GAP_TV_rec, ADMM_TV_rec)
+from .solver import Solver  # noqa: F401
+from . import datasets  # noqa: F401

@@ -1,0 +1,105 @@
+// Shared helpers of the sm_103a kernels: error reporting, argument checks,
+// vector loads, packed-FP32 arithmetic.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "sci_gb300.h"
+
+namespace sci {
+
+// ---------------------------------------------------------------- errors
+void set_error(const char *fmt, ...);
+int cuda_status(cudaError_t e, const char *what);
+
+#define SCI_CHECK_ARG(cond, ...)                                   \
+    do {                                                           \
+        if (!(cond)) {                                             \
+            ::sci::set_error(__VA_ARGS__);                         \
+            return SCI_ERR_INVALID_ARG;                            \
+        }                                                          \
+    } while (0)
+
+#define SCI_CUDA(call)                                             \
+    do {                                                           \
+        cudaError_t _e = (call);                                   \
+        if (_e != cudaSuccess) return ::sci::cuda_status(_e, #call); \
+    } while (0)
+
+#define SCI_LAUNCHED(name) SCI_CUDA(cudaGetLastError())
+
+inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s); }
+
+inline bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
+
+constexpr int kSMs = 152;  // GB300: 2 dies x 76 SMs
+
+// ------------------------------------------------------------- device side
+__device__ __forceinline__ float4 ldg4(const float *p) {
+    return __ldg(reinterpret_cast<const float4 *>(p));
+}
+__device__ __forceinline__ void st4(float *p, float4 v) {
+    *reinterpret_cast<float4 *>(p) = v;
+}
+// streaming store (written once, not re-read by this kernel)
+__device__ __forceinline__ void st4_cs(float *p, float4 v) {
+    __stcs(reinterpret_cast<float4 *>(p), v);
+}
+
+__device__ __forceinline__ float sqrt_approx(float x) {
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
+// ---- packed FP32 pairs (sm_100+ f32x2 arithmetic) --------------------
+// A float2 is held as one 64-bit register pair; add/sub/mul/fma on both
+// halves issue as one instruction.
+struct f2 {
+    unsigned long long v;
+};
+__device__ __forceinline__ f2 mk2(float a, float b) {
+    f2 r;
+    asm("mov.b64 %0, {%1,%2};" : "=l"(r.v) : "f"(a), "f"(b));
+    return r;
+}
+__device__ __forceinline__ float lo(f2 a) {
+    float x, y;
+    asm("mov.b64 {%0,%1}, %2;" : "=f"(x), "=f"(y) : "l"(a.v));
+    return x;
+}
+__device__ __forceinline__ float hi(f2 a) {
+    float x, y;
+    asm("mov.b64 {%0,%1}, %2;" : "=f"(x), "=f"(y) : "l"(a.v));
+    return y;
+}
+__device__ __forceinline__ f2 add2(f2 a, f2 b) {
+    f2 r;
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
+__device__ __forceinline__ f2 sub2(f2 a, f2 b) {
+    f2 r;
+    asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
+__device__ __forceinline__ f2 mul2(f2 a, f2 b) {
+    f2 r;
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(r.v) : "l"(a.v), "l"(b.v));
+    return r;
+}
+__device__ __forceinline__ f2 fma2(f2 a, f2 b, f2 c) {
+    f2 r;
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(r.v) : "l"(a.v), "l"(b.v), "l"(c.v));
+    return r;
+}
+
+}  // namespace sci

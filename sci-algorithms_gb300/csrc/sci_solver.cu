@@ -1,0 +1,288 @@
+// GAP-TV / ADMM-TV iteration loops (PnP_SCI/python/pnp_sci_algo.py:536-706
+// and :708-864 for denoiser='tv') as a native runtime: the whole loop is
+// enqueued on one stream -- per iteration one fused projection kernel, one
+// TV pass and its stop-test launch -- and, with use_graph, captured once into
+// a CUDA graph that is cached per argument set and replayed with a single
+// launch.
+#include <cstring>
+#include <list>
+#include <mutex>
+#include <string>
+#include <utility>
+
+#include "sci_common.cuh"
+
+namespace sci {
+
+int tv_launch(const float *f, float *u, float *resid, int64_t nf, int64_t H, int64_t W,
+              int64_t fs, float weight, float eps, int K, int *steps, double *energy_out,
+              void *workspace, size_t ws_bytes, cudaStream_t s, int force_R);
+size_t tv_workspace_bytes(int64_t nf, int64_t H, int64_t W, int K);
+
+namespace {
+
+struct SolverWs {
+    float *y1, *xp, *theta, *v, *b0, *b1;
+    void *tv;
+    size_t tv_bytes;
+};
+
+size_t round256(size_t b) { return (b + 255) & ~size_t(255); }
+
+size_t solver_layout(bool admm, int64_t B, int64_t H, int64_t W, int K, SolverWs *w,
+                     char *base) {
+    const size_t hw = (size_t)(H * W), n = (size_t)B * hw;
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        size_t o = off;
+        off += round256(bytes);
+        return o;
+    };
+    size_t oy1 = 0, oxp = 0, oth = 0, ov = 0, ob0 = 0, ob1 = 0;
+    if (!admm) {
+        oy1 = take(sizeof(float) * hw);
+        oxp = take(sizeof(float) * n);
+    } else {
+        oth = take(sizeof(float) * n);
+        ov = take(sizeof(float) * n);
+        ob0 = take(sizeof(float) * n);
+        ob1 = take(sizeof(float) * n);
+    }
+    const size_t tvb = tv_workspace_bytes(B, H, W, K);
+    const size_t otv = take(tvb);
+    if (w) {
+        w->y1 = admm ? nullptr : reinterpret_cast<float *>(base + oy1);
+        w->xp = admm ? nullptr : reinterpret_cast<float *>(base + oxp);
+        w->theta = admm ? reinterpret_cast<float *>(base + oth) : nullptr;
+        w->v = admm ? reinterpret_cast<float *>(base + ov) : nullptr;
+        w->b0 = admm ? reinterpret_cast<float *>(base + ob0) : nullptr;
+        w->b1 = admm ? reinterpret_cast<float *>(base + ob1) : nullptr;
+        w->tv = base + otv;
+        w->tv_bytes = tvb;
+    }
+    return off;
+}
+
+// ------------------------------------------------------------ graph cache
+struct GraphCache {
+    std::mutex mu;
+    std::list<std::pair<std::string, cudaGraphExec_t>> entries;  // most recent first
+    static constexpr size_t kMax = 16;
+
+    cudaGraphExec_t find(const std::string &key) {
+        for (auto it = entries.begin(); it != entries.end(); ++it)
+            if (it->first == key) {
+                entries.splice(entries.begin(), entries, it);
+                return entries.front().second;
+            }
+        return nullptr;
+    }
+    void put(const std::string &key, cudaGraphExec_t g) {
+        entries.emplace_front(key, g);
+        while (entries.size() > kMax) {
+            cudaGraphExecDestroy(entries.back().second);
+            entries.pop_back();
+        }
+    }
+};
+GraphCache &graph_cache() {
+    static GraphCache c;
+    return c;
+}
+
+template <typename T>
+void put_bytes(std::string &k, const T &v) {
+    k.append(reinterpret_cast<const char *>(&v), sizeof(T));
+}
+
+struct Args {
+    bool admm;
+    const float *y, *phi;
+    const uint32_t *bits;
+    const float *phisum, *x0;
+    float *x_out;
+    int64_t B, H, W;
+    sci_solve_opts o;
+    void *ws;
+    size_t ws_bytes;
+
+    std::string key() const {
+        std::string k;
+        put_bytes(k, admm);
+        put_bytes(k, y);
+        put_bytes(k, phi);
+        put_bytes(k, bits);
+        put_bytes(k, phisum);
+        put_bytes(k, x0);
+        put_bytes(k, x_out);
+        put_bytes(k, B);
+        put_bytes(k, H);
+        put_bytes(k, W);
+        put_bytes(k, o.iters);
+        put_bytes(k, o.tv_iter_max);
+        put_bytes(k, o.eps);
+        put_bytes(k, o.accelerate);
+        put_bytes(k, o.gamma);
+        put_bytes(k, o.orig);
+        put_bytes(k, o.sqerr);
+        put_bytes(k, o.tv_steps);
+        put_bytes(k, ws);
+        k.append(reinterpret_cast<const char *>(o.lambdas), sizeof(float) * o.iters);
+        k.append(reinterpret_cast<const char *>(o.weights), sizeof(float) * o.iters);
+        put_bytes(k, o.gammas != nullptr);
+        if (o.gammas) k.append(reinterpret_cast<const char *>(o.gammas), sizeof(float) * o.iters);
+        return k;
+    }
+};
+
+// Enqueues the whole solve on stream s.
+int enqueue(const Args &a, cudaStream_t s) {
+    const sci_solve_opts &o = a.o;
+    const int64_t B = a.B, H = a.H, W = a.W, hw = H * W, n = B * hw;
+    const int K = o.tv_iter_max;
+    SolverWs w;
+    solver_layout(a.admm, B, H, W, K, &w, static_cast<char *>(a.ws));
+    if (o.sqerr) SCI_CUDA(cudaMemsetAsync(o.sqerr, 0, sizeof(double) * o.iters, s));
+    if (!a.admm) {
+        // gap_denoise: x = x0; y1 = 0  (pnp_sci_algo.py:633-635)
+        if (a.x0 != a.x_out)
+            SCI_CUDA(cudaMemcpyAsync(a.x_out, a.x0, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+        if (o.accelerate) SCI_CUDA(cudaMemsetAsync(w.y1, 0, sizeof(float) * hw, s));
+        for (int it = 0; it < o.iters; ++it) {
+            int e = sci_proj_gap(a.x_out, a.phi, a.bits, a.y, w.y1, a.phisum, w.xp, o.lambdas[it],
+                                 o.accelerate, B, H, W, s);
+            if (e) return e;
+            e = tv_launch(w.xp, a.x_out, nullptr, B, H, W, hw, o.weights[it], o.eps, K,
+                          o.tv_steps ? o.tv_steps + (int64_t)it * B : nullptr, nullptr, w.tv,
+                          w.tv_bytes, s, 0);
+            if (e) return e;
+            if (o.orig && o.sqerr) {
+                e = sci_sqerr_accum(o.orig, a.x_out, n, o.sqerr + it, s);
+                if (e) return e;
+            }
+        }
+        return SCI_OK;
+    }
+    // admm_denoise: theta = x0, b = 0  (pnp_sci_algo.py:800-802)
+    SCI_CUDA(cudaMemcpyAsync(w.theta, a.x0, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+    SCI_CUDA(cudaMemsetAsync(w.b0, 0, sizeof(float) * n, s));
+    float *bcur = w.b0, *bnext = w.b1;
+    for (int it = 0; it < o.iters; ++it) {
+        const bool want_x = (it == o.iters - 1) || (o.orig && o.sqerr);
+        const float gamma = o.gammas ? o.gammas[it] : o.gamma;
+        int e = sci_proj_admm(w.theta, bcur, a.phi, a.bits, a.y, a.phisum, w.v,
+                              want_x ? a.x_out : nullptr, o.lambdas[it], gamma, B, H, W, s);
+        if (e) return e;
+        // theta = TV(x - b);  b = b - (x - theta) = theta - v
+        e = tv_launch(w.v, w.theta, bnext, B, H, W, hw, o.weights[it], o.eps, K,
+                      o.tv_steps ? o.tv_steps + (int64_t)it * B : nullptr, nullptr, w.tv,
+                      w.tv_bytes, s, 0);
+        if (e) return e;
+        if (o.orig && o.sqerr) {
+            e = sci_sqerr_accum(o.orig, a.x_out, n, o.sqerr + it, s);
+            if (e) return e;
+        }
+        std::swap(bcur, bnext);
+    }
+    return SCI_OK;
+}
+
+int solve(const Args &a, void *stream) {
+    const sci_solve_opts &o = a.o;
+    SCI_CHECK_ARG(a.B >= 1 && a.H >= 1 && a.W >= 1, "solver: invalid sizes");
+    SCI_CHECK_ARG(a.y && a.phisum && a.x0 && a.x_out && (a.phi || a.bits),
+                  "solver: null pointer");
+    SCI_CHECK_ARG(!a.bits || a.B <= 32, "solver: packed mask needs B <= 32");
+    SCI_CHECK_ARG(o.iters >= 0 && o.tv_iter_max >= 1, "solver: iters >= 0, tv_iter_max >= 1");
+    SCI_CHECK_ARG(o.iters == 0 || (o.lambdas && o.weights), "solver: schedules missing");
+    for (int i = 0; i < o.iters; ++i)
+        SCI_CHECK_ARG(o.weights[i] > 0.f, "solver: tv_weight[%d] = %g must be > 0", i,
+                      (double)o.weights[i]);
+    const size_t need = solver_layout(a.admm, a.B, a.H, a.W, o.tv_iter_max, nullptr, nullptr);
+    SCI_CHECK_ARG(a.ws && a.ws_bytes >= need, "solver: workspace of %zu bytes needed, got %zu",
+                  need, a.ws_bytes);
+    cudaStream_t s = as_stream(stream);
+    if (o.iters == 0) {
+        if (a.x0 != a.x_out)
+            SCI_CUDA(cudaMemcpyAsync(a.x_out, a.x0, sizeof(float) * a.B * a.H * a.W,
+                                     cudaMemcpyDeviceToDevice, s));
+        return SCI_OK;
+    }
+    if (!o.use_graph) return enqueue(a, s);
+
+    GraphCache &gc = graph_cache();
+    const std::string key = a.key();
+    {
+        std::lock_guard<std::mutex> lk(gc.mu);
+        if (cudaGraphExec_t g = gc.find(key)) {
+            SCI_CUDA(cudaGraphLaunch(g, s));
+            return SCI_OK;
+        }
+    }
+    // capture on a private stream, then replay on the caller's stream
+    cudaStream_t cs;
+    SCI_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaError_t ce = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (ce != cudaSuccess) {
+        cudaStreamDestroy(cs);
+        return cuda_status(ce, "cudaStreamBeginCapture");
+    }
+    const int e = enqueue(a, cs);
+    cudaGraph_t graph = nullptr;
+    ce = cudaStreamEndCapture(cs, &graph);
+    cudaStreamDestroy(cs);
+    if (e) {
+        if (graph) cudaGraphDestroy(graph);
+        return e;
+    }
+    if (ce != cudaSuccess) return cuda_status(ce, "cudaStreamEndCapture");
+    cudaGraphExec_t exec = nullptr;
+    ce = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) return cuda_status(ce, "cudaGraphInstantiate");
+    {
+        std::lock_guard<std::mutex> lk(gc.mu);
+        gc.put(key, exec);
+    }
+    SCI_CUDA(cudaGraphLaunch(exec, s));
+    return SCI_OK;
+}
+
+}  // namespace
+}  // namespace sci
+
+using namespace sci;
+
+extern "C" {
+
+int sci_solver_workspace_bytes(int64_t B, int64_t H, int64_t W, const sci_solve_opts *opts,
+                               size_t *bytes) {
+    SCI_CHECK_ARG(opts && bytes && B >= 1 && H >= 1 && W >= 1 && opts->tv_iter_max >= 1,
+                  "sci_solver_workspace_bytes: bad argument");
+    const size_t g = solver_layout(false, B, H, W, opts->tv_iter_max, nullptr, nullptr);
+    const size_t a = solver_layout(true, B, H, W, opts->tv_iter_max, nullptr, nullptr);
+    *bytes = g > a ? g : a;
+    return SCI_OK;
+}
+
+int sci_gap_tv(const float *y, const float *phi, const uint32_t *mask_bits, const float *phisum,
+               const float *x0, float *x_out, int64_t B, int64_t H, int64_t W,
+               const sci_solve_opts *opts, void *workspace, size_t workspace_bytes,
+               void *stream) {
+    SCI_CHECK_ARG(opts, "sci_gap_tv: opts is NULL");
+    Args a{false, y, phi, mask_bits, phisum, x0, x_out, B, H, W, *opts, workspace,
+           workspace_bytes};
+    return solve(a, stream);
+}
+
+int sci_admm_tv(const float *y, const float *phi, const uint32_t *mask_bits, const float *phisum,
+                const float *x0, float *x_out, int64_t B, int64_t H, int64_t W,
+                const sci_solve_opts *opts, void *workspace, size_t workspace_bytes,
+                void *stream) {
+    SCI_CHECK_ARG(opts, "sci_admm_tv: opts is NULL");
+    Args a{true, y, phi, mask_bits, phisum, x0, x_out, B, H, W, *opts, workspace,
+           workspace_bytes};
+    return solve(a, stream);
+}
+
+}  // extern "C"

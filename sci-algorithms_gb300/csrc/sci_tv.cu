@@ -1,0 +1,168 @@
+// Host driver of the Chambolle TV (all passes of one call) and its C ABI.
+// The kernels are in sci_tv.cuh (instantiated in sci_tv_k4.cu,
+// sci_tv_k123.cu and sci_tv_fix.cu).
+#include "sci_tv.cuh"
+
+namespace sci {
+namespace tv {
+
+__global__ void k_init_done(int *done, int *steps, int K, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        done[i] = -1;
+        if (steps) steps[i] = K;
+    }
+}
+
+__global__ void k_copy_frames(const float *f, float *u, float *resid, int64_t n, int *steps,
+                              int nf) {
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n;
+         i += (int64_t)gridDim.x * blockDim.x) {
+        u[i] = f[i];
+        if (resid) resid[i] = 0.f;
+        if (steps && i < nf) steps[i] = 1;
+    }
+}
+
+static inline int round4(int v) { return (v + 3) & ~3; }
+
+struct Workspace {
+    double *energy;  // [nf][K][2]
+    int *done;       // [nf]
+    float *pa, *pb;  // [nf][2][H][W] each (multi-pass only)
+};
+
+static size_t ws_layout(int64_t nf, int64_t H, int64_t W, int K, Workspace *w, char *base) {
+    size_t off = 0;
+    auto take = [&](size_t bytes) {
+        size_t o = off;
+        off += (bytes + 255) & ~size_t(255);
+        return o;
+    };
+    const size_t oe = take(sizeof(double) * (size_t)(nf * K * 2));
+    const size_t od = take(sizeof(int) * (size_t)nf);
+    size_t opa = 0, opb = 0;
+    if (K - 1 > SMAX) {
+        opa = take(sizeof(float) * (size_t)(nf * 2 * H * W));
+        opb = take(sizeof(float) * (size_t)(nf * 2 * H * W));
+    }
+    if (w) {
+        w->energy = reinterpret_cast<double *>(base + oe);
+        w->done = reinterpret_cast<int *>(base + od);
+        w->pa = (K - 1 > SMAX) ? reinterpret_cast<float *>(base + opa) : nullptr;
+        w->pb = (K - 1 > SMAX) ? reinterpret_cast<float *>(base + opb) : nullptr;
+    }
+    return off;
+}
+
+// Chooses rows per chunk so that the grid fills the GPU about twice.
+static int choose_R(int64_t nf, int nbands, int H) {
+    const int64_t want = (int64_t)kSMs * 16 * 2;  // warps
+    int R = 256;
+    while (R > 32 && nf * nbands * ((H + R - 1) / R) < want) R >>= 1;
+    return R;
+}
+
+}  // namespace tv
+
+// Host driver: all passes of one TV call.  Used by the C ABI and the solvers.
+int tv_launch(const float *f, float *u, float *resid, int64_t nf, int64_t H, int64_t W,
+              int64_t fs, float weight, float eps, int K, int *steps, double *energy_out,
+              void *workspace, size_t ws_bytes, cudaStream_t s, int force_R) {
+    using namespace tv;
+    SCI_CHECK_ARG(f && u && nf >= 1 && H >= 1 && W >= 1, "tv: bad arguments");
+    SCI_CHECK_ARG(K >= 1, "tv: n_iter_max must be >= 1");
+    SCI_CHECK_ARG(weight > 0.f, "tv: weight must be > 0 (got %g)", (double)weight);
+    SCI_CHECK_ARG(f != u, "tv: input and output must not alias");
+    SCI_CHECK_ARG(H <= (1 << 30) && W <= (1 << 30) && nf <= (1 << 30), "tv: sizes too large");
+    const size_t need = ws_layout(nf, H, W, K, nullptr, nullptr);
+    SCI_CHECK_ARG(workspace && ws_bytes >= need, "tv: workspace of %zu bytes needed, got %zu",
+                  need, ws_bytes);
+    if (K == 1) {
+        k_copy_frames<<<(unsigned)std::min<int64_t>((nf * fs + 255) / 256, kSMs * 16), 256, 0, s>>>(
+            f, u, resid, nf * fs, steps, (int)nf);
+        SCI_LAUNCHED("k_copy_frames");
+        return SCI_OK;
+    }
+    Workspace w;
+    ws_layout(nf, H, W, K, &w, static_cast<char *>(workspace));
+    double *energy = energy_out ? energy_out : w.energy;
+    SCI_CUDA(cudaMemsetAsync(energy, 0, sizeof(double) * (size_t)(nf * K * 2), s));
+    k_init_done<<<(unsigned)((nf + 255) / 256), 256, 0, s>>>(w.done, steps, K, (int)nf);
+    SCI_LAUNCHED("k_init_done");
+
+    const bool vec = (W % 4 == 0) && (fs % 4 == 0) && aligned16(f) && aligned16(u) &&
+                     (!resid || aligned16(resid));
+    const int U = K - 1;  // dual updates
+    const float *pin = nullptr;
+    float *pbuf[2] = {w.pa, w.pb};
+    int pi = 0;
+    for (int a = 0; a < U; a += SMAX) {
+        const int SG = std::min(SMAX, U - a);
+        const bool PIN = a > 0, FINAL = (a + SG == U);
+        Pass P{};
+        P.f = f;
+        P.u = u;
+        P.resid = resid;
+        P.p_in = pin;
+        P.p_out = FINAL ? nullptr : pbuf[pi];
+        P.energy = energy;
+        P.done = w.done;
+        P.steps = steps;
+        P.fs = fs;
+        P.nf = (int)nf;
+        P.H = (int)H;
+        P.W = (int)W;
+        P.K = K;
+        P.a = a;
+        P.tau = 0.25f;
+        P.tw = 0.25f / weight;
+        P.weight = weight;
+        P.eps = eps;
+        P.hl = round4(SG + (PIN ? 1 : 0));
+        P.own = BANDW - P.hl - round4(SG);
+        P.ht = SG + (PIN ? 1 : 0);
+        P.nbands = (int)((W + P.own - 1) / P.own);
+        P.R = force_R > 0 ? force_R : choose_R(nf, P.nbands, (int)H);
+        P.nchunks = (int)((H + P.R - 1) / P.R);
+        P.S = SG;
+        P.vec = vec ? 1 : 0;
+        if (SG == SMAX) launch_main4(P, PIN, FINAL, s);
+        else launch_main123(P, SG, PIN, s);
+        SCI_LAUNCHED("k_tv_main");
+        // the stop test can change the result only when a step k in
+        // [1, K-2] lies in this pass's window
+        if (std::max(1, a) <= std::min(a + SG - 1, K - 2)) {
+            launch_fixup(P, PIN, s);
+            SCI_LAUNCHED("k_tv_fixup");
+        }
+        pin = P.p_out;
+        pi ^= 1;
+    }
+    return SCI_OK;
+}
+
+size_t tv_workspace_bytes(int64_t nf, int64_t H, int64_t W, int K) {
+    return tv::ws_layout(nf, H, W, K, nullptr, nullptr);
+}
+
+}  // namespace sci
+
+extern "C" {
+
+int sci_tv_workspace_bytes(int64_t nframes, int64_t H, int64_t W, int n_iter_max,
+                           size_t *bytes) {
+    SCI_CHECK_ARG(bytes && nframes >= 1 && H >= 1 && W >= 1 && n_iter_max >= 1,
+                  "sci_tv_workspace_bytes: bad argument");
+    *bytes = sci::tv_workspace_bytes(nframes, H, W, n_iter_max);
+    return SCI_OK;
+}
+
+int sci_tv_chambolle(const float *f, float *u, float *resid, int64_t nframes, int64_t H,
+                     int64_t W, float weight, float eps, int n_iter_max, int *steps,
+                     double *energy, void *workspace, size_t workspace_bytes, void *stream) {
+    return sci::tv_launch(f, u, resid, nframes, H, W, H * W, weight, eps, n_iter_max, steps,
+                          energy, workspace, workspace_bytes, sci::as_stream(stream), 0);
+}
+
+}  // extern "C"

@@ -1,0 +1,109 @@
+"""C-ABI library: loads, exports every declared symbol, validates arguments
+(all without touching a GPU)."""
+import ctypes
+import os
+import re
+
+import numpy as np
+import pytest
+
+import sci_algorithms_gb300 as sci
+from sci_algorithms_gb300 import _lib, _dev
+
+REPO = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_symbols():
+    txt = open(os.path.join(REPO, "include", "sci_gb300.h")).read()
+    return sorted(set(re.findall(r"^int\s+(sci_\w+)\s*\(", txt, flags=re.M)))
+
+
+@pytest.fixture(scope="module")
+def L():
+    sci.build()
+    return _lib.load()
+
+
+def test_library_exports_every_declared_symbol(L):
+    declared = header_symbols()
+    assert len(declared) >= 14
+    for name in declared:
+        assert hasattr(L, name), name
+    assert sorted(_lib.exported_symbols()) == declared
+
+
+def test_version_and_error_buffer(L):
+    assert L.sci_version() >= 100
+    buf = ctypes.create_string_buffer(8)
+    n = L.sci_last_error(buf, len(buf))
+    assert n >= 0
+
+
+def test_argument_checks_return_codes_without_gpu(L):
+    s = None
+    assert L.sci_A(None, None, None, 8, 16, 16, s) == -1
+    assert "null pointer" in _lib.last_error()
+    assert L.sci_A(None, None, None, 0, 16, 16, s) == -1
+    assert "invalid sizes" in _lib.last_error()
+    assert L.sci_pack_mask(1, 1, 1, 33, 4, 4, s) == -1
+    assert "B=33" in _lib.last_error()
+    # proj_gap with accelerate but no y1
+    assert L.sci_proj_gap(1, 1, None, 1, None, 1, 2, ctypes.c_float(1.0), 1, 8, 4, 4, s) == -1
+    assert "y1" in _lib.last_error()
+    # aliasing is rejected
+    assert L.sci_proj_gap(1, 1, None, 1, 1, 1, 1, ctypes.c_float(1.0), 1, 8, 4, 4, s) == -1
+    # TV: weight must be positive; workspace must be large enough
+    n = ctypes.c_size_t()
+    assert L.sci_tv_workspace_bytes(4, 64, 64, 5, ctypes.byref(n)) == 0 and n.value > 0
+    assert L.sci_tv_chambolle(1, 2, None, 4, 64, 64, ctypes.c_float(0.0), ctypes.c_float(2e-4),
+                              5, None, None, 3, n.value, s) == -1
+    assert "weight" in _lib.last_error()
+    assert L.sci_tv_chambolle(1, 2, None, 4, 64, 64, ctypes.c_float(0.1), ctypes.c_float(2e-4),
+                              5, None, None, 3, n.value - 1, s) == -1
+    assert "workspace" in _lib.last_error()
+
+
+def test_workspace_sizes_scale():
+    L = _lib.load()
+    n5, n30 = ctypes.c_size_t(), ctypes.c_size_t()
+    L.sci_tv_workspace_bytes(24, 2048, 2048, 5, ctypes.byref(n5))
+    L.sci_tv_workspace_bytes(24, 2048, 2048, 30, ctypes.byref(n30))
+    # a single pass keeps p on chip: only energies and flags
+    assert n5.value < 1 << 16
+    # multi-pass runs carry p (2 planes, two buffers) through the workspace
+    assert n30.value >= 2 * 2 * 24 * 2048 * 2048 * 4
+    o = _lib.SolveOpts()
+    o.tv_iter_max = 5
+    nb = ctypes.c_size_t()
+    assert L.sci_solver_workspace_bytes(24, 2048, 2048, ctypes.byref(o), ctypes.byref(nb)) == 0
+    # ADMM keeps theta, v and two b buffers: 4 stacks
+    assert nb.value >= 4 * 24 * 2048 * 2048 * 4
+
+
+def test_schedule_and_layout_helpers():
+    assert np.array_equal(_dev.schedule(0.5, 3), np.full(3, 0.5, np.float32))
+    assert _dev.schedule([1, 2, 3], 3).dtype == np.float32
+    with pytest.raises(ValueError):
+        _dev.schedule([1, 2], 3)
+    from sci_algorithms_gb300.pnp_sci_algo import _total_iters, _check_plugin, _flip
+    assert _total_iters(50, None) == 50
+    assert _total_iters([10, 10, 5], [1, 2, 3]) == 25
+    with pytest.raises(ValueError):
+        _check_plugin("ffdnet")
+    with pytest.raises(ValueError):
+        _check_plugin("tv", "ATV_ClipA")
+    assert _flip("updown", 1) and not _flip("updown", 0)
+    assert _flip("downup", 0) and not _flip("plain", 1)
+
+
+def test_unsupported_projmeth_raises():
+    with pytest.raises(ValueError):
+        sci.admmdenoise_cacti(np.zeros((4, 4, 1)), np.zeros((4, 4, 2)), None, None,
+                              projmeth="ista")
+
+
+def test_no_gpu_fails_loudly(monkeypatch):
+    import torch
+    monkeypatch.setattr(torch.cuda, "is_available", lambda: False)
+    with pytest.raises(RuntimeError, match="CUDA GPU"):
+        sci.A_(np.zeros((4, 4, 2)), np.ones((4, 4, 2)))
