@@ -289,6 +289,46 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
+def run_kernel(args):
+    """Single-kernel mode for profiling: a few launches of one kernel on a
+    2048 x 2048 x F stack (small enough for an ncu capture)."""
+    import torch
+    import sci_algorithms_gb300 as sci
+    from sci_algorithms_gb300 import _dev
+    from sci_algorithms_gb300._lib import call
+    dev = _dev.device()
+    F = args.frames
+    orig, mask, meas = sci.datasets.video_config(H, W, F, noise_rel=0.01)
+    op = sci.MaskOperator(mask)
+    x = _dev.planar(orig)
+    out = torch.empty_like(x)
+    y = _dev.plane(meas)
+    y1 = torch.zeros_like(y)
+    ws = sci.tv.tv_workspace(F, H, W, TV_ITERS, dev)
+    s = torch.cuda.current_stream()
+
+    def tv_once():
+        call("sci_tv_chambolle", x.data_ptr(), out.data_ptr(), None, F, H, W, 0.1, 2e-4,
+             TV_ITERS, None, None, ws.data_ptr(), ws.numel(), s.cuda_stream)
+
+    def proj_once():
+        call("sci_proj_gap", x.data_ptr(), None, op.bits.data_ptr(), y.data_ptr(),
+             y1.data_ptr(), op.phisum.data_ptr(), out.data_ptr(), 1.0, 1, F, H, W,
+             s.cuda_stream)
+
+    fn = {"tv": tv_once, "proj": proj_once}[args.kernel]
+    fn()
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(args.launches):
+        fn()
+    e1.record(s)
+    torch.cuda.synchronize()
+    print(json.dumps({"kernel": args.kernel, "frames": F, "H": H, "W": W,
+                      "ms_per_launch": e0.elapsed_time(e1) / args.launches}))
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -297,7 +337,13 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--ref-crop", type=int, default=1024)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--kernel", choices=["tv", "proj"], default=None,
+                    help="profiling mode: time one kernel on a 2048x2048xFRAMES stack")
+    ap.add_argument("--frames", type=int, default=8)
+    ap.add_argument("--launches", type=int, default=3)
     args = ap.parse_args()
+    if args.kernel:
+        return run_kernel(args)
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":

@@ -101,8 +101,9 @@ int sci_tv_workspace_bytes(int64_t nframes, int64_t H, int64_t W,
  * frames: u = TV(f).  resid (nullable) receives u - f (the ADMM multiplier
  * update b = theta - v).  steps (nullable, device int[nframes]) receives
  * the number of executed Chambolle steps per frame.  energy (nullable,
- * device double[nframes * n_iter_max * 2]) receives per-frame sums
- * (sum (div p_k)^2, sum |grad u_k|) of the steps it evaluates.
+ * device double[nframes * n_iter_max * 2]) receives, for every step k the
+ * stop test evaluates, H*W*E_k = sum (div p_k)^2 + weight * sum |grad u_k|
+ * in energy[(f*n_iter_max + k)*2] (the odd entries stay 0).
  * Replaces denoise_tv_chambolle(x, weight, n_iter_max, multichannel=True)
  * as called at PnP_SCI/python/pnp_sci_algo.py:650 and :812-813. */
 int sci_tv_chambolle(const float *f, float *u, float *resid, int64_t nframes,
@@ -153,6 +154,68 @@ int sci_admm_tv(const float *y, const float *phi, const uint32_t *mask_bits,
                 const float *phisum, const float *x0, float *x_out,
                 int64_t B, int64_t H, int64_t W, const sci_solve_opts *opts,
                 void *workspace, size_t workspace_bytes, void *stream);
+
+/* ------------------------------------------- spectral (CASSI) operators (K3) */
+/* Single coded aperture phi (H x W) followed by a dispersion that shifts
+ * band b by step*b pixels along W onto an H x Wd detector,
+ * Wd = W + step*(L-1).  No Python counterpart in the reference; the
+ * MATLAB CASSI test uses the same model with a pre-shifted mask and
+ * Phisum = sum(mask.^2, 3) (DeSCI/test_desci_cassi.m:58-62). */
+
+/* y[h, w + step b] += phi[h, w] x_b[h, w]   (x: L x H x W, y: H x Wd) */
+int sci_cassi_A(const float *x, const float *phi, float *y, int64_t L,
+                int64_t H, int64_t W, int step, void *stream);
+
+/* x_b[h, w] = phi[h, w] y[h, w + step b]    (the transposed unshift) */
+int sci_cassi_At(const float *y, const float *phi, float *x, int64_t L,
+                 int64_t H, int64_t W, int step, void *stream);
+
+/* phisum[h, w'] = sum_b phi[h, w' - step b]^2, zeros -> 1 when guard_zero */
+int sci_cassi_phisum(const float *phi, float *phisum, int64_t L, int64_t H,
+                     int64_t W, int step, int guard_zero, void *stream);
+
+int sci_cassi_workspace_bytes(int64_t L, int64_t H, int64_t W, int step,
+                              int tv_iter_max, size_t *bytes);
+
+/* GAP-TV with the CASSI operators (gap_denoise, pnp_sci_algo.py:536-706,
+ * with A/At = the operators above; per-band Chambolle TV).  Uses
+ * opts->iters, lambdas, weights, tv_iter_max, eps, accelerate, orig,
+ * sqerr, tv_steps. */
+int sci_cassi_gap_tv(const float *y, const float *phi, const float *phisum,
+                     const float *x0, float *x_out, int64_t L, int64_t H,
+                     int64_t W, int step, const sci_solve_opts *opts,
+                     void *workspace, size_t workspace_bytes, void *stream);
+
+/* ------------------------------- differentiable unrolled GAP-TV (K4) */
+/* A batch of N scenes x_true (N x B x H x W) sharing one learnable mask
+ * Phi = sigmoid(logits) (B x H x W) and per-iteration step sizes
+ * lambdas (device float[K]):  y = A(x_true), x^0 = At(y / Phi_sum), then K
+ * accelerated GAP iterations (pnp_sci_algo.py:641-643) each followed by a
+ * fixed tv_iters-step Chambolle TV (no stop test), weight tv_weight;
+ * loss = mean (x^K - x_true)^2.  No reference counterpart: the reference's
+ * solvers are not differentiable; this is the unrolled form of its
+ * gap_denoise loop. */
+
+int sci_unrolled_workspace_bytes(int64_t N, int64_t B, int64_t H, int64_t W,
+                                 int K, int tv_iters, size_t *bytes);
+
+/* Forward: writes *loss = sum (x^K - x_true)^2 (device double; divide by
+ * N*B*H*W for the mean) and, when x_out is non-NULL, x^K.
+ * Keeps the outer iterates in the workspace for sci_unrolled_bwd. */
+int sci_unrolled_fwd(const float *logits, const float *lambdas,
+                     const float *x_true, int64_t N, int64_t B, int64_t H,
+                     int64_t W, int K, int tv_iters, float tv_weight,
+                     double *loss, float *x_out, void *workspace,
+                     size_t workspace_bytes, void *stream);
+
+/* Reverse pass of the preceding sci_unrolled_fwd on the same workspace and
+ * arguments: grad_logits (B x H x W) and grad_lambdas (device double[K])
+ * of grad_loss * loss.  Recomputes each TV call from its checkpoint. */
+int sci_unrolled_bwd(const float *logits, const float *lambdas,
+                     const float *x_true, int64_t N, int64_t B, int64_t H,
+                     int64_t W, int K, int tv_iters, float tv_weight,
+                     float grad_loss, float *grad_logits, double *grad_lambdas,
+                     void *workspace, size_t workspace_bytes, void *stream);
 
 #ifdef __cplusplus
 }

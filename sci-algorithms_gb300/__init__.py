@@ -13,4 +13,7 @@ from .tv import denoise_tv_chambolle, tv_frames  # noqa: F401
 from .pnp_sci_algo import (admmdenoise_cacti, gap_denoise, admm_denoise,  # noqa: F401
                            GAP_TV_rec, ADMM_TV_rec)
 from .solver import Solver  # noqa: F401
+from .cassi import CassiOperator, CassiSolver, make_cassi_ops  # noqa: F401
+from .unrolled import (UnrolledGapTV, unrolled_loss, unrolled_workspace,  # noqa: F401
+                       torch_unrolled_loss)
 from . import datasets  # noqa: F401

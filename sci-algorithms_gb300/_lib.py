@@ -64,6 +64,19 @@ _SIGS = {
                    ctypes.POINTER(SolveOpts), c_vp, c_sz, c_vp],
     "sci_admm_tv": [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_i64, c_i64,
                     ctypes.POINTER(SolveOpts), c_vp, c_sz, c_vp],
+    "sci_cassi_A": [c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, ctypes.c_int, c_vp],
+    "sci_cassi_At": [c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, ctypes.c_int, c_vp],
+    "sci_cassi_phisum": [c_vp, c_vp, c_i64, c_i64, c_i64, ctypes.c_int, ctypes.c_int, c_vp],
+    "sci_cassi_workspace_bytes": [c_i64, c_i64, c_i64, ctypes.c_int, ctypes.c_int,
+                                  ctypes.POINTER(c_sz)],
+    "sci_cassi_gap_tv": [c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, ctypes.c_int,
+                         ctypes.POINTER(SolveOpts), c_vp, c_sz, c_vp],
+    "sci_unrolled_workspace_bytes": [c_i64, c_i64, c_i64, c_i64, ctypes.c_int, ctypes.c_int,
+                                     ctypes.POINTER(c_sz)],
+    "sci_unrolled_fwd": [c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_i64, ctypes.c_int,
+                         ctypes.c_int, c_f, c_vp, c_vp, c_vp, c_sz, c_vp],
+    "sci_unrolled_bwd": [c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_i64, ctypes.c_int,
+                         ctypes.c_int, c_f, c_f, c_vp, c_vp, c_vp, c_sz, c_vp],
 }
 
 _lib = None

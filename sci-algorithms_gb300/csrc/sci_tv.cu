@@ -1,6 +1,8 @@
 // Host driver of the Chambolle TV (all passes of one call) and its C ABI.
 // The kernels are in sci_tv.cuh (instantiated in sci_tv_k4.cu,
 // sci_tv_k123.cu and sci_tv_fix.cu).
+#include <cstdlib>
+
 #include "sci_tv.cuh"
 
 namespace sci {
@@ -24,7 +26,7 @@ __global__ void k_copy_frames(const float *f, float *u, float *resid, int64_t n,
     }
 }
 
-static inline int round4(int v) { return (v + 3) & ~3; }
+static inline int round_up(int v, int m) { return (v + m - 1) / m * m; }
 
 struct Workspace {
     double *energy;  // [nf][K][2]
@@ -57,6 +59,10 @@ static size_t ws_layout(int64_t nf, int64_t H, int64_t W, int K, Workspace *w, c
 
 // Chooses rows per chunk so that the grid fills the GPU about twice.
 static int choose_R(int64_t nf, int nbands, int H) {
+    if (const char *e = getenv("SCI_TV_R")) {
+        const int v = atoi(e);
+        if (v >= 8) return v;
+    }
     const int64_t want = (int64_t)kSMs * 16 * 2;  // warps
     int R = 256;
     while (R > 32 && nf * nbands * ((H + R - 1) / R) < want) R >>= 1;
@@ -65,10 +71,25 @@ static int choose_R(int64_t nf, int nbands, int H) {
 
 }  // namespace tv
 
+// Columns per lane: 4 halves the halo overhead of a band (8 of 128 columns
+// instead of 8 of 64) but doubles the registers of the pipeline state; 2
+// keeps ~1.3x more warps resident.  Measured at 2048 x 2048 x 24, 4 is
+// faster (0.44 vs 0.52 ms).  SCI_TV_CPL overrides the choice.
+static int choose_cpl(int64_t W) {
+    if (const char *e = getenv("SCI_TV_CPL")) {
+        const int v = atoi(e);
+        if (v == 2 || v == 4) return v;
+    }
+    return 4;
+}
+
 // Host driver: all passes of one TV call.  Used by the C ABI and the solvers.
-int tv_launch(const float *f, float *u, float *resid, int64_t nf, int64_t H, int64_t W,
-              int64_t fs, float weight, float eps, int K, int *steps, double *energy_out,
-              void *workspace, size_t ws_bytes, cudaStream_t s, int force_R) {
+// flags & 1: run all n_iter_max steps without the stop test (the unrolled,
+// differentiable form).
+int tv_launch_flags(const float *f, float *u, float *resid, int64_t nf, int64_t H, int64_t W,
+                    int64_t fs, float weight, float eps, int K, int *steps, double *energy_out,
+                    void *workspace, size_t ws_bytes, cudaStream_t s, int force_R, int flags) {
+    const bool no_stop = (flags & 1) != 0;
     using namespace tv;
     SCI_CHECK_ARG(f && u && nf >= 1 && H >= 1 && W >= 1, "tv: bad arguments");
     SCI_CHECK_ARG(K >= 1, "tv: n_iter_max must be >= 1");
@@ -88,12 +109,18 @@ int tv_launch(const float *f, float *u, float *resid, int64_t nf, int64_t H, int
     ws_layout(nf, H, W, K, &w, static_cast<char *>(workspace));
     double *energy = energy_out ? energy_out : w.energy;
     SCI_CUDA(cudaMemsetAsync(energy, 0, sizeof(double) * (size_t)(nf * K * 2), s));
-    k_init_done<<<(unsigned)((nf + 255) / 256), 256, 0, s>>>(w.done, steps, K, (int)nf);
-    SCI_LAUNCHED("k_init_done");
-
-    const bool vec = (W % 4 == 0) && (fs % 4 == 0) && aligned16(f) && aligned16(u) &&
-                     (!resid || aligned16(resid));
     const int U = K - 1;  // dual updates
+    // done flags are read only by later passes; steps are written by the
+    // stop-test launch of the last window (K >= 3) or here
+    if (U > SMAX || ((K < 3 || no_stop) && steps)) {
+        k_init_done<<<(unsigned)((nf + 255) / 256), 256, 0, s>>>(w.done, steps, K, (int)nf);
+        SCI_LAUNCHED("k_init_done");
+    }
+
+    const int cpl = choose_cpl(W);
+    const bool vec = (W % cpl == 0) && (fs % cpl == 0) &&
+                     ((reinterpret_cast<uintptr_t>(f) | reinterpret_cast<uintptr_t>(u) |
+                       reinterpret_cast<uintptr_t>(resid)) % (4 * cpl) == 0);
     const float *pin = nullptr;
     float *pbuf[2] = {w.pa, w.pb};
     int pi = 0;
@@ -119,20 +146,27 @@ int tv_launch(const float *f, float *u, float *resid, int64_t nf, int64_t H, int
         P.tw = 0.25f / weight;
         P.weight = weight;
         P.eps = eps;
-        P.hl = round4(SG + (PIN ? 1 : 0));
-        P.own = BANDW - P.hl - round4(SG);
+        P.cpl = cpl;
+        P.hl = round_up(SG + (PIN ? 1 : 0), cpl);
+        P.own = 32 * cpl - P.hl - round_up(SG, cpl);
         P.ht = SG + (PIN ? 1 : 0);
         P.nbands = (int)((W + P.own - 1) / P.own);
         P.R = force_R > 0 ? force_R : choose_R(nf, P.nbands, (int)H);
         P.nchunks = (int)((H + P.R - 1) / P.R);
         P.S = SG;
         P.vec = vec ? 1 : 0;
-        if (SG == SMAX) launch_main4(P, PIN, FINAL, s);
-        else launch_main123(P, SG, PIN, s);
+        const int per_frame_blocks = (P.nbands * P.nchunks + WPB - 1) / WPB;
+        P.gpf = std::max(1, std::min(per_frame_blocks, 16));
+        if (SG == SMAX) {
+            if (cpl == 2) launch_main4_c2(P, PIN, FINAL, s);
+            else launch_main4_c4(P, PIN, FINAL, s);
+        } else {
+            launch_main123(P, SG, PIN, s);
+        }
         SCI_LAUNCHED("k_tv_main");
         // the stop test can change the result only when a step k in
         // [1, K-2] lies in this pass's window
-        if (std::max(1, a) <= std::min(a + SG - 1, K - 2)) {
+        if (!no_stop && std::max(1, a) <= std::min(a + SG - 1, K - 2)) {
             launch_fixup(P, PIN, s);
             SCI_LAUNCHED("k_tv_fixup");
         }
@@ -140,6 +174,13 @@ int tv_launch(const float *f, float *u, float *resid, int64_t nf, int64_t H, int
         pi ^= 1;
     }
     return SCI_OK;
+}
+
+int tv_launch(const float *f, float *u, float *resid, int64_t nf, int64_t H, int64_t W,
+              int64_t fs, float weight, float eps, int K, int *steps, double *energy_out,
+              void *workspace, size_t ws_bytes, cudaStream_t s, int force_R) {
+    return tv_launch_flags(f, u, resid, nf, H, W, fs, weight, eps, K, steps, energy_out,
+                           workspace, ws_bytes, s, force_R, 0);
 }
 
 size_t tv_workspace_bytes(int64_t nf, int64_t H, int64_t W, int K) {

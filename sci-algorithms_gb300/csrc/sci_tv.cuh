@@ -12,15 +12,17 @@
 //   stop after step k >= 1 when |E_{k-1} - E_k| < eps E_0; the result is
 //   u_k of the last executed step (u_{K-1} without an early stop).
 //
-// Mapping.  One warp owns a band of 128 columns (4 per lane, float4 loads
-// along W) of one frame and marches down a chunk of rows.  The K-1 dual
+// Mapping.  One warp owns a band of 32*CPL columns (CPL = 2 or 4 per lane,
+// vector loads along W) of one frame and marches down a chunk of rows.  The K-1 dual
 // updates form a register pipeline: stage k (k = 1..S) handles row r-k when
 // input row r arrives, computing p_k and u_k of that row from stage k-1's
 // rows r-k and r-k+1.  p and div p never leave registers; horizontal
 // neighbours come from warp shuffles; the band overlaps its neighbours by
-// S (+1) halo columns and the chunk by S (+1) halo rows, and a stage reads
-// the input row it needs back from L1.  Per pass the frame is read once and
-// written once: 8 bytes per pixel of HBM traffic.
+// S (+1) halo columns and the chunk by S (+1) halo rows.  Each stage hands
+// its input row down to the next stage, and the next input row is
+// prefetched one step ahead.  Arithmetic on column pairs uses the packed
+// f32x2 instructions.  Per pass the frame is read once and written once:
+// 8 bytes per pixel of HBM traffic.
 //
 // Stop test.  The per-frame energies E_k need whole-frame sums, which a
 // tiled pipeline sees only after every tile has finished.  The pass
@@ -42,8 +44,6 @@
 namespace sci {
 namespace tv {
 
-constexpr int CPL = 4;             // columns per lane
-constexpr int BANDW = 32 * CPL;    // columns per warp band
 constexpr int WPB = 4;             // warps per block
 constexpr int SMAX = 4;            // dual updates per pass
 constexpr unsigned FULL = 0xffffffffu;
@@ -56,7 +56,7 @@ struct Pass {
     float *resid;         // nullable: u - f
     const float *p_in;    // nullable: [nf][2][H][W]  (pr plane, pc plane)
     float *p_out;         // nullable
-    double *energy;       // [nf][K][2]: sum (div p_k)^2, sum |grad u_k|
+    double *energy;       // [nf][K][2]: H*W*E_k in [.][k][0]; [.][k][1] stays 0
     int *done;            // [nf]: stop index j >= 1, or -1
     int *steps;           // nullable [nf]: executed Chambolle steps
     int64_t fs;           // frame stride of f/u/resid (elements)
@@ -66,229 +66,304 @@ struct Pass {
     float weight, eps;
     int nbands, nchunks, R, own, hl, ht;
     int S;                // dual updates of this pass (geometry of the window)
-    int vec;              // 1: rows are 16-byte aligned (float4 path)
+    int vec;              // 1: rows are aligned for CPL-wide vector loads
+    int cpl;              // columns per lane (2 or 4)
+    int gpf;              // stop-test launch: blocks per frame
 };
 
-struct V4 {
-    float x, y, z, w;
-};
-__device__ __forceinline__ V4 v4(float4 a) { return {a.x, a.y, a.z, a.w}; }
-__device__ __forceinline__ float4 f4(V4 a) { return make_float4(a.x, a.y, a.z, a.w); }
-__device__ __forceinline__ V4 zero4() { return {0.f, 0.f, 0.f, 0.f}; }
 
-template <int S>
-struct St {
-    V4 up[S > 0 ? S : 1];  // up[k]: u_k at stage (k+1)'s current row (k = 0..S-1)
-    V4 pr[S + 1];          // pr[k]: p_k (row component) at the row of stage k+1
-    V4 pc[S > 0 ? S : 1];  // pc[k]: p_k (column component) at the row of stage k+1
+// ------------------------------------------------------------ lane vectors
+// CPL consecutive columns of one row held by a lane, as CPL/2 packed pairs.
+template <int CPL>
+struct Row {
+    f2 q[CPL / 2];
 };
 
-template <int MODE>
-__device__ __forceinline__ V4 load_row(const float *rowp, int col, int W, bool vec) {
-    if (MODE == INTERIOR) return v4(ldg4(rowp + col));
-    if (vec) return (col >= 0 && col < W) ? v4(ldg4(rowp + col)) : zero4();
-    V4 v;
-    v.x = (col + 0 >= 0 && col + 0 < W) ? __ldg(rowp + col + 0) : 0.f;
-    v.y = (col + 1 >= 0 && col + 1 < W) ? __ldg(rowp + col + 1) : 0.f;
-    v.z = (col + 2 >= 0 && col + 2 < W) ? __ldg(rowp + col + 2) : 0.f;
-    v.w = (col + 3 >= 0 && col + 3 < W) ? __ldg(rowp + col + 3) : 0.f;
-    return v;
+template <int CPL>
+__device__ __forceinline__ Row<CPL> zrow() {
+    Row<CPL> r;
+#pragma unroll
+    for (int j = 0; j < CPL / 2; ++j) r.q[j].v = 0ull;
+    return r;
+}
+
+template <int CPL>
+__device__ __forceinline__ Row<CPL> vload(const float *p) {
+    Row<CPL> r;
+    if (CPL == 2) {
+        r.q[0].v = __ldg(reinterpret_cast<const unsigned long long *>(p));
+    } else {
+        const ulonglong2 t = __ldg(reinterpret_cast<const ulonglong2 *>(p));
+        r.q[0].v = t.x;
+        r.q[CPL / 2 - 1].v = t.y;
+    }
+    return r;
+}
+
+template <int CPL>
+__device__ __forceinline__ void vstore(float *p, const Row<CPL> &v) {
+    if (CPL == 2) {
+        *reinterpret_cast<unsigned long long *>(p) = v.q[0].v;
+    } else {
+        ulonglong2 t;
+        t.x = v.q[0].v;
+        t.y = v.q[CPL / 2 - 1].v;
+        *reinterpret_cast<ulonglong2 *>(p) = t;
+    }
+}
+
+template <int CPL>
+__device__ __forceinline__ float elem(const Row<CPL> &v, int c) {
+    return (c & 1) ? hi(v.q[c >> 1]) : lo(v.q[c >> 1]);
+}
+
+// Row load with the band's bounds handling (zeros outside the frame).
+template <int CPL, int MODE>
+__device__ __forceinline__ Row<CPL> load_row(const float *rowp, int col, int W, bool vec) {
+    if (MODE == INTERIOR) return vload<CPL>(rowp + col);
+    if (vec) return (col >= 0 && col < W) ? vload<CPL>(rowp + col) : zrow<CPL>();
+    Row<CPL> r;
+#pragma unroll
+    for (int j = 0; j < CPL / 2; ++j) {
+        const int c = col + 2 * j;
+        const float a = (c >= 0 && c < W) ? __ldg(rowp + c) : 0.f;
+        const float b = (c + 1 >= 0 && c + 1 < W) ? __ldg(rowp + c + 1) : 0.f;
+        r.q[j] = mk2(a, b);
+    }
+    return r;
 }
 
 // Store the columns of this lane that the band owns.
-template <int MODE>
-__device__ __forceinline__ void store_row(float *rowp, int col, V4 v, bool lane_own,
-                                          const V4 &mk, bool vec) {
+template <int CPL, int MODE>
+__device__ __forceinline__ void store_row(float *rowp, int col, const Row<CPL> &v,
+                                          bool lane_own, const Row<CPL> &mk, bool vec) {
     if (MODE == INTERIOR || vec) {
-        if (lane_own) st4(rowp + col, f4(v));
+        if (lane_own) vstore<CPL>(rowp + col, v);
     } else {
-        if (mk.x != 0.f) rowp[col + 0] = v.x;
-        if (mk.y != 0.f) rowp[col + 1] = v.y;
-        if (mk.z != 0.f) rowp[col + 2] = v.z;
-        if (mk.w != 0.f) rowp[col + 3] = v.w;
+#pragma unroll
+        for (int c = 0; c < CPL; ++c)
+            if (elem<CPL>(mk, c) != 0.f) rowp[col + c] = elem<CPL>(v, c);
     }
+}
+
+// Pipeline state between steps.
+template <int S, int CPL>
+struct St {
+    Row<CPL> up[S > 0 ? S : 1];  // u_k at the row of stage k+1 (k = 0..S-1)
+    Row<CPL> fv[S > 0 ? S : 1];  // f at the row of stage k+1
+    Row<CPL> pr[S + 1];          // p_k (row component) at the row of stage k+1
+    Row<CPL> pc[S > 0 ? S : 1];  // p_k (column component) at the row of stage k+1
+    Row<CPL> nf, nr, nc;         // next input row: f (and p_in planes when PIN)
+};
+
+template <int S, int CPL>
+__device__ __forceinline__ void zero_state(St<S, CPL> &A) {
+#pragma unroll
+    for (int k = 0; k < (S > 0 ? S : 1); ++k) {
+        A.up[k] = zrow<CPL>();
+        A.fv[k] = zrow<CPL>();
+        A.pc[k] = zrow<CPL>();
+    }
+#pragma unroll
+    for (int k = 0; k <= S; ++k) A.pr[k] = zrow<CPL>();
+    A.nf = A.nr = A.nc = zrow<CPL>();
+}
+
+// Per-lane constants of a band.
+template <int CPL>
+struct Lane {
+    int col;           // first column of this lane
+    bool lane_own;     // every column of the lane is owned by the band
+    bool first_col;    // this lane holds column 0 (edge bands)
+    Row<CPL> mk;       // 1 for owned columns
+    Row<CPL> gmask;    // 0 at column W-1 (edge bands)
+};
+
+// div p of a row: (pr - pr_up) + (pc - pc_left), with pc_left shifted in
+// from the lane on the left.
+template <int CPL>
+__device__ __forceinline__ Row<CPL> divergence(const Row<CPL> &prn, const Row<CPL> &pcn,
+                                               const Row<CPL> &pru, bool first_col) {
+    float pcl = __shfl_up_sync(FULL, hi(pcn.q[CPL / 2 - 1]), 1);
+    if (first_col) pcl = 0.f;
+    Row<CPL> d;
+#pragma unroll
+    for (int j = 0; j < CPL / 2; ++j) {
+        const f2 left = mk2(j == 0 ? pcl : hi(pcn.q[j - 1]), lo(pcn.q[j]));
+        d.q[j] = sub2(sub2(add2(prn.q[j], pcn.q[j]), pru.q[j]), left);
+    }
+    return d;
 }
 
 // One pipeline step: input row r enters, stage k handles row r-k.
 // GEN: rows may be outside [r0, r1) or touch the frame's first/last row.
-template <int S, bool PIN, bool OUT_U, bool ENERGY, int MODE, bool GEN>
-__device__ __forceinline__ void step(const Pass &P, const St<S> &in, St<S> &out, int r, int rs,
-                                     int r0, int r1, int col, const float *fb, const float *pinb,
-                                     float *ob, float *rb, bool lane_own, const V4 &mk,
-                                     float (&en)[S > 0 ? S : 1], float (&ed)[S > 0 ? S : 1]) {
+template <int S, int CPL, bool PIN, bool OUT_U, bool ENERGY, int MODE, bool GEN>
+__device__ __forceinline__ void step(const Pass &P, const St<S, CPL> &in, St<S, CPL> &out,
+                                     int r, int rs, int r0, int r1, const Lane<CPL> &L,
+                                     const float *fb, const float *pinb, float *ob, float *rb,
+                                     f2 (&ek)[S > 0 ? S : 1]) {
+    constexpr int NQ = CPL / 2;
     const int H = P.H, W = P.W;
     const bool vec = P.vec != 0;
     const int64_t hw = (int64_t)H * W;
-    const bool cedge = (MODE != INTERIOR);
-    // per-column frame-boundary flags (edge bands only)
-    const bool first_col = cedge && (col == 0);
-    const bool lastx = cedge && (col + 0 == W - 1), lasty = cedge && (col + 1 == W - 1),
-               lastz = cedge && (col + 2 == W - 1), lastw = cedge && (col + 3 == W - 1);
+    const f2 one2 = mk2(1.f, 1.f), tw2 = mk2(P.tw, P.tw), nt2 = mk2(-P.tau, -P.tau);
+    const f2 w2 = mk2(P.weight, P.weight);
+
+    // prefetch the next input row (clamped into the frame; unused past it)
+    {
+        const int64_t rn = (int64_t)min(r + 1, H - 1) * W;
+        out.nf = load_row<CPL, MODE>(fb + rn, L.col, W, vec);
+        if (PIN) {
+            out.nr = load_row<CPL, MODE>(pinb + rn, L.col, W, vec);
+            out.nc = load_row<CPL, MODE>(pinb + hw + rn, L.col, W, vec);
+        }
+    }
 
     // ---------------- stage 0: u_0 at row r
     const bool act0 = !GEN || (r < H);
-    V4 ucur = act0 ? load_row<MODE>(fb + (int64_t)r * W, col, W, vec) : zero4();
+    const Row<CPL> fr = act0 ? in.nf : zrow<CPL>();
+    Row<CPL> ucur = fr;
     if (PIN) {
-        V4 qr = act0 ? load_row<MODE>(pinb + (int64_t)r * W, col, W, vec) : zero4();
-        V4 qc = act0 ? load_row<MODE>(pinb + hw + (int64_t)r * W, col, W, vec) : zero4();
-        float pcl = __shfl_up_sync(FULL, qc.w, 1);
-        if (first_col) pcl = 0.f;
-        const V4 pu = in.pr[0];
-        V4 d;
-        d.x = (qr.x + qc.x) - pu.x - pcl;
-        d.y = (qr.y + qc.y) - pu.y - qc.x;
-        d.z = (qr.z + qc.z) - pu.z - qc.y;
-        d.w = (qr.w + qc.w) - pu.w - qc.z;
-        ucur.x -= d.x;
-        ucur.y -= d.y;
-        ucur.z -= d.z;
-        ucur.w -= d.w;
+        const Row<CPL> qr = act0 ? in.nr : zrow<CPL>();
+        const Row<CPL> qc = act0 ? in.nc : zrow<CPL>();
+        const Row<CPL> d = divergence<CPL>(qr, qc, in.pr[0], L.first_col);
+#pragma unroll
+        for (int j = 0; j < NQ; ++j) ucur.q[j] = sub2(fr.q[j], d.q[j]);
         if (ENERGY && act0 && (!GEN || (r >= r0 && r < r1))) {
-            if (MODE == INTERIOR)
-                ed[0] += d.x * d.x + d.y * d.y + d.z * d.z + d.w * d.w;
-            else
-                ed[0] += mk.x * d.x * d.x + mk.y * d.y * d.y + mk.z * d.z * d.z + mk.w * d.w * d.w;
+#pragma unroll
+            for (int j = 0; j < NQ; ++j)
+                ek[0] = (MODE == INTERIOR) ? fma2(d.q[j], d.q[j], ek[0])
+                                           : fma2(mul2(L.mk.q[j], d.q[j]), d.q[j], ek[0]);
         }
         out.pr[0] = qr;
         if (S > 0) out.pc[0] = qc;
         if (S == 0 && OUT_U && act0 && (!GEN || (r >= r0 && r < r1))) {
             const int64_t ro = (int64_t)r * W;
-            store_row<MODE>(ob + ro, col, ucur, lane_own, mk, vec);
+            store_row<CPL, MODE>(ob + ro, L.col, ucur, L.lane_own, L.mk, vec);
             if (rb) {
-                const V4 fr = load_row<MODE>(fb + ro, col, W, vec);
-                store_row<MODE>(rb + ro, col, {ucur.x - fr.x, ucur.y - fr.y, ucur.z - fr.z, ucur.w - fr.w},
-                                lane_own, mk, vec);
+                Row<CPL> dr;
+#pragma unroll
+                for (int j = 0; j < NQ; ++j) dr.q[j] = sub2(ucur.q[j], fr.q[j]);
+                store_row<CPL, MODE>(rb + ro, L.col, dr, L.lane_own, L.mk, vec);
             }
         }
     }
+    if (S > 0) out.fv[0] = fr;
 
     // ---------------- stages 1..S
 #pragma unroll
     for (int k = 1; k <= S; ++k) {
         const int i = r - k;
-        out.up[k - 1] = ucur;  // u_{k-1}(i+1): stage k's "current" row next step
+        out.up[k - 1] = ucur;  // u_{k-1}(i+1): stage k's row in the next step
         const bool act = !GEN || (i >= rs && i < H);
-        if (!act) {
-            out.pr[k] = zero4();
-            if (k < S) out.pc[k] = zero4();
-            ucur = zero4();
-            // keep the warp converged: shuffles below are skipped uniformly
+        if (!act) {  // warp-uniform
+            out.pr[k] = zrow<CPL>();
+            if (k < S) {
+                out.pc[k] = zrow<CPL>();
+                out.fv[k] = zrow<CPL>();
+            }
+            ucur = zrow<CPL>();
             continue;
         }
-        const V4 up = in.up[k - 1];  // u_{k-1}(i)
-        float uR = __shfl_down_sync(FULL, up.x, 1);
-        V4 gc;
-        gc.x = lastx ? 0.f : up.y - up.x;
-        gc.y = lasty ? 0.f : up.z - up.y;
-        gc.z = lastz ? 0.f : up.w - up.z;
-        gc.w = lastw ? 0.f : uR - up.w;
-        V4 gr;
-        if (GEN && i == H - 1) {
-            gr = zero4();
-        } else {
-            gr.x = ucur.x - up.x;
-            gr.y = ucur.y - up.y;
-            gr.z = ucur.z - up.z;
-            gr.w = ucur.w - up.w;
+        const Row<CPL> &up = in.up[k - 1];  // u_{k-1}(i)
+        const Row<CPL> &fi = in.fv[k - 1];  // f(i)
+        const float uR = __shfl_down_sync(FULL, lo(up.q[0]), 1);
+        const bool last_row = GEN && (i == H - 1);
+        Row<CPL> gr, gc, n, ri, prn, pcn;
+#pragma unroll
+        for (int j = 0; j < NQ; ++j) {
+            const f2 right = mk2(hi(up.q[j]), j + 1 < NQ ? lo(up.q[j + 1]) : uR);
+            gc.q[j] = sub2(right, up.q[j]);
+            if (MODE != INTERIOR) gc.q[j] = mul2(gc.q[j], L.gmask.q[j]);
+            gr.q[j] = last_row ? mk2(0.f, 0.f) : sub2(ucur.q[j], up.q[j]);
+            const f2 s = fma2(gr.q[j], gr.q[j], mul2(gc.q[j], gc.q[j]));
+            n.q[j] = mk2(sqrt_approx(lo(s)), sqrt_approx(hi(s)));
+            const f2 den = fma2(tw2, n.q[j], one2);
+            ri.q[j] = mk2(rcp_approx(lo(den)), rcp_approx(hi(den)));
+            const bool p0zero = (k == 1 && !PIN);
+            const f2 qr = p0zero ? mk2(0.f, 0.f) : in.pr[k - 1].q[j];
+            const f2 qc = p0zero ? mk2(0.f, 0.f) : in.pc[k - 1].q[j];
+            prn.q[j] = mul2(fma2(nt2, gr.q[j], qr), ri.q[j]);
+            pcn.q[j] = mul2(fma2(nt2, gc.q[j], qc), ri.q[j]);
         }
-        V4 n;
-        n.x = sqrt_approx(fmaf(gr.x, gr.x, gc.x * gc.x));
-        n.y = sqrt_approx(fmaf(gr.y, gr.y, gc.y * gc.y));
-        n.z = sqrt_approx(fmaf(gr.z, gr.z, gc.z * gc.z));
-        n.w = sqrt_approx(fmaf(gr.w, gr.w, gc.w * gc.w));
-        V4 ri;
-        ri.x = rcp_approx(fmaf(P.tw, n.x, 1.f));
-        ri.y = rcp_approx(fmaf(P.tw, n.y, 1.f));
-        ri.z = rcp_approx(fmaf(P.tw, n.z, 1.f));
-        ri.w = rcp_approx(fmaf(P.tw, n.w, 1.f));
-        const bool p0zero = (k == 1 && !PIN);
-        const V4 qr = p0zero ? zero4() : in.pr[k - 1];
-        const V4 qc = p0zero ? zero4() : in.pc[k - 1];
-        const float nt = -P.tau;
-        V4 prn, pcn;
-        prn.x = fmaf(nt, gr.x, qr.x) * ri.x;
-        prn.y = fmaf(nt, gr.y, qr.y) * ri.y;
-        prn.z = fmaf(nt, gr.z, qr.z) * ri.z;
-        prn.w = fmaf(nt, gr.w, qr.w) * ri.w;
-        pcn.x = fmaf(nt, gc.x, qc.x) * ri.x;
-        pcn.y = fmaf(nt, gc.y, qc.y) * ri.y;
-        pcn.z = fmaf(nt, gc.z, qc.z) * ri.z;
-        pcn.w = fmaf(nt, gc.w, qc.w) * ri.w;
         out.pr[k] = prn;
         if (k < S) out.pc[k] = pcn;
-        // div p_k at row i
-        float pcl = __shfl_up_sync(FULL, pcn.w, 1);
-        if (first_col) pcl = 0.f;
-        const V4 pu = in.pr[k];  // pr_k(i-1)
-        V4 d;
-        d.x = (prn.x + pcn.x) - pu.x - pcl;
-        d.y = (prn.y + pcn.y) - pu.y - pcn.x;
-        d.z = (prn.z + pcn.z) - pu.z - pcn.y;
-        d.w = (prn.w + pcn.w) - pu.w - pcn.z;
-        const int64_t ro = (int64_t)i * W;
-        const V4 fi = load_row<MODE>(fb + ro, col, W, vec);
-        V4 uk;
-        uk.x = fi.x - d.x;
-        uk.y = fi.y - d.y;
-        uk.z = fi.z - d.z;
-        uk.w = fi.w - d.w;
+        const Row<CPL> d = divergence<CPL>(prn, pcn, in.pr[k], L.first_col);
+        Row<CPL> uk;
+#pragma unroll
+        for (int j = 0; j < NQ; ++j) uk.q[j] = sub2(fi.q[j], d.q[j]);
         if (ENERGY && (!GEN || (i >= r0 && i < r1))) {
-            if (MODE == INTERIOR) {
-                en[k - 1] += (n.x + n.y) + (n.z + n.w);
-                if (k < S) ed[k] += d.x * d.x + d.y * d.y + d.z * d.z + d.w * d.w;
-            } else {
-                en[k - 1] += mk.x * n.x + mk.y * n.y + mk.z * n.z + mk.w * n.w;
-                if (k < S)
-                    ed[k] += mk.x * d.x * d.x + mk.y * d.y * d.y + mk.z * d.z * d.z +
-                             mk.w * d.w * d.w;
+#pragma unroll
+            for (int j = 0; j < NQ; ++j) {
+                if (MODE == INTERIOR) {
+                    ek[k - 1] = fma2(w2, n.q[j], ek[k - 1]);
+                    if (k < S) ek[k] = fma2(d.q[j], d.q[j], ek[k]);
+                } else {
+                    ek[k - 1] = fma2(mul2(w2, L.mk.q[j]), n.q[j], ek[k - 1]);
+                    if (k < S) ek[k] = fma2(mul2(L.mk.q[j], d.q[j]), d.q[j], ek[k]);
+                }
             }
         }
-        if (k == S && (!GEN || (i >= r0 && i < r1))) {
-            if (OUT_U) {
-                store_row<MODE>(ob + ro, col, uk, lane_own, mk, vec);
-                if (rb)
-                    store_row<MODE>(rb + ro, col, {uk.x - fi.x, uk.y - fi.y, uk.z - fi.z, uk.w - fi.w},
-                                    lane_own, mk, vec);
-            } else {
-                store_row<MODE>(ob + ro, col, prn, lane_own, mk, vec);
-                store_row<MODE>(ob + hw + ro, col, pcn, lane_own, mk, vec);
+        if (k == S) {
+            if (!GEN || (i >= r0 && i < r1)) {
+                const int64_t ro = (int64_t)i * W;
+                if (OUT_U) {
+                    store_row<CPL, MODE>(ob + ro, L.col, uk, L.lane_own, L.mk, vec);
+                    if (rb) {
+                        Row<CPL> dr;
+#pragma unroll
+                        for (int j = 0; j < NQ; ++j) dr.q[j] = sub2(uk.q[j], fi.q[j]);
+                        store_row<CPL, MODE>(rb + ro, L.col, dr, L.lane_own, L.mk, vec);
+                    }
+                } else {
+                    store_row<CPL, MODE>(ob + ro, L.col, prn, L.lane_own, L.mk, vec);
+                    store_row<CPL, MODE>(ob + hw + ro, L.col, pcn, L.lane_own, L.mk, vec);
+                }
             }
+        } else {
+            out.fv[k] = fi;
         }
         ucur = uk;
     }
 }
 
-template <int S, bool PIN, bool OUT_U, bool ENERGY, int MODE>
+template <int S, int CPL, bool PIN, bool OUT_U, bool ENERGY, int MODE>
 __device__ __forceinline__ void run(const Pass &P, int frame, int chunk, int band, int lane) {
     const int H = P.H, W = P.W;
-    const int col = band * P.own - P.hl + lane * CPL;
+    Lane<CPL> L;
+    L.col = band * P.own - P.hl + lane * CPL;
     const int r0 = chunk * P.R, r1 = min(r0 + P.R, H);
     const int rs = max(0, r0 - P.ht);
     const int own_lo = band * P.own, own_hi = min(own_lo + P.own, W);
-    const bool lane_own = (col >= own_lo) && (col + CPL <= own_hi);
-    V4 mk;
-    mk.x = (col + 0 >= own_lo && col + 0 < own_hi) ? 1.f : 0.f;
-    mk.y = (col + 1 >= own_lo && col + 1 < own_hi) ? 1.f : 0.f;
-    mk.z = (col + 2 >= own_lo && col + 2 < own_hi) ? 1.f : 0.f;
-    mk.w = (col + 3 >= own_lo && col + 3 < own_hi) ? 1.f : 0.f;
+    L.lane_own = (L.col >= own_lo) && (L.col + CPL <= own_hi);
+    L.first_col = (MODE != INTERIOR) && (L.col == 0);
+#pragma unroll
+    for (int j = 0; j < CPL / 2; ++j) {
+        const int c = L.col + 2 * j;
+        L.mk.q[j] = mk2((c >= own_lo && c < own_hi) ? 1.f : 0.f,
+                        (c + 1 >= own_lo && c + 1 < own_hi) ? 1.f : 0.f);
+        L.gmask.q[j] = mk2(c == W - 1 ? 0.f : 1.f, c + 1 == W - 1 ? 0.f : 1.f);
+    }
 
     const int64_t hw = (int64_t)H * W;
     const float *fb = P.f + (int64_t)frame * P.fs;
     const float *pinb = PIN ? P.p_in + (int64_t)frame * 2 * hw : nullptr;
     float *ob = OUT_U ? P.u + (int64_t)frame * P.fs : P.p_out + (int64_t)frame * 2 * hw;
     float *rb = (OUT_U && P.resid) ? P.resid + (int64_t)frame * P.fs : nullptr;
+    const bool vec = P.vec != 0;
 
-    St<S> A, B;
+    St<S, CPL> A, B;
+    zero_state<S, CPL>(A);
+    // ek[k]: this lane's part of H*W*E_{a+k} = sum (div p)^2 + weight sum |grad u|
+    f2 ek[S > 0 ? S : 1];
 #pragma unroll
-    for (int k = 0; k < (S > 0 ? S : 1); ++k) {
-        A.up[k] = zero4();
-        A.pc[k] = zero4();
+    for (int k = 0; k < (S > 0 ? S : 1); ++k) ek[k].v = 0ull;
+    // first input row
+    A.nf = load_row<CPL, MODE>(fb + (int64_t)rs * W, L.col, W, vec);
+    if (PIN) {
+        A.nr = load_row<CPL, MODE>(pinb + (int64_t)rs * W, L.col, W, vec);
+        A.nc = load_row<CPL, MODE>(pinb + hw + (int64_t)rs * W, L.col, W, vec);
     }
-#pragma unroll
-    for (int k = 0; k <= S; ++k) A.pr[k] = zero4();
-    float en[S > 0 ? S : 1], ed[S > 0 ? S : 1];
-#pragma unroll
-    for (int k = 0; k < (S > 0 ? S : 1); ++k) en[k] = ed[k] = 0.f;
 
     const int rlast = min(r1 - 1 + S, H - 1 + S);
     // Fast steps: every stage inside [r0, r1), away from the frame's last row.
@@ -298,47 +373,40 @@ __device__ __forceinline__ void run(const Pass &P, int frame, int chunk, int ban
     while (r <= rlast) {
         if (r == rfb && r + 1 <= rfe) {
             for (; r + 1 <= rfe; r += 2) {
-                step<S, PIN, OUT_U, ENERGY, MODE, false>(P, A, B, r, rs, r0, r1, col, fb, pinb,
-                                                          ob, rb, lane_own, mk, en, ed);
-                step<S, PIN, OUT_U, ENERGY, MODE, false>(P, B, A, r + 1, rs, r0, r1, col, fb,
-                                                          pinb, ob, rb, lane_own, mk, en, ed);
+                step<S, CPL, PIN, OUT_U, ENERGY, MODE, false>(P, A, B, r, rs, r0, r1, L, fb, pinb,
+                                                               ob, rb, ek);
+                step<S, CPL, PIN, OUT_U, ENERGY, MODE, false>(P, B, A, r + 1, rs, r0, r1, L, fb,
+                                                               pinb, ob, rb, ek);
             }
             continue;
         }
         // prologue (halo rows, first S steps) and epilogue (chunk tail, last row)
-        step<S, PIN, OUT_U, ENERGY, MODE, true>(P, A, B, r, rs, r0, r1, col, fb, pinb, ob, rb,
-                                                 lane_own, mk, en, ed);
+        step<S, CPL, PIN, OUT_U, ENERGY, MODE, true>(P, A, B, r, rs, r0, r1, L, fb, pinb, ob, rb,
+                                                      ek);
         A = B;
         ++r;
     }
 
     if (ENERGY) {
-        const float lm = (MODE == INTERIOR) ? (lane_own ? 1.f : 0.f) : 1.f;
+        const float lm = (MODE == INTERIOR) ? (L.lane_own ? 1.f : 0.f) : 1.f;
         double *eb = P.energy + (int64_t)frame * P.K * 2;
 #pragma unroll
         for (int k = 0; k < (S > 0 ? S : 1); ++k) {
-            double vn = (double)(en[k] * lm), vd = (double)(ed[k] * lm);
+            double v = (double)((lo(ek[k]) + hi(ek[k])) * lm);
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) {
-                vn += __shfl_xor_sync(FULL, vn, o);
-                vd += __shfl_xor_sync(FULL, vd, o);
-            }
-            if (lane == 0) {
-                const int j = P.a + k;
-                if (S > 0) atomicAdd(eb + 2 * j + 1, vn);
-                if (k > 0 || PIN) atomicAdd(eb + 2 * j + 0, vd);
-            }
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+            if (lane == 0) atomicAdd(eb + 2 * (P.a + k), v);
         }
     }
 }
 
-template <int S, bool PIN, bool OUT_U, bool ENERGY>
+template <int S, int CPL, bool PIN, bool OUT_U, bool ENERGY>
 __device__ __forceinline__ void run_mode(const Pass &P, int frame, int chunk, int band, int lane) {
     const int c0 = band * P.own - P.hl;
-    if (P.vec && c0 >= 0 && c0 + BANDW - 1 <= P.W - 1)
-        run<S, PIN, OUT_U, ENERGY, INTERIOR>(P, frame, chunk, band, lane);
+    if (P.vec && c0 >= 0 && c0 + 32 * CPL - 1 <= P.W - 1)
+        run<S, CPL, PIN, OUT_U, ENERGY, INTERIOR>(P, frame, chunk, band, lane);
     else
-        run<S, PIN, OUT_U, ENERGY, EDGE>(P, frame, chunk, band, lane);
+        run<S, CPL, PIN, OUT_U, ENERGY, EDGE>(P, frame, chunk, band, lane);
 }
 
 // Decodes a warp's work item: (frame, row chunk, column band).
@@ -372,41 +440,56 @@ __device__ __forceinline__ int find_stop(const Pass &P, int frame) {
     return -1;
 }
 
+template <int CPL>
+constexpr int min_blocks() { return CPL == 2 ? 4 : 3; }
+
 // Main launch of one pass: every frame not yet stopped runs all SG updates.
-template <int SG, bool PIN, bool FINAL>
-__global__ void __launch_bounds__(WPB * 32) k_tv_main(Pass P) {
+template <int SG, bool PIN, bool FINAL, int CPL>
+__global__ void __launch_bounds__(WPB * 32, min_blocks<CPL>()) k_tv_main(Pass P) {
     int frame, chunk, band;
     if (!decode_item(P, frame, chunk, band)) return;
-    if (P.done[frame] >= 0) return;
-    run_mode<SG, PIN, FINAL, true>(P, frame, chunk, band, threadIdx.x & 31);
+    if (PIN && P.done[frame] >= 0) return;  // stopped in an earlier pass
+    run_mode<SG, CPL, PIN, FINAL, true>(P, frame, chunk, band, threadIdx.x & 31);
 }
 
-// Stop-test launch of one pass: frames whose rule fires at j inside the
-// window [a, a+S-1] are recomputed with j - a updates and write u_j.
-template <bool PIN>
-__global__ void __launch_bounds__(WPB * 32) k_tv_fixup(Pass P) {
-    int frame, chunk, band;
-    if (!decode_item(P, frame, chunk, band)) return;
-    const int d = P.done[frame];
-    if (d >= 0 && d < P.a) return;  // stopped in an earlier window
+// Stop-test launch of one pass, P.gpf blocks per frame: frames whose rule
+// fires at j inside the window [a, a+S-1] are recomputed with j - a updates
+// and write u_j; the other frames' blocks exit after reading 2K doubles.
+template <bool PIN, int CPL>
+__global__ void __launch_bounds__(WPB * 32, min_blocks<CPL>()) k_tv_fixup(Pass P) {
+    const int frame = blockIdx.x / P.gpf, g = blockIdx.x - frame * P.gpf;
+    if (frame >= P.nf) return;
+    if (PIN) {
+        const int d = P.done[frame];
+        if (d >= 0 && d < P.a) return;  // stopped in an earlier window
+    }
     const int j = find_stop(P, frame);
-    if (j < 0) return;
-    const int lane = threadIdx.x & 31;
-    if (chunk == 0 && band == 0 && lane == 0) {
-        P.done[frame] = j;  // every block of this frame writes the same j
+    const bool lead = (g == 0 && threadIdx.x == 0);
+    if (j < 0) {
+        if (lead && P.steps && P.a + P.S == P.K - 1) P.steps[frame] = P.K;
+        return;
+    }
+    if (lead) {
+        P.done[frame] = j;
         if (P.steps) P.steps[frame] = j + 1;
     }
-    switch (j - P.a) {
-        case 0: if constexpr (PIN) run_mode<0, PIN, true, false>(P, frame, chunk, band, lane); break;
-        case 1: run_mode<1, PIN, true, false>(P, frame, chunk, band, lane); break;
-        case 2: run_mode<2, PIN, true, false>(P, frame, chunk, band, lane); break;
-        case 3: run_mode<3, PIN, true, false>(P, frame, chunk, band, lane); break;
-        default: break;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int per_frame = P.nbands * P.nchunks;
+    for (int it = g * WPB + warp; it < per_frame; it += P.gpf * WPB) {
+        const int chunk = it / P.nbands, band = it - chunk * P.nbands;
+        switch (j - P.a) {
+            case 0: if constexpr (PIN) run_mode<0, CPL, PIN, true, false>(P, frame, chunk, band, lane); break;
+            case 1: run_mode<1, CPL, PIN, true, false>(P, frame, chunk, band, lane); break;
+            case 2: run_mode<2, CPL, PIN, true, false>(P, frame, chunk, band, lane); break;
+            case 3: run_mode<3, CPL, PIN, true, false>(P, frame, chunk, band, lane); break;
+            default: break;
+        }
     }
 }
 
 // Host launchers (one translation unit each, compiled in parallel).
-void launch_main4(const Pass &P, bool pin, bool final_pass, cudaStream_t s);
+void launch_main4_c4(const Pass &P, bool pin, bool final_pass, cudaStream_t s);
+void launch_main4_c2(const Pass &P, bool pin, bool final_pass, cudaStream_t s);
 void launch_main123(const Pass &P, int SG, bool pin, cudaStream_t s);
 void launch_fixup(const Pass &P, bool pin, cudaStream_t s);
 

@@ -1,16 +1,17 @@
-// Chambolle TV pass kernels with 4 dual updates per pass (n_iter_max = 5 in
-// one pass; the 4-update passes of longer runs).  See sci_tv.cuh.
+// Chambolle TV pass kernels with 4 dual updates per pass, 4 columns per lane
+// (n_iter_max = 5 in one pass; the 4-update passes of longer runs).
+// See sci_tv.cuh.
 #include "sci_tv.cuh"
 
 namespace sci {
 namespace tv {
 
-void launch_main4(const Pass &P, bool pin, bool final_pass, cudaStream_t s) {
+void launch_main4_c4(const Pass &P, bool pin, bool final_pass, cudaStream_t s) {
     const unsigned g = pass_blocks(P);
-    if (!pin && final_pass) k_tv_main<4, false, true><<<g, WPB * 32, 0, s>>>(P);
-    else if (!pin) k_tv_main<4, false, false><<<g, WPB * 32, 0, s>>>(P);
-    else if (final_pass) k_tv_main<4, true, true><<<g, WPB * 32, 0, s>>>(P);
-    else k_tv_main<4, true, false><<<g, WPB * 32, 0, s>>>(P);
+    if (!pin && final_pass) k_tv_main<4, false, true, 4><<<g, WPB * 32, 0, s>>>(P);
+    else if (!pin) k_tv_main<4, false, false, 4><<<g, WPB * 32, 0, s>>>(P);
+    else if (final_pass) k_tv_main<4, true, true, 4><<<g, WPB * 32, 0, s>>>(P);
+    else k_tv_main<4, true, false, 4><<<g, WPB * 32, 0, s>>>(P);
 }
 
 }  // namespace tv

@@ -32,6 +32,7 @@ from . import _dev
 from .metrics import frame_psnr, frame_ssim
 from .solver import Solver
 from .tv import tv_frames, tv_workspace
+from .cassi import CassiOperator, CassiSolver
 from .utils import MaskOperator, operator_of, psnr_from_mse, sum_sq_err
 
 
@@ -64,7 +65,13 @@ def _solve(projmeth, y, Phi_sum, A, At, iters, _lambda, tv_weight, tv_iter_max, 
     y_d = _dev.plane(y)
     ps_d = _dev.plane(Phi_sum)
     want_iqa = show_iqa and X_orig is not None
-    if op is not None:
+    if isinstance(op, CassiOperator) and projmeth == "gap":
+        solver = CassiSolver(op, iters, _lambda, tv_weight, tv_iter_max, eps, accelerate)
+        x0_d = None if x0 is None else _dev.planar(x0)
+        orig_d = _dev.planar(X_orig) if want_iqa else None
+        x = solver.run(y_d, x0=x0_d, phisum=ps_d, orig=orig_d)
+        return x, (solver.psnr_all() if want_iqa else [])
+    if isinstance(op, MaskOperator):
         solver = Solver(op, projmeth, iters, _lambda, tv_weight, tv_iter_max, eps, accelerate,
                         gamma, use_graph=use_graph)
         x0_d = None if x0 is None else _dev.planar(x0)

@@ -78,12 +78,16 @@ def make_ops(mask, pack=True):
 
 
 def operator_of(A, At):
-    """The MaskOperator behind (A, At) if both are its bound methods."""
+    """The native operator (MaskOperator, CassiOperator) behind (A, At) if
+    both are the forward / adjoint bound methods of the same object."""
     oa = getattr(A, "__self__", None)
     ot = getattr(At, "__self__", None)
-    if isinstance(oa, MaskOperator) and oa is ot and \
-            getattr(A, "__func__", None) is MaskOperator.forward and \
-            getattr(At, "__func__", None) is MaskOperator.adjoint:
+    if oa is None or oa is not ot:
+        return None
+    cls = type(oa)
+    if getattr(A, "__func__", None) is getattr(cls, "forward", None) and \
+            getattr(At, "__func__", None) is getattr(cls, "adjoint", None) and \
+            hasattr(oa, "phisum"):
         return oa
     return None
 
