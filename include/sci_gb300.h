@@ -111,6 +111,24 @@ int sci_tv_chambolle(const float *f, float *u, float *resid, int64_t nframes,
                      int n_iter_max, int *steps, double *energy,
                      void *workspace, size_t workspace_bytes, void *stream);
 
+/* Allocation-free variant of sci_tv_chambolle, for callers that cannot
+ * allocate device memory (a host framework that owns all device memory
+ * through its own pool, a plug-in handed only its input and output
+ * buffers, a loop where cudaMalloc would synchronise the device).  Its
+ * scratch is a fixed 64 KiB array in the library's device image (kept on
+ * every GPU that loads the library until exit), so it needs no workspace
+ * argument.  Limits: n_iter_max <= 5 and nframes * n_iter_max * 16 bytes
+ * (+ 4 bytes per frame) <= 64 KiB (nframes <= 777 at n_iter_max = 5);
+ * larger requests return SCI_ERR_INVALID_ARG.  All calls share the array:
+ * calls whose work overlaps on the GPU race and must be ordered by the
+ * caller.  The first call on a device looks up the array's address; make
+ * it before any stream capture on that device.  No counterpart in the
+ * reference (which allocates on the host through numpy). */
+int sci_tv_chambolle_noalloc(const float *f, float *u, float *resid,
+                             int64_t nframes, int64_t H, int64_t W,
+                             float weight, float eps, int n_iter_max,
+                             int *steps, void *stream);
+
 /* -------------------------------------------------- metrics (diagnostics) */
 
 /* out[0] += sum_i (a_i - b_i)^2 in float64 (PSNR numerator for
