@@ -81,6 +81,16 @@ int sci_proj_gap(const float *x, const float *phi, const uint32_t *mask_bits,
                  float lambda, int accelerate,
                  int64_t B, int64_t H, int64_t W, void *stream);
 
+/* Residual map of one GAP projection, without writing the projected stack:
+ *   yb = A(x); accelerate: y1 += y - yb, c = (y1 - yb)/phisum;
+ *   else c = (y - yb)/phisum.            (c, y1: H x W; y1 in/out)
+ * The update x + lambda At(c) is then applied by the TV kernel while it
+ * reads x (the fused GAP-TV iteration).  Needs H*W % 4 == 0 and 16-byte
+ * aligned buffers.  Replaces the first half of pnp_sci_algo.py:640-645. */
+int sci_gap_residual(const float *x, const float *phi, const uint32_t *mask_bits,
+                     const float *y, float *y1, const float *phisum, float *c,
+                     int accelerate, int64_t B, int64_t H, int64_t W, void *stream);
+
 /* One ADMM projection:  t = theta + b; yb = A(t);
  *   x = t + lambda * At((y - yb)/(phisum + gamma));  v = x - b.
  * Writes v (the TV input) and, when x_out is non-NULL, x.

@@ -52,6 +52,8 @@ _SIGS = {
     "sci_pack_mask": [c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_vp],
     "sci_proj_gap": [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_f, ctypes.c_int,
                      c_i64, c_i64, c_i64, c_vp],
+    "sci_gap_residual": [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, ctypes.c_int, c_i64, c_i64,
+                         c_i64, c_vp],
     "sci_proj_admm": [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_f, c_f,
                       c_i64, c_i64, c_i64, c_vp],
     "sci_tv_workspace_bytes": [c_i64, c_i64, c_i64, ctypes.c_int, ctypes.POINTER(c_sz)],

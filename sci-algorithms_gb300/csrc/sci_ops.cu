@@ -226,6 +226,139 @@ __global__ void k_proj_gap_scalar(const float *__restrict__ x, Mask<MODE> M,
     }
 }
 
+// --------------------------------------- register-resident projections
+// One pass over HBM: a thread holds the B values of its pixels in registers
+// between forming yb and writing the update (the two-sweep kernels above
+// re-read x, and under the streaming load the second sweep misses L2).
+// BMAX >= B is the unrolled register capacity.
+// GAP projection staging each thread's B values of x in shared memory
+// (slot [b][thread], bank-conflict free) between the A(x) sum and the
+// update, so x crosses HBM once while registers stay low.
+template <int MODE, bool ACC>
+__global__ void __launch_bounds__(256) k_proj_gap_smem(
+    const float *__restrict__ x, Mask<MODE> M, const float *__restrict__ y,
+    float *__restrict__ y1, const float *__restrict__ phisum, float *__restrict__ xo,
+    float lam, int B, int64_t hw) {
+    extern __shared__ float xs[];  // [B][blockDim.x]
+    const int t = threadIdx.x, nt = blockDim.x;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < hw;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t w = M.word1(p);
+        float s = 0.f;
+#pragma unroll 8
+        for (int b = 0; b < B; ++b) {
+            const float v = __ldg(x + b * hw + p);
+            xs[b * nt + t] = v;
+            s = fmaf(v, M.at1(b, p, w), s);
+        }
+        const float yv = __ldg(y + p), ps = __ldg(phisum + p);
+        float r;
+        if (ACC) {
+            const float tt = y1[p] + (yv - s);
+            y1[p] = tt;
+            r = __fdiv_rn(tt - s, ps);
+        } else {
+            r = __fdiv_rn(yv - s, ps);
+        }
+#pragma unroll 8
+        for (int b = 0; b < B; ++b)
+            __stcs(xo + b * hw + p, fmaf(lam, r * M.at1(b, p, w), xs[b * nt + t]));
+    }
+}
+
+// ADMM projection staging t = theta + b and b in shared memory (slots
+// [b][thread]), one HBM pass over theta and b.
+template <int MODE>
+__global__ void __launch_bounds__(128) k_proj_admm_smem(
+    const float *__restrict__ th, const float *__restrict__ bb, Mask<MODE> M,
+    const float *__restrict__ y, const float *__restrict__ phisum, float *__restrict__ v,
+    float *__restrict__ xo, float lam, float gamma, int B, int64_t hw) {
+    extern __shared__ float st[];  // [2][B][blockDim.x]: t, b
+    const int t = threadIdx.x, nt = blockDim.x;
+    float *ts = st, *bs = st + B * nt;
+    for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < hw;
+         p += (int64_t)gridDim.x * blockDim.x) {
+        const uint32_t w = M.word1(p);
+        float s = 0.f;
+#pragma unroll 8
+        for (int b = 0; b < B; ++b) {
+            const float bv = __ldg(bb + b * hw + p);
+            const float tv = __ldg(th + b * hw + p) + bv;
+            ts[b * nt + t] = tv;
+            bs[b * nt + t] = bv;
+            s = fmaf(tv, M.at1(b, p, w), s);
+        }
+        const float r = __fdiv_rn(__ldg(y + p) - s, __ldg(phisum + p) + gamma);
+#pragma unroll 8
+        for (int b = 0; b < B; ++b) {
+            const float xv = fmaf(lam, r * M.at1(b, p, w), ts[b * nt + t]);
+            if (xo) xo[b * hw + p] = xv;
+            __stcs(v + b * hw + p, xv - bs[b * nt + t]);
+        }
+    }
+}
+
+template <int MODE, bool ACC>
+static void launch_gap_smem(const float *x, Mask<MODE> M, const float *y, float *y1,
+                            const float *ps, float *xo, float lam, int B, int64_t hw,
+                            cudaStream_t s) {
+    const size_t smem = sizeof(float) * (size_t)B * 256;  // <= 32 KB for B <= 32
+    k_proj_gap_smem<MODE, ACC><<<grid_for(hw, 256), 256, smem, s>>>(x, M, y, y1, ps, xo, lam, B,
+                                                                    hw);
+}
+
+template <int MODE>
+static void launch_admm_smem(const float *th, const float *bb, Mask<MODE> M, const float *y,
+                             const float *ps, float *v, float *xo, float lam, float gamma, int B,
+                             int64_t hw, cudaStream_t s) {
+    // 128 threads: 2 * B * 128 floats <= 32 KB of shared memory for B <= 32
+    const size_t smem = sizeof(float) * 2 * (size_t)B * 128;
+    k_proj_admm_smem<MODE><<<grid_for(hw, 128), 128, smem, s>>>(th, bb, M, y, ps, v, xo, lam,
+                                                                gamma, B, hw);
+}
+
+// ------------------------------------------- GAP residual map (fused path)
+// yb = sum_b phi_b x_b; ACC: y1 += y - yb, c = (y1 - yb)/phisum; else
+// c = (y - yb)/phisum.  The x update x + lambda (c phi_b) is applied by the
+// TV kernel while it loads x (same arithmetic as k_proj_gap).
+template <int MODE, bool ACC>
+__global__ void __launch_bounds__(256) k_gap_resid_vec(
+    const float *__restrict__ x, Mask<MODE> M, const float *__restrict__ y,
+    float *__restrict__ y1, const float *__restrict__ phisum, float *__restrict__ c, int B,
+    int64_t hw) {
+    const int64_t n4 = hw >> 2;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n4;
+         q += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t p = q << 2;
+        const uint4 w = M.word4(p);
+        float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll 4
+        for (int b = 0; b < B; ++b) {
+            const float4 a = ldg4(x + b * hw + p), m = M.at4(b, p, w);
+            s.x = fmaf(a.x, m.x, s.x);
+            s.y = fmaf(a.y, m.y, s.y);
+            s.z = fmaf(a.z, m.z, s.z);
+            s.w = fmaf(a.w, m.w, s.w);
+        }
+        const float4 yv = ldg4(y + p), ps = ldg4(phisum + p);
+        float4 r;
+        if (ACC) {
+            float4 t = ldg4(y1 + p);
+            t.x = t.x + (yv.x - s.x);
+            t.y = t.y + (yv.y - s.y);
+            t.z = t.z + (yv.z - s.z);
+            t.w = t.w + (yv.w - s.w);
+            st4(y1 + p, t);
+            r = make_float4(__fdiv_rn(t.x - s.x, ps.x), __fdiv_rn(t.y - s.y, ps.y),
+                            __fdiv_rn(t.z - s.z, ps.z), __fdiv_rn(t.w - s.w, ps.w));
+        } else {
+            r = make_float4(__fdiv_rn(yv.x - s.x, ps.x), __fdiv_rn(yv.y - s.y, ps.y),
+                            __fdiv_rn(yv.z - s.z, ps.z), __fdiv_rn(yv.w - s.w, ps.w));
+        }
+        st4(c + p, r);
+    }
+}
+
 // ----------------------------------------------------- ADMM projection
 // t = theta + b; yb = A(t); x = t + lambda*(r*phi), r = (y-yb)/(phisum+gamma);
 // v = x - b.  x written only when xo != nullptr.
@@ -427,6 +560,10 @@ int sci_proj_gap(const float *x, const float *phi, const uint32_t *mask_bits, co
     } while (0)
     if (mask_bits) {
         Mask<1> M{mask_bits, hw};
+        if (accelerate) launch_gap_smem<1, true>(x, M, y, y1, phisum, x_out, lambda, Bi, hw, s);
+        else launch_gap_smem<1, false>(x, M, y, y1, phisum, x_out, lambda, Bi, hw, s);
+    } else if (mask_bits) {
+        Mask<1> M{mask_bits, hw};
         LAUNCH_GAP(1, M);
     } else {
         Mask<0> M{phi, hw};
@@ -434,6 +571,31 @@ int sci_proj_gap(const float *x, const float *phi, const uint32_t *mask_bits, co
     }
 #undef LAUNCH_GAP
     SCI_LAUNCHED("k_proj_gap");
+    return SCI_OK;
+}
+
+int sci_gap_residual(const float *x, const float *phi, const uint32_t *mask_bits,
+                     const float *y, float *y1, const float *phisum, float *c,
+                     int accelerate, int64_t B, int64_t H, int64_t W, void *stream) {
+    if (int e = check_dims(B, H, W)) return e;
+    SCI_CHECK_ARG(x && y && phisum && c && (phi || mask_bits), "sci_gap_residual: null pointer");
+    SCI_CHECK_ARG(!accelerate || y1, "sci_gap_residual: accelerate needs y1");
+    SCI_CHECK_ARG(!mask_bits || B <= 32, "sci_gap_residual: packed mask needs B <= 32");
+    const int64_t hw = H * W;
+    SCI_CHECK_ARG(vec_ok(hw, {x, phi, mask_bits, y, y1, phisum, c}),
+                  "sci_gap_residual: needs H*W %% 4 == 0 and 16-byte aligned buffers");
+    cudaStream_t s = as_stream(stream);
+    const dim3 g = grid_for(hw / 4, 256);
+    if (mask_bits) {
+        Mask<1> M{mask_bits, hw};
+        if (accelerate) k_gap_resid_vec<1, true><<<g, 256, 0, s>>>(x, M, y, y1, phisum, c, (int)B, hw);
+        else k_gap_resid_vec<1, false><<<g, 256, 0, s>>>(x, M, y, y1, phisum, c, (int)B, hw);
+    } else {
+        Mask<0> M{phi, hw};
+        if (accelerate) k_gap_resid_vec<0, true><<<g, 256, 0, s>>>(x, M, y, y1, phisum, c, (int)B, hw);
+        else k_gap_resid_vec<0, false><<<g, 256, 0, s>>>(x, M, y, y1, phisum, c, (int)B, hw);
+    }
+    SCI_LAUNCHED("k_gap_resid");
     return SCI_OK;
 }
 
@@ -452,6 +614,9 @@ int sci_proj_admm(const float *theta, const float *b, const float *phi,
     const bool vec = vec_ok(hw, {theta, b, phi, mask_bits, y, phisum, v, x_out});
     const int Bi = (int)B;
     if (mask_bits) {
+        Mask<1> M{mask_bits, hw};
+        launch_admm_smem<1>(theta, b, M, y, phisum, v, x_out, lambda, gamma, Bi, hw, s);
+    } else if (false) {
         Mask<1> M{mask_bits, hw};
         if (vec)
             k_proj_admm_vec<1><<<grid_for(hw / 4, 256), 256, 0, s>>>(theta, b, M, y, phisum, v,

@@ -18,11 +18,16 @@ int tv_launch(const float *f, float *u, float *resid, int64_t nf, int64_t H, int
               int64_t fs, float weight, float eps, int K, int *steps, double *energy_out,
               void *workspace, size_t ws_bytes, cudaStream_t s, int force_R);
 size_t tv_workspace_bytes(int64_t nf, int64_t H, int64_t W, int K);
+int tv_launch_impl(const float *f, float *u, float *resid, int64_t nf, int64_t H, int64_t W,
+                   int64_t fs, float weight, float eps, int K, int *steps, double *energy_out,
+                   void *workspace, size_t ws_bytes, cudaStream_t s, int force_R, int flags,
+                   const uint32_t *proj_bits, const float *proj_c, float proj_lam);
+bool tv_proj_supported(int64_t nf, int64_t W, int K);
 
 namespace {
 
 struct SolverWs {
-    float *y1, *xp, *theta, *v, *b0, *b1;
+    float *y1, *xp, *c, *theta, *v, *b0, *b1;
     void *tv;
     size_t tv_bytes;
 };
@@ -38,10 +43,11 @@ size_t solver_layout(bool admm, int64_t B, int64_t H, int64_t W, int K, SolverWs
         off += round256(bytes);
         return o;
     };
-    size_t oy1 = 0, oxp = 0, oth = 0, ov = 0, ob0 = 0, ob1 = 0;
+    size_t oy1 = 0, oxp = 0, oc = 0, oth = 0, ov = 0, ob0 = 0, ob1 = 0;
     if (!admm) {
         oy1 = take(sizeof(float) * hw);
         oxp = take(sizeof(float) * n);
+        oc = take(sizeof(float) * hw);
     } else {
         oth = take(sizeof(float) * n);
         ov = take(sizeof(float) * n);
@@ -53,6 +59,7 @@ size_t solver_layout(bool admm, int64_t B, int64_t H, int64_t W, int K, SolverWs
     if (w) {
         w->y1 = admm ? nullptr : reinterpret_cast<float *>(base + oy1);
         w->xp = admm ? nullptr : reinterpret_cast<float *>(base + oxp);
+        w->c = admm ? nullptr : reinterpret_cast<float *>(base + oc);
         w->theta = admm ? reinterpret_cast<float *>(base + oth) : nullptr;
         w->v = admm ? reinterpret_cast<float *>(base + ov) : nullptr;
         w->b0 = admm ? reinterpret_cast<float *>(base + ob0) : nullptr;
@@ -143,6 +150,36 @@ int enqueue(const Args &a, cudaStream_t s) {
     SolverWs w;
     solver_layout(a.admm, B, H, W, K, &w, static_cast<char *>(a.ws));
     if (o.sqerr) SCI_CUDA(cudaMemsetAsync(o.sqerr, 0, sizeof(double) * o.iters, s));
+    const bool aligned = ((reinterpret_cast<uintptr_t>(a.x0) | reinterpret_cast<uintptr_t>(a.x_out) |
+                           reinterpret_cast<uintptr_t>(a.y) | reinterpret_cast<uintptr_t>(a.phisum) |
+                           reinterpret_cast<uintptr_t>(a.bits)) & 15u) == 0;
+    if (!a.admm && a.bits && aligned && hw % 4 == 0 && tv_proj_supported(B, W, K)) {
+        // Fused iteration: a read-only pass forms the residual map c (and
+        // y1); the TV kernel applies x + lambda (c phi_b) while it loads x.
+        // x ping-pongs between x_out and xp; start so the last iterate
+        // lands in x_out.
+        float *X[2] = {a.x_out, w.xp};
+        const int start = o.iters & 1;
+        if (a.x0 != X[start])
+            SCI_CUDA(cudaMemcpyAsync(X[start], a.x0, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+        if (o.accelerate) SCI_CUDA(cudaMemsetAsync(w.y1, 0, sizeof(float) * hw, s));
+        for (int it = 0; it < o.iters; ++it) {
+            const float *cur = X[(start + it) & 1];
+            float *nxt = X[(start + it + 1) & 1];
+            int e = sci_gap_residual(cur, nullptr, a.bits, a.y, w.y1, a.phisum, w.c, o.accelerate,
+                                     B, H, W, s);
+            if (e) return e;
+            e = tv_launch_impl(cur, nxt, nullptr, B, H, W, hw, o.weights[it], o.eps, K,
+                               o.tv_steps ? o.tv_steps + (int64_t)it * B : nullptr, nullptr, w.tv,
+                               w.tv_bytes, s, 0, 0, a.bits, w.c, o.lambdas[it]);
+            if (e) return e;
+            if (o.orig && o.sqerr) {
+                e = sci_sqerr_accum(o.orig, nxt, n, o.sqerr + it, s);
+                if (e) return e;
+            }
+        }
+        return SCI_OK;
+    }
     if (!a.admm) {
         // gap_denoise: x = x0; y1 = 0  (pnp_sci_algo.py:633-635)
         if (a.x0 != a.x_out)

@@ -75,6 +75,25 @@ static int choose_R(int64_t nf, int nbands, int H) {
 // instead of 8 of 64) but doubles the registers of the pipeline state; 2
 // keeps ~1.3x more warps resident.  Measured at 2048 x 2048 x 24, 4 is
 // faster (0.44 vs 0.52 ms).  SCI_TV_CPL overrides the choice.
+// Work-item order (SCI_TV_ORDER: 0 bands of a frame adjacent, 1 frames of
+// a tile adjacent).  Frame-fastest is faster for both variants at
+// 2048 x 2048 x 24 (385 vs 395 us plain; the on-load projection shares the
+// tile's map rows across frames in L1/L2).
+static int frame_fast_order(bool) {
+    if (const char *e = getenv("SCI_TV_ORDER")) return atoi(e) ? 1 : 0;
+    return 1;
+}
+
+// Pipeline lag (1: chained stages, 2: independent stages); SCI_TV_LAG
+// overrides the choice.
+static int choose_lag() {
+    if (const char *e = getenv("SCI_TV_LAG")) {
+        const int v = atoi(e);
+        if (v == 1 || v == 2) return v;
+    }
+    return 1;
+}
+
 static int choose_cpl(int64_t W) {
     if (const char *e = getenv("SCI_TV_CPL")) {
         const int v = atoi(e);
@@ -85,11 +104,14 @@ static int choose_cpl(int64_t W) {
 
 // Host driver: all passes of one TV call.  Used by the C ABI and the solvers.
 // flags & 1: run all n_iter_max steps without the stop test (the unrolled,
-// differentiable form).
-int tv_launch_flags(const float *f, float *u, float *resid, int64_t nf, int64_t H, int64_t W,
-                    int64_t fs, float weight, float eps, int K, int *steps, double *energy_out,
-                    void *workspace, size_t ws_bytes, cudaStream_t s, int force_R, int flags) {
+// differentiable form).  proj (nullable): apply the GAP projection
+// f = x + lam (c phi_b) while loading the input x (see tv_proj_supported).
+int tv_launch_impl(const float *f, float *u, float *resid, int64_t nf, int64_t H, int64_t W,
+                   int64_t fs, float weight, float eps, int K, int *steps, double *energy_out,
+                   void *workspace, size_t ws_bytes, cudaStream_t s, int force_R, int flags,
+                   const uint32_t *proj_bits, const float *proj_c, float proj_lam) {
     const bool no_stop = (flags & 1) != 0;
+    const bool proj = proj_bits != nullptr;
     using namespace tv;
     SCI_CHECK_ARG(f && u && nf >= 1 && H >= 1 && W >= 1, "tv: bad arguments");
     SCI_CHECK_ARG(K >= 1, "tv: n_iter_max must be >= 1");
@@ -99,6 +121,10 @@ int tv_launch_flags(const float *f, float *u, float *resid, int64_t nf, int64_t 
     const size_t need = ws_layout(nf, H, W, K, nullptr, nullptr);
     SCI_CHECK_ARG(workspace && ws_bytes >= need, "tv: workspace of %zu bytes needed, got %zu",
                   need, ws_bytes);
+    if (proj) {
+        SCI_CHECK_ARG(proj_c && nf <= 32 && K >= 2 && K <= SMAX + 1 && !resid && !no_stop,
+                      "tv: on-load projection needs K in [2, 5], nf <= 32, no resid");
+    }
     if (K == 1) {
         k_copy_frames<<<(unsigned)std::min<int64_t>((nf * fs + 255) / 256, kSMs * 16), 256, 0, s>>>(
             f, u, resid, nf * fs, steps, (int)nf);
@@ -117,7 +143,8 @@ int tv_launch_flags(const float *f, float *u, float *resid, int64_t nf, int64_t 
         SCI_LAUNCHED("k_init_done");
     }
 
-    const int cpl = choose_cpl(W);
+    const int cpl = proj ? 4 : choose_cpl(W);
+    const int lag = proj ? 1 : choose_lag();
     const bool vec = (W % cpl == 0) && (fs % cpl == 0) &&
                      ((reinterpret_cast<uintptr_t>(f) | reinterpret_cast<uintptr_t>(u) |
                        reinterpret_cast<uintptr_t>(resid)) % (4 * cpl) == 0);
@@ -150,6 +177,12 @@ int tv_launch_flags(const float *f, float *u, float *resid, int64_t nf, int64_t 
         P.hl = round_up(SG + (PIN ? 1 : 0), cpl);
         P.own = 32 * cpl - P.hl - round_up(SG, cpl);
         P.ht = SG + (PIN ? 1 : 0);
+        P.lag = lag;
+        P.proj = proj ? 1 : 0;
+        P.bits = proj_bits;
+        P.cmap = proj_c;
+        P.lam = proj_lam;
+        P.frame_fast = frame_fast_order(proj);
         P.nbands = (int)((W + P.own - 1) / P.own);
         P.R = force_R > 0 ? force_R : choose_R(nf, P.nbands, (int)H);
         P.nchunks = (int)((H + P.R - 1) / P.R);
@@ -157,8 +190,11 @@ int tv_launch_flags(const float *f, float *u, float *resid, int64_t nf, int64_t 
         P.vec = vec ? 1 : 0;
         const int per_frame_blocks = (P.nbands * P.nchunks + WPB - 1) / WPB;
         P.gpf = std::max(1, std::min(per_frame_blocks, 16));
-        if (SG == SMAX) {
-            if (cpl == 2) launch_main4_c2(P, PIN, FINAL, s);
+        if (proj) {
+            launch_main_proj(P, SG, s);
+        } else if (SG == SMAX) {
+            if (lag == 2) launch_main4_lag2(P, PIN, FINAL, s);
+            else if (cpl == 2) launch_main4_c2(P, PIN, FINAL, s);
             else launch_main4_c4(P, PIN, FINAL, s);
         } else {
             launch_main123(P, SG, PIN, s);
@@ -167,7 +203,8 @@ int tv_launch_flags(const float *f, float *u, float *resid, int64_t nf, int64_t 
         // the stop test can change the result only when a step k in
         // [1, K-2] lies in this pass's window
         if (!no_stop && std::max(1, a) <= std::min(a + SG - 1, K - 2)) {
-            launch_fixup(P, PIN, s);
+            if (proj) launch_fixup_proj(P, s);
+            else launch_fixup(P, PIN, s);
             SCI_LAUNCHED("k_tv_fixup");
         }
         pin = P.p_out;
@@ -176,11 +213,30 @@ int tv_launch_flags(const float *f, float *u, float *resid, int64_t nf, int64_t 
     return SCI_OK;
 }
 
+int tv_launch_flags(const float *f, float *u, float *resid, int64_t nf, int64_t H, int64_t W,
+                    int64_t fs, float weight, float eps, int K, int *steps, double *energy_out,
+                    void *workspace, size_t ws_bytes, cudaStream_t s, int force_R, int flags) {
+    return tv_launch_impl(f, u, resid, nf, H, W, fs, weight, eps, K, steps, energy_out,
+                          workspace, ws_bytes, s, force_R, flags, nullptr, nullptr, 0.f);
+}
+
 int tv_launch(const float *f, float *u, float *resid, int64_t nf, int64_t H, int64_t W,
               int64_t fs, float weight, float eps, int K, int *steps, double *energy_out,
               void *workspace, size_t ws_bytes, cudaStream_t s, int force_R) {
     return tv_launch_flags(f, u, resid, nf, H, W, fs, weight, eps, K, steps, energy_out,
                            workspace, ws_bytes, s, force_R, 0);
+}
+
+// The on-load projection path covers one measurement of <= 32 frames with a
+// packed mask, 2..5 Chambolle steps (one pass) and 16-byte aligned rows.
+// It is opt-in (SCI_FUSED_PROJ=1): measured at 2048 x 2048 x 24 the fused
+// TV pass (552 us) costs more than the plain pass plus the separate
+// projection saves (385 + 179 us vs 552 + 73 us), because the extra loads
+// and registers slow the register-limited pipeline.
+bool tv_proj_supported(int64_t nf, int64_t W, int K) {
+    const char *e = getenv("SCI_FUSED_PROJ");
+    return e && atoi(e) != 0 && nf <= 32 && K >= 2 && K <= tv::SMAX + 1 && W % 4 == 0 &&
+           !getenv("SCI_TV_CPL") && !getenv("SCI_TV_LAG");
 }
 
 size_t tv_workspace_bytes(int64_t nf, int64_t H, int64_t W, int K) {

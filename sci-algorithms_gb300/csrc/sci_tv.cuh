@@ -45,6 +45,9 @@ namespace sci {
 namespace tv {
 
 constexpr int WPB = 4;             // warps per block
+#ifndef SCI_TV_PF
+#define SCI_TV_PF 2                // input prefetch distance in rows (1 or 2)
+#endif
 constexpr int SMAX = 4;            // dual updates per pass
 constexpr unsigned FULL = 0xffffffffu;
 
@@ -69,6 +72,15 @@ struct Pass {
     int vec;              // 1: rows are aligned for CPL-wide vector loads
     int cpl;              // columns per lane (2 or 4)
     int gpf;              // stop-test launch: blocks per frame
+    int lag;              // 1: stages chained within a step; 2: independent stages
+    // GAP projection applied while loading f (proj = 1): the stored stack
+    // holds x and f = x + lam * (c * phi_b) with phi_b = bit `frame` of the
+    // packed mask word and c the per-pixel residual map.
+    int proj;
+    const uint32_t *bits; // [H][W] packed binary mask
+    const float *cmap;    // [H][W] (y1 - A x) / Phi_sum
+    float lam;
+    int frame_fast;       // work-item order: 1 = frames of one tile adjacent
 };
 
 
@@ -146,6 +158,27 @@ __device__ __forceinline__ void store_row(float *rowp, int col, const Row<CPL> &
     }
 }
 
+// Input row of frame `frame`: the stored row, or with the GAP projection
+// applied on the fly (same arithmetic as k_proj_gap: x + lam * (c * phi_b)).
+template <int CPL, int MODE, int PROJ>
+__device__ __forceinline__ Row<CPL> load_f(const Pass &P, const float *fb, int frame, int64_t row,
+                                           int col, int W, bool vec) {
+    const Row<CPL> x = load_row<CPL, MODE>(fb + row * W, col, W, vec);
+    if (PROJ == 0) return x;
+    const Row<CPL> c = load_row<CPL, MODE>(P.cmap + row * W, col, W, vec);
+    const Row<CPL> wb =
+        load_row<CPL, MODE>(reinterpret_cast<const float *>(P.bits) + row * W, col, W, vec);
+    Row<CPL> f;
+#pragma unroll
+    for (int j = 0; j < CPL / 2; ++j) {
+        const float m0 = ((__float_as_uint(lo(wb.q[j])) >> frame) & 1u) ? 1.f : 0.f;
+        const float m1 = ((__float_as_uint(hi(wb.q[j])) >> frame) & 1u) ? 1.f : 0.f;
+        f.q[j] = mk2(fmaf(P.lam, lo(c.q[j]) * m0, lo(x.q[j])),
+                     fmaf(P.lam, hi(c.q[j]) * m1, hi(x.q[j])));
+    }
+    return f;
+}
+
 // Pipeline state between steps.
 template <int S, int CPL>
 struct St {
@@ -154,6 +187,7 @@ struct St {
     Row<CPL> pr[S + 1];          // p_k (row component) at the row of stage k+1
     Row<CPL> pc[S > 0 ? S : 1];  // p_k (column component) at the row of stage k+1
     Row<CPL> nf, nr, nc;         // next input row: f (and p_in planes when PIN)
+    Row<CPL> nf2;                // the input row after it (prefetch distance 2)
 };
 
 template <int S, int CPL>
@@ -166,7 +200,7 @@ __device__ __forceinline__ void zero_state(St<S, CPL> &A) {
     }
 #pragma unroll
     for (int k = 0; k <= S; ++k) A.pr[k] = zrow<CPL>();
-    A.nf = A.nr = A.nc = zrow<CPL>();
+    A.nf = A.nr = A.nc = A.nf2 = zrow<CPL>();
 }
 
 // Per-lane constants of a band.
@@ -197,11 +231,11 @@ __device__ __forceinline__ Row<CPL> divergence(const Row<CPL> &prn, const Row<CP
 
 // One pipeline step: input row r enters, stage k handles row r-k.
 // GEN: rows may be outside [r0, r1) or touch the frame's first/last row.
-template <int S, int CPL, bool PIN, bool OUT_U, bool ENERGY, int MODE, bool GEN>
+template <int S, int CPL, bool PIN, bool OUT_U, bool ENERGY, int MODE, bool GEN, int PROJ>
 __device__ __forceinline__ void step(const Pass &P, const St<S, CPL> &in, St<S, CPL> &out,
                                      int r, int rs, int r0, int r1, const Lane<CPL> &L,
                                      const float *fb, const float *pinb, float *ob, float *rb,
-                                     f2 (&ek)[S > 0 ? S : 1]) {
+                                     f2 (&ek)[S > 0 ? S : 1], int frame) {
     constexpr int NQ = CPL / 2;
     const int H = P.H, W = P.W;
     const bool vec = P.vec != 0;
@@ -209,10 +243,15 @@ __device__ __forceinline__ void step(const Pass &P, const St<S, CPL> &in, St<S, 
     const f2 one2 = mk2(1.f, 1.f), tw2 = mk2(P.tw, P.tw), nt2 = mk2(-P.tau, -P.tau);
     const f2 w2 = mk2(P.weight, P.weight);
 
-    // prefetch the next input row (clamped into the frame; unused past it)
+    // prefetch the input rows ahead (clamped into the frame; unused past it)
     {
         const int64_t rn = (int64_t)min(r + 1, H - 1) * W;
-        out.nf = load_row<CPL, MODE>(fb + rn, L.col, W, vec);
+        if (PIN || SCI_TV_PF == 1) {
+            out.nf = load_f<CPL, MODE, PROJ>(P, fb, frame, min(r + 1, H - 1), L.col, W, vec);
+        } else {
+            out.nf = in.nf2;
+            out.nf2 = load_f<CPL, MODE, PROJ>(P, fb, frame, min(r + 2, H - 1), L.col, W, vec);
+        }
         if (PIN) {
             out.nr = load_row<CPL, MODE>(pinb + rn, L.col, W, vec);
             out.nc = load_row<CPL, MODE>(pinb + hw + rn, L.col, W, vec);
@@ -327,7 +366,7 @@ __device__ __forceinline__ void step(const Pass &P, const St<S, CPL> &in, St<S, 
     }
 }
 
-template <int S, int CPL, bool PIN, bool OUT_U, bool ENERGY, int MODE>
+template <int S, int CPL, bool PIN, bool OUT_U, bool ENERGY, int MODE, int PROJ>
 __device__ __forceinline__ void run(const Pass &P, int frame, int chunk, int band, int lane) {
     const int H = P.H, W = P.W;
     Lane<CPL> L;
@@ -358,8 +397,9 @@ __device__ __forceinline__ void run(const Pass &P, int frame, int chunk, int ban
     f2 ek[S > 0 ? S : 1];
 #pragma unroll
     for (int k = 0; k < (S > 0 ? S : 1); ++k) ek[k].v = 0ull;
-    // first input row
-    A.nf = load_row<CPL, MODE>(fb + (int64_t)rs * W, L.col, W, vec);
+    // first input rows
+    A.nf = load_f<CPL, MODE, PROJ>(P, fb, frame, rs, L.col, W, vec);
+    A.nf2 = load_f<CPL, MODE, PROJ>(P, fb, frame, min(rs + 1, H - 1), L.col, W, vec);
     if (PIN) {
         A.nr = load_row<CPL, MODE>(pinb + (int64_t)rs * W, L.col, W, vec);
         A.nc = load_row<CPL, MODE>(pinb + hw + (int64_t)rs * W, L.col, W, vec);
@@ -373,16 +413,16 @@ __device__ __forceinline__ void run(const Pass &P, int frame, int chunk, int ban
     while (r <= rlast) {
         if (r == rfb && r + 1 <= rfe) {
             for (; r + 1 <= rfe; r += 2) {
-                step<S, CPL, PIN, OUT_U, ENERGY, MODE, false>(P, A, B, r, rs, r0, r1, L, fb, pinb,
-                                                               ob, rb, ek);
-                step<S, CPL, PIN, OUT_U, ENERGY, MODE, false>(P, B, A, r + 1, rs, r0, r1, L, fb,
-                                                               pinb, ob, rb, ek);
+                step<S, CPL, PIN, OUT_U, ENERGY, MODE, false, PROJ>(P, A, B, r, rs, r0, r1, L, fb,
+                                                                     pinb, ob, rb, ek, frame);
+                step<S, CPL, PIN, OUT_U, ENERGY, MODE, false, PROJ>(P, B, A, r + 1, rs, r0, r1, L,
+                                                                     fb, pinb, ob, rb, ek, frame);
             }
             continue;
         }
         // prologue (halo rows, first S steps) and epilogue (chunk tail, last row)
-        step<S, CPL, PIN, OUT_U, ENERGY, MODE, true>(P, A, B, r, rs, r0, r1, L, fb, pinb, ob, rb,
-                                                      ek);
+        step<S, CPL, PIN, OUT_U, ENERGY, MODE, true, PROJ>(P, A, B, r, rs, r0, r1, L, fb, pinb, ob,
+                                                            rb, ek, frame);
         A = B;
         ++r;
     }
@@ -400,26 +440,274 @@ __device__ __forceinline__ void run(const Pass &P, int frame, int chunk, int ban
     }
 }
 
-template <int S, int CPL, bool PIN, bool OUT_U, bool ENERGY>
-__device__ __forceinline__ void run_mode(const Pass &P, int frame, int chunk, int band, int lane) {
-    const int c0 = band * P.own - P.hl;
-    if (P.vec && c0 >= 0 && c0 + 32 * CPL - 1 <= P.W - 1)
-        run<S, CPL, PIN, OUT_U, ENERGY, INTERIOR>(P, frame, chunk, band, lane);
-    else
-        run<S, CPL, PIN, OUT_U, ENERGY, EDGE>(P, frame, chunk, band, lane);
+// ------------------------------------------------------- lag-2 pipeline
+// Stage k handles row r - 2k when input row r arrives, so it consumes only
+// rows its predecessor produced in the two previous steps: the S stages of
+// a step are independent of each other (S-fold instruction-level
+// parallelism per warp) at the cost of a two-row history per stage.
+template <int CPL>
+struct Slab {
+    Row<CPL> u, pr, pc, f;  // u_k, p_k (both components) and f of one row
+};
+
+template <int S, int CPL>
+struct St2 {
+    Slab<CPL> X1[S > 0 ? S : 1];  // newest row produced by stage k (k = 0..S-1)
+    Slab<CPL> X2[S > 0 ? S : 1];  // the row before it
+    Row<CPL> ps1;                 // stage S: its previous row of p_S (row component)
+    Row<CPL> nf, nr, nc;          // next input row
+};
+
+template <int CPL>
+__device__ __forceinline__ Slab<CPL> zslab() {
+    Slab<CPL> z;
+    z.u = z.pr = z.pc = z.f = zrow<CPL>();
+    return z;
 }
 
-// Decodes a warp's work item: (frame, row chunk, column band).
-__device__ __forceinline__ bool decode_item(const Pass &P, int &frame, int &chunk, int &band) {
-    const int warp = threadIdx.x >> 5;
+template <int S, int CPL, bool PIN, bool OUT_U, bool ENERGY, int MODE, bool GEN>
+__device__ __forceinline__ void step2(const Pass &P, const St2<S, CPL> &in, St2<S, CPL> &out,
+                                      int r, int rs, int r0, int r1, const Lane<CPL> &L,
+                                      const float *fb, const float *pinb, float *ob, float *rb,
+                                      f2 (&ek)[S > 0 ? S : 1]) {
+    constexpr int NQ = CPL / 2;
+    const int H = P.H, W = P.W;
+    const bool vec = P.vec != 0;
+    const int64_t hw = (int64_t)H * W;
+    const f2 one2 = mk2(1.f, 1.f), tw2 = mk2(P.tw, P.tw), nt2 = mk2(-P.tau, -P.tau);
+    const f2 w2 = mk2(P.weight, P.weight);
+
+    {   // prefetch the next input row (clamped into the frame; unused past it)
+        const int64_t rn = (int64_t)min(r + 1, H - 1) * W;
+        out.nf = load_row<CPL, MODE>(fb + rn, L.col, W, vec);
+        if (PIN) {
+            out.nr = load_row<CPL, MODE>(pinb + rn, L.col, W, vec);
+            out.nc = load_row<CPL, MODE>(pinb + hw + rn, L.col, W, vec);
+        }
+    }
+
+    // ---------------- stages S..1: row i = r - 2k, inputs from earlier steps
+#pragma unroll
+    for (int k = S; k >= 1; --k) {
+        const int i = r - 2 * k;
+        const bool act = !GEN || (i >= rs && i < H);
+        if (!act) {  // warp-uniform
+            if (k < S) out.X1[k] = zslab<CPL>();
+            else out.ps1 = zrow<CPL>();
+            continue;
+        }
+        const Slab<CPL> &a = in.X2[k - 1];  // stage k-1, row i
+        const Slab<CPL> &b = in.X1[k - 1];  // stage k-1, row i+1
+        const Row<CPL> &pru = (k < S) ? in.X1[k].pr : in.ps1;  // p_k row i-1
+        const float uR = __shfl_down_sync(FULL, lo(a.u.q[0]), 1);
+        const bool last_row = GEN && (i == H - 1);
+        Row<CPL> gr, gc, n, prn, pcn;
+#pragma unroll
+        for (int j = 0; j < NQ; ++j) {
+            const f2 right = mk2(hi(a.u.q[j]), j + 1 < NQ ? lo(a.u.q[j + 1]) : uR);
+            gc.q[j] = sub2(right, a.u.q[j]);
+            if (MODE != INTERIOR) gc.q[j] = mul2(gc.q[j], L.gmask.q[j]);
+            gr.q[j] = last_row ? mk2(0.f, 0.f) : sub2(b.u.q[j], a.u.q[j]);
+            const f2 s2 = fma2(gr.q[j], gr.q[j], mul2(gc.q[j], gc.q[j]));
+            n.q[j] = mk2(sqrt_approx(lo(s2)), sqrt_approx(hi(s2)));
+            const f2 den = fma2(tw2, n.q[j], one2);
+            const f2 ri = mk2(rcp_approx(lo(den)), rcp_approx(hi(den)));
+            const bool p0zero = (k == 1 && !PIN);
+            const f2 qr = p0zero ? mk2(0.f, 0.f) : a.pr.q[j];
+            const f2 qc = p0zero ? mk2(0.f, 0.f) : a.pc.q[j];
+            prn.q[j] = mul2(fma2(nt2, gr.q[j], qr), ri);
+            pcn.q[j] = mul2(fma2(nt2, gc.q[j], qc), ri);
+        }
+        const Row<CPL> d = divergence<CPL>(prn, pcn, pru, L.first_col);
+        Row<CPL> uk;
+#pragma unroll
+        for (int j = 0; j < NQ; ++j) uk.q[j] = sub2(a.f.q[j], d.q[j]);
+        if (ENERGY && (!GEN || (i >= r0 && i < r1))) {
+#pragma unroll
+            for (int j = 0; j < NQ; ++j) {
+                if (MODE == INTERIOR) {
+                    ek[k - 1] = fma2(w2, n.q[j], ek[k - 1]);
+                    if (k < S) ek[k] = fma2(d.q[j], d.q[j], ek[k]);
+                } else {
+                    ek[k - 1] = fma2(mul2(w2, L.mk.q[j]), n.q[j], ek[k - 1]);
+                    if (k < S) ek[k] = fma2(mul2(L.mk.q[j], d.q[j]), d.q[j], ek[k]);
+                }
+            }
+        }
+        if (k == S) {
+            out.ps1 = prn;
+            if (!GEN || (i >= r0 && i < r1)) {
+                const int64_t ro = (int64_t)i * W;
+                if (OUT_U) {
+                    store_row<CPL, MODE>(ob + ro, L.col, uk, L.lane_own, L.mk, vec);
+                    if (rb) {
+                        Row<CPL> dr;
+#pragma unroll
+                        for (int j = 0; j < NQ; ++j) dr.q[j] = sub2(uk.q[j], a.f.q[j]);
+                        store_row<CPL, MODE>(rb + ro, L.col, dr, L.lane_own, L.mk, vec);
+                    }
+                } else {
+                    store_row<CPL, MODE>(ob + ro, L.col, prn, L.lane_own, L.mk, vec);
+                    store_row<CPL, MODE>(ob + hw + ro, L.col, pcn, L.lane_own, L.mk, vec);
+                }
+            }
+        } else {
+            Slab<CPL> o;
+            o.u = uk;
+            o.pr = prn;
+            o.pc = pcn;
+            o.f = a.f;
+            out.X1[k] = o;
+        }
+    }
+    // history shift
+#pragma unroll
+    for (int k = 0; k < S; ++k) out.X2[k] = in.X1[k];
+
+    // ---------------- stage 0: u_0 at row r
+    const bool act0 = !GEN || (r < H);
+    const Row<CPL> fr = act0 ? in.nf : zrow<CPL>();
+    Slab<CPL> o0;
+    o0.u = fr;
+    o0.f = fr;
+    o0.pr = zrow<CPL>();
+    o0.pc = zrow<CPL>();
+    if (PIN) {
+        const Row<CPL> qr = act0 ? in.nr : zrow<CPL>();
+        const Row<CPL> qc = act0 ? in.nc : zrow<CPL>();
+        const Row<CPL> &pru0 = (S > 0) ? in.X1[0].pr : in.ps1;
+        const Row<CPL> d = divergence<CPL>(qr, qc, pru0, L.first_col);
+#pragma unroll
+        for (int j = 0; j < NQ; ++j) o0.u.q[j] = sub2(fr.q[j], d.q[j]);
+        if (ENERGY && act0 && (!GEN || (r >= r0 && r < r1))) {
+#pragma unroll
+            for (int j = 0; j < NQ; ++j)
+                ek[0] = (MODE == INTERIOR) ? fma2(d.q[j], d.q[j], ek[0])
+                                           : fma2(mul2(L.mk.q[j], d.q[j]), d.q[j], ek[0]);
+        }
+        o0.pr = qr;
+        o0.pc = qc;
+        if (S == 0) {
+            out.ps1 = qr;
+            if (OUT_U && act0 && (!GEN || (r >= r0 && r < r1))) {
+                const int64_t ro = (int64_t)r * W;
+                store_row<CPL, MODE>(ob + ro, L.col, o0.u, L.lane_own, L.mk, vec);
+                if (rb) {
+                    Row<CPL> dr;
+#pragma unroll
+                    for (int j = 0; j < NQ; ++j) dr.q[j] = sub2(o0.u.q[j], fr.q[j]);
+                    store_row<CPL, MODE>(rb + ro, L.col, dr, L.lane_own, L.mk, vec);
+                }
+            }
+        }
+    }
+    if (S > 0) out.X1[0] = o0;
+}
+
+template <int S, int CPL, bool PIN, bool OUT_U, bool ENERGY, int MODE>
+__device__ __forceinline__ void run2(const Pass &P, int frame, int chunk, int band, int lane) {
+    const int H = P.H, W = P.W;
+    Lane<CPL> L;
+    L.col = band * P.own - P.hl + lane * CPL;
+    const int r0 = chunk * P.R, r1 = min(r0 + P.R, H);
+    const int rs = max(0, r0 - P.ht);
+    const int own_lo = band * P.own, own_hi = min(own_lo + P.own, W);
+    L.lane_own = (L.col >= own_lo) && (L.col + CPL <= own_hi);
+    L.first_col = (MODE != INTERIOR) && (L.col == 0);
+#pragma unroll
+    for (int j = 0; j < CPL / 2; ++j) {
+        const int c = L.col + 2 * j;
+        L.mk.q[j] = mk2((c >= own_lo && c < own_hi) ? 1.f : 0.f,
+                        (c + 1 >= own_lo && c + 1 < own_hi) ? 1.f : 0.f);
+        L.gmask.q[j] = mk2(c == W - 1 ? 0.f : 1.f, c + 1 == W - 1 ? 0.f : 1.f);
+    }
+    const int64_t hw = (int64_t)H * W;
+    const float *fb = P.f + (int64_t)frame * P.fs;
+    const float *pinb = PIN ? P.p_in + (int64_t)frame * 2 * hw : nullptr;
+    float *ob = OUT_U ? P.u + (int64_t)frame * P.fs : P.p_out + (int64_t)frame * 2 * hw;
+    float *rb = (OUT_U && P.resid) ? P.resid + (int64_t)frame * P.fs : nullptr;
+    const bool vec = P.vec != 0;
+
+    St2<S, CPL> A, B;
+#pragma unroll
+    for (int k = 0; k < (S > 0 ? S : 1); ++k) A.X1[k] = A.X2[k] = zslab<CPL>();
+    A.ps1 = A.nr = A.nc = zrow<CPL>();
+    f2 ek[S > 0 ? S : 1];
+#pragma unroll
+    for (int k = 0; k < (S > 0 ? S : 1); ++k) ek[k].v = 0ull;
+    A.nf = load_row<CPL, MODE>(fb + (int64_t)rs * W, L.col, W, vec);
+    if (PIN) {
+        A.nr = load_row<CPL, MODE>(pinb + (int64_t)rs * W, L.col, W, vec);
+        A.nc = load_row<CPL, MODE>(pinb + hw + (int64_t)rs * W, L.col, W, vec);
+    }
+    const int rlast = min(r1 - 1 + 2 * S, H - 1 + 2 * S);
+    const int rfb = r0 + 2 * S;
+    const int rfe = min((PIN || S == 0) ? r1 - 1 : r1 + 1, H - 1);
+    int r = rs;
+    while (r <= rlast) {
+        if (r == rfb && r + 1 <= rfe) {
+            for (; r + 1 <= rfe; r += 2) {
+                step2<S, CPL, PIN, OUT_U, ENERGY, MODE, false>(P, A, B, r, rs, r0, r1, L, fb,
+                                                                pinb, ob, rb, ek);
+                step2<S, CPL, PIN, OUT_U, ENERGY, MODE, false>(P, B, A, r + 1, rs, r0, r1, L, fb,
+                                                                pinb, ob, rb, ek);
+            }
+            continue;
+        }
+        step2<S, CPL, PIN, OUT_U, ENERGY, MODE, true>(P, A, B, r, rs, r0, r1, L, fb, pinb, ob,
+                                                       rb, ek);
+        A = B;
+        ++r;
+    }
+    if (ENERGY) {
+        const float lm = (MODE == INTERIOR) ? (L.lane_own ? 1.f : 0.f) : 1.f;
+        double *eb = P.energy + (int64_t)frame * P.K * 2;
+#pragma unroll
+        for (int k = 0; k < (S > 0 ? S : 1); ++k) {
+            double v = (double)((lo(ek[k]) + hi(ek[k])) * lm);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
+            if (lane == 0) atomicAdd(eb + 2 * (P.a + k), v);
+        }
+    }
+}
+
+template <int S, int CPL, bool PIN, bool OUT_U, bool ENERGY, int LAG = 1, int PROJ = 0>
+__device__ __forceinline__ void run_mode(const Pass &P, int frame, int chunk, int band, int lane) {
+    const int c0 = band * P.own - P.hl;
+    const bool interior = P.vec && c0 >= 0 && c0 + 32 * CPL - 1 <= P.W - 1;
+    if (LAG == 2) {
+        if (interior) run2<S, CPL, PIN, OUT_U, ENERGY, INTERIOR>(P, frame, chunk, band, lane);
+        else run2<S, CPL, PIN, OUT_U, ENERGY, EDGE>(P, frame, chunk, band, lane);
+    } else {
+        if (interior) run<S, CPL, PIN, OUT_U, ENERGY, INTERIOR, PROJ>(P, frame, chunk, band, lane);
+        else run<S, CPL, PIN, OUT_U, ENERGY, EDGE, PROJ>(P, frame, chunk, band, lane);
+    }
+}
+
+// Decodes a work item: (frame, row chunk, column band).  With frame_fast
+// the frames of one tile are adjacent items (they share the tile's rows of
+// the per-pixel maps in L1/L2); otherwise the bands of one frame are.
+__device__ __forceinline__ bool decode_index(const Pass &P, int64_t item, int &frame, int &chunk,
+                                             int &band) {
     const int64_t per_frame = (int64_t)P.nbands * P.nchunks;
-    const int64_t item = (int64_t)blockIdx.x * WPB + warp;
     if (item >= per_frame * P.nf) return false;
-    frame = (int)(item / per_frame);
-    const int rem = (int)(item - (int64_t)frame * per_frame);
+    int rem;
+    if (P.frame_fast) {
+        const int64_t tile = item / P.nf;
+        frame = (int)(item - tile * P.nf);
+        rem = (int)tile;
+    } else {
+        frame = (int)(item / per_frame);
+        rem = (int)(item - (int64_t)frame * per_frame);
+    }
     chunk = rem / P.nbands;
     band = rem - chunk * P.nbands;
     return true;
+}
+
+__device__ __forceinline__ bool decode_item(const Pass &P, int &frame, int &chunk, int &band) {
+    return decode_index(P, (int64_t)blockIdx.x * WPB + (threadIdx.x >> 5), frame, chunk, band);
 }
 
 // First j in this pass's window with |E_{j-1} - E_j| < eps * E_0, or -1.
@@ -444,52 +732,52 @@ template <int CPL>
 constexpr int min_blocks() { return CPL == 2 ? 4 : 3; }
 
 // Main launch of one pass: every frame not yet stopped runs all SG updates.
-template <int SG, bool PIN, bool FINAL, int CPL>
+template <int SG, bool PIN, bool FINAL, int CPL, int LAG = 1, int PROJ = 0>
 __global__ void __launch_bounds__(WPB * 32, min_blocks<CPL>()) k_tv_main(Pass P) {
     int frame, chunk, band;
     if (!decode_item(P, frame, chunk, band)) return;
     if (PIN && P.done[frame] >= 0) return;  // stopped in an earlier pass
-    run_mode<SG, CPL, PIN, FINAL, true>(P, frame, chunk, band, threadIdx.x & 31);
+    run_mode<SG, CPL, PIN, FINAL, true, LAG, PROJ>(P, frame, chunk, band, threadIdx.x & 31);
 }
 
-// Stop-test launch of one pass, P.gpf blocks per frame: frames whose rule
-// fires at j inside the window [a, a+S-1] are recomputed with j - a updates
-// and write u_j; the other frames' blocks exit after reading 2K doubles.
-template <bool PIN, int CPL>
+// Stop-test launch of one pass over the same work items as the main launch:
+// frames whose rule fires at j inside the window [a, a+S-1] are recomputed
+// (by all their items at once) with j - a updates and write u_j; the other
+// items exit after reading a few doubles.
+template <bool PIN, int CPL, int PROJ = 0>
 __global__ void __launch_bounds__(WPB * 32, min_blocks<CPL>()) k_tv_fixup(Pass P) {
-    const int frame = blockIdx.x / P.gpf, g = blockIdx.x - frame * P.gpf;
-    if (frame >= P.nf) return;
+    int frame, chunk, band;
+    if (!decode_item(P, frame, chunk, band)) return;
     if (PIN) {
         const int d = P.done[frame];
         if (d >= 0 && d < P.a) return;  // stopped in an earlier window
     }
     const int j = find_stop(P, frame);
-    const bool lead = (g == 0 && threadIdx.x == 0);
+    const int lane = threadIdx.x & 31;
+    const bool lead = (chunk == 0 && band == 0 && lane == 0);
     if (j < 0) {
         if (lead && P.steps && P.a + P.S == P.K - 1) P.steps[frame] = P.K;
         return;
     }
     if (lead) {
-        P.done[frame] = j;
+        P.done[frame] = j;  // every warp of this frame computes the same j
         if (P.steps) P.steps[frame] = j + 1;
     }
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int per_frame = P.nbands * P.nchunks;
-    for (int it = g * WPB + warp; it < per_frame; it += P.gpf * WPB) {
-        const int chunk = it / P.nbands, band = it - chunk * P.nbands;
-        switch (j - P.a) {
-            case 0: if constexpr (PIN) run_mode<0, CPL, PIN, true, false>(P, frame, chunk, band, lane); break;
-            case 1: run_mode<1, CPL, PIN, true, false>(P, frame, chunk, band, lane); break;
-            case 2: run_mode<2, CPL, PIN, true, false>(P, frame, chunk, band, lane); break;
-            case 3: run_mode<3, CPL, PIN, true, false>(P, frame, chunk, band, lane); break;
-            default: break;
-        }
+    switch (j - P.a) {
+        case 0: if constexpr (PIN) run_mode<0, CPL, PIN, true, false, 1, PROJ>(P, frame, chunk, band, lane); break;
+        case 1: run_mode<1, CPL, PIN, true, false, 1, PROJ>(P, frame, chunk, band, lane); break;
+        case 2: run_mode<2, CPL, PIN, true, false, 1, PROJ>(P, frame, chunk, band, lane); break;
+        case 3: run_mode<3, CPL, PIN, true, false, 1, PROJ>(P, frame, chunk, band, lane); break;
+        default: break;
     }
 }
 
 // Host launchers (one translation unit each, compiled in parallel).
 void launch_main4_c4(const Pass &P, bool pin, bool final_pass, cudaStream_t s);
 void launch_main4_c2(const Pass &P, bool pin, bool final_pass, cudaStream_t s);
+void launch_main4_lag2(const Pass &P, bool pin, bool final_pass, cudaStream_t s);
+void launch_main_proj(const Pass &P, int SG, cudaStream_t s);
+void launch_fixup_proj(const Pass &P, cudaStream_t s);
 void launch_main123(const Pass &P, int SG, bool pin, cudaStream_t s);
 void launch_fixup(const Pass &P, bool pin, cudaStream_t s);
 

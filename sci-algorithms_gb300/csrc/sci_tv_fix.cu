@@ -5,7 +5,7 @@ namespace sci {
 namespace tv {
 
 void launch_fixup(const Pass &P, bool pin, cudaStream_t s) {
-    const unsigned g = (unsigned)(P.nf * P.gpf);
+    const unsigned g = pass_blocks(P);
     if (P.cpl == 2) {
         if (pin) k_tv_fixup<true, 2><<<g, WPB * 32, 0, s>>>(P);
         else k_tv_fixup<false, 2><<<g, WPB * 32, 0, s>>>(P);

@@ -162,3 +162,25 @@ def test_run_host_end_to_end():
     assert not x_host.is_cuda
     ref = s.run(_dev.plane(meas)).cpu()
     assert torch.equal(x_host, ref)
+
+
+@pytest.mark.parametrize("eps", [2e-4, 0.05])
+@pytest.mark.parametrize("iters", [7, 8])
+def test_fused_projection_path_is_bitwise_equal(monkeypatch, eps, iters):
+    """The fused iteration (residual map + projection applied while the TV
+    kernel loads x) against the two-kernel iteration, including early stops
+    of the TV inside the fused kernel (eps = 0.05)."""
+    orig, mask, meas = sci.datasets.video_config(64, 96, 8)
+    op = sci.MaskOperator(mask)
+    y = _dev.plane(meas)
+    monkeypatch.setenv("SCI_FUSED_PROJ", "1")
+    fused = sci.Solver(op, "gap", iters, 1.0, 0.1, 5, eps=eps, use_graph=False)
+    a = fused.run(y, tv_steps=True).clone()
+    sa = fused.tv_steps.clone()
+    monkeypatch.delenv("SCI_FUSED_PROJ")
+    plain = sci.Solver(op, "gap", iters, 1.0, 0.1, 5, eps=eps, use_graph=False)
+    b = plain.run(y, tv_steps=True).clone()
+    assert torch.equal(a, b)
+    assert torch.equal(sa, plain.tv_steps)
+    if eps > 0.01:
+        assert int((sa < 5).sum()) > 0  # the stop test fired somewhere
