@@ -13,6 +13,13 @@ Also reported on the same JSON line:
                 measurement in, host result out, copies inside the timed region
   cpu_baseline  the numpy port of the reference path on a bounded sample
   admm          ADMM-TV iterations per second on the same workload
+  cassi         spectral GAP-TV (256 x 256 x 28 cube, 2-pixel dispersion onto
+                256 x 310, 80 iterations): iterations per second
+  unrolled      differentiable unrolled GAP-TV (16 x 256 x 256 x 8, K = 20, 5 TV
+                steps): hand-written forward+backward ms vs plain-torch autograd
+                of the same loop, and the gradients' relative difference
+  batched       64 uneven measurements (H = W in 128..1024, B in 8..32), 50
+                GAP-TV iterations each, one graph: ms per batch
 
 ``--impl reference`` times the reference's CPU implementation (the numpy
 port in oracle/, the reference being Python) on a bounded sample instead.
@@ -253,6 +260,8 @@ def run_gpu(args):
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         ms_e2e = float(t.item())
 
+    extras = {} if args.no_extras else side_workloads(dev)
+
     if rank == 0:
         cpu_v, cpu_note, _ = (None, None, None)
         if world == 1 and not args.no_cpu:
@@ -278,9 +287,12 @@ def run_gpu(args):
             "e2e": {"value": world * ITERS * 1e3 / ms_e2e, "unit": "iter/s",
                     "h2d_bytes_per_step": 4 * H * W, "d2h_bytes_per_step": 4 * n,
                     "ms_per_step": ms_e2e},
-            "gpu_launches": args.steps * ITERS * 4,
+            # per solve: x0 = At(y), then per iteration projection, TV pass,
+            # stop-test launch
+            "gpu_launches": args.steps * (1 + ITERS * 3),
             "clocks": clk,
         }
+        line.update(extras)
         if cpu_v is not None:
             line["cpu_baseline"] = {"value": cpu_v, "unit": "iter/s", "cores": 1,
                                     "kind": "port", "sample": cpu_note}
@@ -329,6 +341,85 @@ def run_kernel(args):
                       "ms_per_launch": e0.elapsed_time(e1) / args.launches}))
 
 
+def side_workloads(dev):
+    """The spectral (CASSI) and differentiable workloads, timed with events."""
+    import torch
+    import sci_algorithms_gb300 as sci
+    from sci_algorithms_gb300 import _dev
+    from sci_algorithms_gb300.unrolled import torch_unrolled_loss, unrolled_loss
+    out = {}
+    stream = torch.cuda.current_stream()
+
+    def ev_time(fn, reps, warm=2):
+        for _ in range(warm):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        return e0.elapsed_time(e1) / reps
+
+    # spectral: 256 x 256 x 28, step 2, 80 iterations
+    L, it = 28, 80
+    cube = sci.datasets.spectral_cube(256, 256, L, seed=0)
+    phi = sci.datasets.bernoulli_mask(256, 256, 1, seed=1)[..., 0]
+    op = sci.CassiOperator(phi, L, 2)
+    yd = op.forward(torch.from_numpy(cube).float().to(dev))
+    cs = sci.CassiSolver(op, it, 1.0, 0.05, 5)
+    ms = ev_time(lambda: cs.run(yd), 10)
+    out["cassi"] = {"workload": "cassi_256x256x28_step2", "iters": it, "value": it * 1e3 / ms,
+                    "unit": "iter/s", "ms_per_solve": ms}
+
+    # differentiable unrolled GAP-TV: 16 x 8 x 256 x 256, K = 20
+    N, B, H, W, K = 16, 8, 256, 256, 20
+    xs = [sci.datasets.video_scene(H, W, B, seed=n) for n in range(N)]
+    xt = torch.from_numpy(np.stack([np.moveaxis(x, -1, 0) for x in xs])).float().to(dev)
+    g = torch.Generator().manual_seed(0)
+    logits0 = torch.randn((B, H, W), generator=g).to(dev)
+    lam0 = torch.full((K,), 0.1, device=dev)
+    ws = sci.unrolled_workspace(N, B, H, W, K, 5, dev)
+    res = {}
+
+    def ours():
+        lg = logits0.clone().requires_grad_(True)
+        lm = lam0.clone().requires_grad_(True)
+        unrolled_loss(lg, lm, xt, K=K, ws=ws).backward()
+        res["ours"] = (lg.grad, lm.grad)
+
+    def ref():
+        lg = logits0.clone().requires_grad_(True)
+        lm = lam0.clone().requires_grad_(True)
+        torch_unrolled_loss(lg, lm, xt, K=K).backward()
+        res["ref"] = (lg.grad, lm.grad)
+
+    ms_ours = ev_time(ours, 5)
+    ms_ref = ev_time(ref, 3, warm=1)
+    ga, gb = res["ours"][0].double(), res["ref"][0].double()
+    la, lb = res["ours"][1].double(), res["ref"][1].double()
+    out["unrolled"] = {"workload": "unrolled_gaptv_16x256x256x8_K20", "fwd_bwd_ms": ms_ours,
+                       "autograd_fwd_bwd_ms": ms_ref, "speedup": ms_ref / ms_ours,
+                       "grad_logits_rel_diff": float((ga - gb).norm() / gb.norm()),
+                       "grad_lambda_rel_diff": float((la - lb).norm() / lb.norm())}
+    # batched uneven solve: 64 measurements, H = W in {128..1024}, B in {8..32}
+    meas, masks, elems = [], [], 0
+    for orig, mask, y in sci.datasets.batch_config(64, seed=0):
+        meas.append(torch.from_numpy(y).float().to(dev))
+        masks.append(torch.from_numpy(mask).float().to(dev))
+        elems += mask.size
+        del orig
+    bsol = sci.BatchSolver(meas, masks, iters=50, tv_weight=0.1, autotune=True)
+    del masks
+    ms_b = ev_time(lambda: bsol.run(), 3, warm=1)
+    out["batched"] = {"workload": "batch64_uneven_128-1024_B8-32", "items": 64, "iters": 50,
+                      "elements": elems, "ms_per_batch": ms_b,
+                      "element_iters_per_s": elems * 50 / (ms_b * 1e-3),
+                      "chunk_rows": sorted(set(bsol.chunk_rows()))}
+    return out
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -337,6 +428,8 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--ref-crop", type=int, default=1024)
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the spectral and differentiable side workloads")
     ap.add_argument("--kernel", choices=["tv", "proj"], default=None,
                     help="profiling mode: time one kernel on a 2048x2048xFRAMES stack")
     ap.add_argument("--frames", type=int, default=8)

@@ -214,6 +214,43 @@ int sci_cassi_gap_tv(const float *y, const float *phi, const float *phisum,
                      int64_t W, int step, const sci_solve_opts *opts,
                      void *workspace, size_t workspace_bytes, void *stream);
 
+/* ------------------------------------- batched uneven GAP-TV (K5) */
+/* One measurement of a batch: device pointers (y: H x W, mask_bits: packed
+ * binary mask, one uint32 word per pixel, bit b = frame b, B <= 32;
+ * phisum: H x W; x: B x H x W, in: x0 (unless init_x0), out: result),
+ * sizes (W % 4 == 0, 16-byte aligned buffers), step size, TV weight, and
+ * the TV row-chunk height R (0: default; sci_batch_autotune fills it). */
+typedef struct sci_batch_item {
+    const float *y;
+    const uint32_t *mask_bits;
+    const float *phisum;
+    float *x;
+    int64_t B, H, W;
+    float lambda;
+    float tv_weight;
+    int R;
+} sci_batch_item;
+
+int sci_batch_workspace_bytes(const sci_batch_item *items, int n, int tv_iter_max,
+                              size_t *bytes);
+
+/* Times the TV pass of each distinct (B, H, W) for a set of row-chunk
+ * heights on the item's own data and writes the fastest into items[i].R
+ * (cached per process).  Synchronises the stream. */
+int sci_batch_autotune(sci_batch_item *items, int n, int tv_iter_max,
+                       void *workspace, size_t workspace_bytes, void *stream);
+
+/* GAP-TV (pnp_sci_algo.py:536-706, denoiser='tv') of n <= 256 independent
+ * measurements: `iters` iterations, all items advancing together; each
+ * phase is one launch over the tiles of every item, and with use_graph the
+ * whole loop is captured once into a cached CUDA graph.  init_x0: start
+ * from At(y / phisum) (else from x).  tv_iter_max in [2, 5].  The item
+ * table is uploaded synchronously before the work is enqueued. */
+int sci_batch_gap_tv(const sci_batch_item *items, int n, int iters,
+                     int tv_iter_max, float eps, int accelerate, int init_x0,
+                     int use_graph, void *workspace, size_t workspace_bytes,
+                     void *stream);
+
 /* ------------------------------- differentiable unrolled GAP-TV (K4) */
 /* A batch of N scenes x_true (N x B x H x W) sharing one learnable mask
  * Phi = sigmoid(logits) (B x H x W) and per-iteration step sizes

@@ -16,4 +16,5 @@ from .solver import Solver  # noqa: F401
 from .cassi import CassiOperator, CassiSolver, make_cassi_ops  # noqa: F401
 from .unrolled import (UnrolledGapTV, unrolled_loss, unrolled_workspace,  # noqa: F401
                        torch_unrolled_loss)
+from .batch import BatchSolver  # noqa: F401
 from . import datasets  # noqa: F401

@@ -42,6 +42,13 @@ class SolveOpts(ctypes.Structure):
                 ("use_graph", ctypes.c_int)]
 
 
+class BatchItem(ctypes.Structure):
+    """``sci_batch_item`` of include/sci_gb300.h."""
+    _fields_ = [("y", c_vp), ("mask_bits", c_vp), ("phisum", c_vp), ("x", c_vp),
+                ("B", c_i64), ("H", c_i64), ("W", c_i64), ("lam", c_f), ("tv_weight", c_f),
+                ("R", ctypes.c_int)]
+
+
 # name -> argtypes (all functions return int status)
 _SIGS = {
     "sci_version": [],
@@ -75,6 +82,12 @@ _SIGS = {
                                   ctypes.POINTER(c_sz)],
     "sci_cassi_gap_tv": [c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, ctypes.c_int,
                          ctypes.POINTER(SolveOpts), c_vp, c_sz, c_vp],
+    "sci_batch_workspace_bytes": [ctypes.POINTER(BatchItem), ctypes.c_int, ctypes.c_int,
+                                  ctypes.POINTER(c_sz)],
+    "sci_batch_autotune": [ctypes.POINTER(BatchItem), ctypes.c_int, ctypes.c_int, c_vp, c_sz,
+                           c_vp],
+    "sci_batch_gap_tv": [ctypes.POINTER(BatchItem), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                         c_f, ctypes.c_int, ctypes.c_int, ctypes.c_int, c_vp, c_sz, c_vp],
     "sci_unrolled_workspace_bytes": [c_i64, c_i64, c_i64, c_i64, ctypes.c_int, ctypes.c_int,
                                      ctypes.POINTER(c_sz)],
     "sci_unrolled_fwd": [c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_i64, ctypes.c_int,

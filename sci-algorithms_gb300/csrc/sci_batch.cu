@@ -1,0 +1,428 @@
+// Batched GAP-TV over many measurements of uneven sizes.
+//
+// The reference reconstructs coded-frame blocks one after another
+// (admmdenoise_cacti's frame-block loop, PnP_SCI/python/pnp_sci_algo.py:498);
+// here a batch of independent measurements (each with its own H x W x B and
+// packed binary mask) advances together.  Every phase of an iteration is
+// one launch over a work queue spanning all items: the GAP projection over
+// 256-pixel tiles of every item, then the Chambolle TV pass over every
+// item's (frame, row chunk, column band) tiles, then the stop-test launch
+// over the same tiles.  Items are found from the tile index through prefix
+// tables in a device-resident item table.  The whole multi-iteration loop is
+// captured once into a CUDA graph and replayed.  An autotuner times the TV
+// row-chunk height per distinct frame shape on the item's own data.
+#include <algorithm>
+#include <cstring>
+#include <list>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "sci_tv.cuh"
+
+namespace sci {
+
+int tv_launch(const float *f, float *u, float *resid, int64_t nf, int64_t H, int64_t W,
+              int64_t fs, float weight, float eps, int K, int *steps, double *energy_out,
+              void *workspace, size_t ws_bytes, cudaStream_t s, int force_R);
+size_t tv_workspace_bytes(int64_t nf, int64_t H, int64_t W, int K);
+
+namespace batch {
+
+constexpr int MAXI = 256;  // items per batch
+constexpr int PROJ_T = 256;
+
+struct Item {
+    tv::Pass tv;  // f = xp (projected stack), u = x
+    const float *y;
+    const uint32_t *bits;
+    const float *phisum;
+    float *x, *xp, *y1;
+    int B;
+    int64_t hw;
+    float lam;
+};
+
+struct Table {
+    int n;
+    int proj_prefix[MAXI + 1];  // 256-pixel tiles
+    int tv_prefix[MAXI + 1];    // warp work items
+    Item it[MAXI];
+};
+
+__device__ __forceinline__ int find_item(const int *prefix, int n, int g) {
+    int lo = 0, hi = n;  // prefix[lo] <= g < prefix[hi]
+    while (hi - lo > 1) {
+        const int mid = (lo + hi) >> 1;
+        if (prefix[mid] <= g) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// x0 = At(y / Phi_sum) for every item (the start point of the GAP loop).
+__global__ void __launch_bounds__(PROJ_T) k_batch_x0(const Table *__restrict__ T) {
+    const int g = blockIdx.x;
+    if (g >= T->proj_prefix[T->n]) return;
+    const int i = find_item(T->proj_prefix, T->n, g);
+    const Item &I = T->it[i];
+    const int64_t p = (int64_t)(g - T->proj_prefix[i]) * PROJ_T + threadIdx.x;
+    if (p >= I.hw) return;
+    const uint32_t w = I.bits[p];
+    const float s0 = I.y[p] / I.phisum[p];
+    for (int b = 0; b < I.B; ++b) I.x[b * I.hw + p] = ((w >> b) & 1u) ? s0 : 0.f * s0;
+}
+
+// GAP projection (acc: y1 += y - A x, x_p = x + lam At((y1 - A x)/Phi_sum)).
+template <bool ACC>
+__global__ void __launch_bounds__(PROJ_T) k_batch_proj(const Table *__restrict__ T) {
+    __shared__ float xs[32 * PROJ_T];
+    const int g = blockIdx.x;
+    if (g >= T->proj_prefix[T->n]) return;
+    const int i = find_item(T->proj_prefix, T->n, g);
+    const Item &I = T->it[i];
+    const int t = threadIdx.x;
+    const int64_t p = (int64_t)(g - T->proj_prefix[i]) * PROJ_T + t;
+    if (p >= I.hw) return;
+    const int64_t hw = I.hw;
+    const int B = I.B;
+    const uint32_t w = __ldg(I.bits + p);
+    float s = 0.f;
+    for (int b = 0; b < B; ++b) {
+        const float v = __ldg(I.x + b * hw + p);
+        xs[b * PROJ_T + t] = v;
+        s = fmaf(v, ((w >> b) & 1u) ? 1.f : 0.f, s);
+    }
+    const float yv = __ldg(I.y + p), ps = __ldg(I.phisum + p);
+    float r;
+    if (ACC) {
+        const float tt = I.y1[p] + (yv - s);
+        I.y1[p] = tt;
+        r = __fdiv_rn(tt - s, ps);
+    } else {
+        r = __fdiv_rn(yv - s, ps);
+    }
+    for (int b = 0; b < B; ++b) {
+        const float m = ((w >> b) & 1u) ? 1.f : 0.f;
+        __stcs(I.xp + b * hw + p, fmaf(I.lam, r * m, xs[b * PROJ_T + t]));
+    }
+}
+
+// TV pass (FIX = 0) or its stop-test launch (FIX = 1) over all items' tiles.
+template <int FIX>
+__global__ void __launch_bounds__(tv::WPB * 32, 3) k_batch_tv(const Table *__restrict__ T) {
+    const int g = blockIdx.x * tv::WPB + (threadIdx.x >> 5);
+    if (g >= T->tv_prefix[T->n]) return;  // warp-uniform
+    const int i = find_item(T->tv_prefix, T->n, g);
+    const tv::Pass &P = T->it[i].tv;
+    int frame, chunk, band;
+    if (!tv::decode_index(P, g - T->tv_prefix[i], frame, chunk, band)) return;
+    const int lane = threadIdx.x & 31;
+    if (!FIX) {
+        switch (P.S) {
+            case 1: tv::run_mode<1, 4, false, true, true>(P, frame, chunk, band, lane); break;
+            case 2: tv::run_mode<2, 4, false, true, true>(P, frame, chunk, band, lane); break;
+            case 3: tv::run_mode<3, 4, false, true, true>(P, frame, chunk, band, lane); break;
+            default: tv::run_mode<4, 4, false, true, true>(P, frame, chunk, band, lane); break;
+        }
+        return;
+    }
+    const int j = tv::find_stop(P, frame);
+    switch (j) {  // a = 0: j in [1, S-1] re-runs with j updates
+        case 1: tv::run_mode<1, 4, false, true, false>(P, frame, chunk, band, lane); break;
+        case 2: tv::run_mode<2, 4, false, true, false>(P, frame, chunk, band, lane); break;
+        case 3: tv::run_mode<3, 4, false, true, false>(P, frame, chunk, band, lane); break;
+        default: break;
+    }
+}
+
+// --------------------------------------------------------------- host side
+size_t r256(size_t b) { return (b + 255) & ~size_t(255); }
+
+struct Layout {
+    size_t table, xp, y1, energy, tvscratch, total;
+    std::vector<size_t> item_xp, item_y1, item_e;
+};
+
+Layout layout(const sci_batch_item *items, int n, int K) {
+    Layout L;
+    size_t off = 0;
+    L.table = off;
+    off += r256(sizeof(Table));
+    for (int i = 0; i < n; ++i) {
+        const int64_t hw = items[i].H * items[i].W, nn = items[i].B * hw;
+        L.item_xp.push_back(off);
+        off += r256(4 * (size_t)nn);
+        L.item_y1.push_back(off);
+        off += r256(4 * (size_t)hw);
+    }
+    L.energy = off;
+    for (int i = 0; i < n; ++i) {
+        L.item_e.push_back(off - L.energy);
+        off += r256(sizeof(double) * 2 * K * (size_t)items[i].B);
+    }
+    const size_t energy_end = off;
+    L.tvscratch = off;
+    size_t tvmax = 0;  // autotuning scratch: the largest single-item TV workspace
+    for (int i = 0; i < n; ++i)
+        tvmax = std::max(tvmax, tv_workspace_bytes(items[i].B, items[i].H, items[i].W, K));
+    off += r256(tvmax);
+    L.total = off;
+    (void)energy_end;
+    return L;
+}
+
+int check(const sci_batch_item *items, int n, int K) {
+    SCI_CHECK_ARG(items && n >= 1 && n <= MAXI, "batch: 1..%d items (got %d)", MAXI, n);
+    SCI_CHECK_ARG(K >= 2 && K <= tv::SMAX + 1, "batch: tv_iter_max must be in [2, 5]");
+    for (int i = 0; i < n; ++i) {
+        const sci_batch_item &it = items[i];
+        SCI_CHECK_ARG(it.y && it.mask_bits && it.phisum && it.x, "batch: item %d null pointer", i);
+        SCI_CHECK_ARG(it.B >= 1 && it.B <= 32 && it.H >= 1 && it.W >= 4 && it.W % 4 == 0,
+                      "batch: item %d needs 1 <= B <= 32, W %% 4 == 0 (B=%lld H=%lld W=%lld)", i,
+                      (long long)it.B, (long long)it.H, (long long)it.W);
+        SCI_CHECK_ARG(it.tv_weight > 0.f, "batch: item %d tv_weight must be > 0", i);
+        SCI_CHECK_ARG(((reinterpret_cast<uintptr_t>(it.x) | reinterpret_cast<uintptr_t>(it.y) |
+                        reinterpret_cast<uintptr_t>(it.phisum)) & 15u) == 0,
+                      "batch: item %d buffers must be 16-byte aligned", i);
+    }
+    return SCI_OK;
+}
+
+int default_R(int64_t H, int64_t W, int64_t B) {
+    (void)W;
+    (void)B;
+    return H >= 1024 ? 256 : (H >= 256 ? 128 : 64);
+}
+
+// Builds the host copy of the device table.
+void build_table(const sci_batch_item *items, int n, int K, float eps, char *ws, const Layout &L,
+                 Table &T) {
+    memset(&T, 0, sizeof(T));
+    T.n = n;
+    T.proj_prefix[0] = T.tv_prefix[0] = 0;
+    for (int i = 0; i < n; ++i) {
+        const sci_batch_item &s = items[i];
+        Item &I = T.it[i];
+        I.y = s.y;
+        I.bits = s.mask_bits;
+        I.phisum = s.phisum;
+        I.x = s.x;
+        I.xp = reinterpret_cast<float *>(ws + L.item_xp[i]);
+        I.y1 = reinterpret_cast<float *>(ws + L.item_y1[i]);
+        I.B = (int)s.B;
+        I.hw = s.H * s.W;
+        I.lam = s.lambda;
+        tv::Pass &P = I.tv;
+        P.f = I.xp;
+        P.u = s.x;
+        P.energy = reinterpret_cast<double *>(ws + L.energy + L.item_e[i]);
+        P.fs = I.hw;
+        P.nf = (int)s.B;
+        P.H = (int)s.H;
+        P.W = (int)s.W;
+        P.K = K;
+        P.a = 0;
+        P.tau = 0.25f;
+        P.tw = 0.25f / s.tv_weight;
+        P.weight = s.tv_weight;
+        P.eps = eps;
+        P.cpl = 4;
+        P.S = K - 1;
+        P.hl = 4;
+        P.own = 128 - 4 - 4;
+        P.ht = K - 1;
+        P.nbands = (int)((s.W + P.own - 1) / P.own);
+        P.R = s.R > 0 ? s.R : default_R(s.H, s.W, s.B);
+        P.nchunks = (int)((s.H + P.R - 1) / P.R);
+        P.vec = 1;
+        P.lag = 1;
+        P.frame_fast = 1;
+        T.proj_prefix[i + 1] = T.proj_prefix[i] + (int)((I.hw + PROJ_T - 1) / PROJ_T);
+        T.tv_prefix[i + 1] = T.tv_prefix[i] + P.nbands * P.nchunks * P.nf;
+    }
+}
+
+struct GraphCache {
+    std::mutex mu;
+    std::list<std::pair<std::string, cudaGraphExec_t>> e;
+};
+GraphCache &cache() {
+    static GraphCache c;
+    return c;
+}
+
+int enqueue(const Table &T, Table *dT, const Layout &L, char *ws, int n, int iters, int K,
+            int accelerate, int init_x0, cudaStream_t s) {
+    const int pb = T.proj_prefix[n], tb = (T.tv_prefix[n] + tv::WPB - 1) / tv::WPB;
+    if (init_x0) {
+        k_batch_x0<<<pb, PROJ_T, 0, s>>>(dT);
+        SCI_LAUNCHED("k_batch_x0");
+    }
+    for (int i = 0; i < n; ++i)
+        if (accelerate) SCI_CUDA(cudaMemsetAsync(T.it[i].y1, 0, 4 * T.it[i].hw, s));
+    const size_t ebytes = L.tvscratch - L.energy;
+    for (int it = 0; it < iters; ++it) {
+        if (accelerate) k_batch_proj<true><<<pb, PROJ_T, 0, s>>>(dT);
+        else k_batch_proj<false><<<pb, PROJ_T, 0, s>>>(dT);
+        SCI_LAUNCHED("k_batch_proj");
+        SCI_CUDA(cudaMemsetAsync(ws + L.energy, 0, ebytes, s));
+        k_batch_tv<0><<<tb, tv::WPB * 32, 0, s>>>(dT);
+        SCI_LAUNCHED("k_batch_tv");
+        if (K >= 3) {
+            k_batch_tv<1><<<tb, tv::WPB * 32, 0, s>>>(dT);
+            SCI_LAUNCHED("k_batch_tv fixup");
+        }
+    }
+    return SCI_OK;
+}
+
+}  // namespace batch
+}  // namespace sci
+
+using namespace sci;
+using namespace sci::batch;
+
+extern "C" {
+
+int sci_batch_workspace_bytes(const sci_batch_item *items, int n, int tv_iter_max,
+                              size_t *bytes) {
+    if (int e = check(items, n, tv_iter_max)) return e;
+    SCI_CHECK_ARG(bytes, "null bytes");
+    *bytes = layout(items, n, tv_iter_max).total;
+    return SCI_OK;
+}
+
+int sci_batch_autotune(sci_batch_item *items, int n, int tv_iter_max, void *workspace,
+                       size_t workspace_bytes, void *stream) {
+    if (int e = check(items, n, tv_iter_max)) return e;
+    const Layout L = layout(items, n, tv_iter_max);
+    SCI_CHECK_ARG(workspace && workspace_bytes >= L.total, "batch: workspace too small");
+    char *ws = static_cast<char *>(workspace);
+    cudaStream_t s = as_stream(stream);
+    // one timing per distinct (B, H, W): the TV pass of the item's own x
+    // into its projection buffer, for each candidate chunk height
+    static std::mutex mu;
+    static std::map<std::tuple<int64_t, int64_t, int64_t, int>, int> tuned;
+    cudaEvent_t e0, e1;
+    SCI_CUDA(cudaEventCreate(&e0));
+    SCI_CUDA(cudaEventCreate(&e1));
+    int rc = SCI_OK;
+    for (int i = 0; i < n && rc == SCI_OK; ++i) {
+        sci_batch_item &it = items[i];
+        const auto key = std::make_tuple(it.B, it.H, it.W, tv_iter_max);
+        {
+            std::lock_guard<std::mutex> lk(mu);
+            auto f = tuned.find(key);
+            if (f != tuned.end()) {
+                it.R = f->second;
+                continue;
+            }
+        }
+        float best = 1e30f;
+        int bestR = default_R(it.H, it.W, it.B);
+        for (int R : {32, 64, 128, 256, 512}) {
+            if (R > 2 * it.H && R != 32) break;
+            float ms = 0.f;
+            for (int rep = 0; rep < 3 && rc == SCI_OK; ++rep) {
+                cudaEventRecord(e0, s);
+                rc = tv_launch(it.x, reinterpret_cast<float *>(ws + L.item_xp[i]), nullptr, it.B,
+                               it.H, it.W, it.H * it.W, it.tv_weight, 2e-4f, tv_iter_max, nullptr,
+                               nullptr, ws + L.tvscratch, L.total - L.tvscratch, s, R);
+                cudaEventRecord(e1, s);
+                cudaEventSynchronize(e1);
+                float t = 0.f;
+                cudaEventElapsedTime(&t, e0, e1);
+                if (rep > 0) ms += t;  // the first run warms up
+            }
+            if (rc == SCI_OK && ms < best) {
+                best = ms;
+                bestR = R;
+            }
+        }
+        it.R = bestR;
+        std::lock_guard<std::mutex> lk(mu);
+        tuned[key] = bestR;
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    return rc;
+}
+
+int sci_batch_gap_tv(const sci_batch_item *items, int n, int iters, int tv_iter_max, float eps,
+                     int accelerate, int init_x0, int use_graph, void *workspace,
+                     size_t workspace_bytes, void *stream) {
+    if (int e = check(items, n, tv_iter_max)) return e;
+    SCI_CHECK_ARG(iters >= 0, "batch: iters must be >= 0");
+    const Layout L = layout(items, n, tv_iter_max);
+    SCI_CHECK_ARG(workspace && workspace_bytes >= L.total,
+                  "batch: workspace of %zu bytes needed, got %zu", L.total, workspace_bytes);
+    char *ws = static_cast<char *>(workspace);
+    cudaStream_t s = as_stream(stream);
+    Table *hT = new Table;
+    build_table(items, n, tv_iter_max, eps, ws, L, *hT);
+    Table *dT = reinterpret_cast<Table *>(ws + L.table);
+    // the table is tiny; a stream-ordered copy from this host struct needs
+    // it to stay alive until the copy ran, so the copy is synchronous here
+    cudaError_t ce = cudaStreamSynchronize(s);
+    if (ce == cudaSuccess) ce = cudaMemcpy(dT, hT, sizeof(Table), cudaMemcpyHostToDevice);
+    if (ce != cudaSuccess) {
+        delete hT;
+        return cuda_status(ce, "batch table upload");
+    }
+    int rc = SCI_OK;
+    if (!use_graph) {
+        rc = enqueue(*hT, dT, L, ws, n, iters, tv_iter_max, accelerate, init_x0, s);
+        delete hT;
+        return rc;
+    }
+    std::string key(reinterpret_cast<const char *>(hT), sizeof(Table));
+    key.append(reinterpret_cast<const char *>(&iters), sizeof(int));
+    key.append(reinterpret_cast<const char *>(&accelerate), sizeof(int));
+    key.append(reinterpret_cast<const char *>(&init_x0), sizeof(int));
+    GraphCache &gc = cache();
+    {
+        std::lock_guard<std::mutex> lk(gc.mu);
+        for (auto &kv : gc.e)
+            if (kv.first == key) {
+                delete hT;
+                SCI_CUDA(cudaGraphLaunch(kv.second, s));
+                return SCI_OK;
+            }
+    }
+    cudaStream_t cs;
+    ce = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
+    if (ce != cudaSuccess) {
+        delete hT;
+        return cuda_status(ce, "cudaStreamCreate");
+    }
+    ce = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    if (ce == cudaSuccess) rc = enqueue(*hT, dT, L, ws, n, iters, tv_iter_max, accelerate, init_x0, cs);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ce2 = (ce == cudaSuccess) ? cudaStreamEndCapture(cs, &graph) : ce;
+    cudaStreamDestroy(cs);
+    delete hT;
+    if (rc) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    if (ce2 != cudaSuccess) return cuda_status(ce2, "batch graph capture");
+    cudaGraphExec_t exec = nullptr;
+    ce = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) return cuda_status(ce, "cudaGraphInstantiate");
+    {
+        std::lock_guard<std::mutex> lk(gc.mu);
+        gc.e.emplace_front(key, exec);
+        while (gc.e.size() > 8) {
+            cudaGraphExecDestroy(gc.e.back().second);
+            gc.e.pop_back();
+        }
+    }
+    SCI_CUDA(cudaGraphLaunch(exec, s));
+    return SCI_OK;
+}
+
+}  // extern "C"

@@ -17,6 +17,10 @@
 //   ubar_k = -div gbar_k,  fbar += ubar_k,  pbar_k = r_k pbar_{k+1} + grad ubar_k.
 // then the adjoint of the projection (including d/dPhi through A, At and
 // Phi_sum, and d/dlambda_k), and finally of the measurement and x^0.
+#include <list>
+#include <mutex>
+#include <string>
+
 #include "sci_common.cuh"
 
 namespace sci {
@@ -360,6 +364,64 @@ int forward(const float *logits, const float *lambdas, const float *xt, int64_t 
     return SCI_OK;
 }
 
+// Cached CUDA graphs of whole forward / reverse passes (keyed by every
+// argument): the reverse pass is ~20 launches per outer iteration.
+struct GraphCache {
+    std::mutex mu;
+    std::list<std::pair<std::string, cudaGraphExec_t>> e;
+};
+GraphCache &cache() {
+    static GraphCache c;
+    return c;
+}
+
+template <typename F>
+int run_graph(const std::string &key, cudaStream_t s, F enqueue) {
+    GraphCache &gc = cache();
+    {
+        std::lock_guard<std::mutex> lk(gc.mu);
+        for (auto &kv : gc.e)
+            if (kv.first == key) {
+                SCI_CUDA(cudaGraphLaunch(kv.second, s));
+                return SCI_OK;
+            }
+    }
+    cudaStream_t cs;
+    SCI_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
+    cudaError_t ce = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
+    int rc = SCI_OK;
+    if (ce == cudaSuccess) rc = enqueue(cs);
+    cudaGraph_t graph = nullptr;
+    const cudaError_t ce2 = (ce == cudaSuccess) ? cudaStreamEndCapture(cs, &graph) : ce;
+    cudaStreamDestroy(cs);
+    if (rc) {
+        if (graph) cudaGraphDestroy(graph);
+        return rc;
+    }
+    if (ce2 != cudaSuccess) return cuda_status(ce2, "unrolled graph capture");
+    cudaGraphExec_t exec = nullptr;
+    ce = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    if (ce != cudaSuccess) return cuda_status(ce, "cudaGraphInstantiate");
+    {
+        std::lock_guard<std::mutex> lk(gc.mu);
+        gc.e.emplace_front(key, exec);
+        while (gc.e.size() > 8) {
+            cudaGraphExecDestroy(gc.e.back().second);
+            gc.e.pop_back();
+        }
+    }
+    SCI_CUDA(cudaGraphLaunch(exec, s));
+    return SCI_OK;
+}
+
+template <typename... T>
+std::string make_key(const T &...v) {
+    std::string k;
+    (k.append(reinterpret_cast<const char *>(&v), sizeof(T)), ...);
+    return k;
+}
+
 }  // namespace unr
 }  // namespace sci
 
@@ -388,15 +450,20 @@ int sci_unrolled_fwd(const float *logits, const float *lambdas, const float *x_t
                   workspace_bytes);
     Ws w;
     layout(N, B, H, W, K, tv_iters, &w, static_cast<char *>(workspace));
-    cudaStream_t s = as_stream(stream);
-    if (int e = forward(logits, lambdas, x_true, N, B, H, W, K, tv_iters, tv_weight, w, s))
-        return e;
     const int64_t nbhw = N * B * H * W;
-    if (loss) SCI_CUDA(cudaMemcpyAsync(loss, w.loss, sizeof(double), cudaMemcpyDeviceToDevice, s));
-    if (x_out)
-        SCI_CUDA(cudaMemcpyAsync(x_out, w.X + (int64_t)K * nbhw, 4 * nbhw,
-                                 cudaMemcpyDeviceToDevice, s));
-    return SCI_OK;
+    auto body = [&](cudaStream_t s) -> int {
+        if (int e = forward(logits, lambdas, x_true, N, B, H, W, K, tv_iters, tv_weight, w, s))
+            return e;
+        if (loss)
+            SCI_CUDA(cudaMemcpyAsync(loss, w.loss, sizeof(double), cudaMemcpyDeviceToDevice, s));
+        if (x_out)
+            SCI_CUDA(cudaMemcpyAsync(x_out, w.X + (int64_t)K * nbhw, 4 * nbhw,
+                                     cudaMemcpyDeviceToDevice, s));
+        return SCI_OK;
+    };
+    const std::string key = make_key(1, logits, lambdas, x_true, N, B, H, W, K, tv_iters,
+                                     tv_weight, loss, x_out, workspace);
+    return run_graph(key, as_stream(stream), body);
 }
 
 int sci_unrolled_bwd(const float *logits, const float *lambdas, const float *x_true, int64_t N,
@@ -412,7 +479,9 @@ int sci_unrolled_bwd(const float *logits, const float *lambdas, const float *x_t
                   workspace_bytes);
     Ws w;
     layout(N, B, H, W, K, tv_iters, &w, static_cast<char *>(workspace));
-    cudaStream_t s = as_stream(stream);
+    const std::string key = make_key(2, logits, lambdas, x_true, N, B, H, W, K, tv_iters,
+                                     tv_weight, grad_loss, grad_logits, grad_lambdas, workspace);
+    return run_graph(key, as_stream(stream), [&](cudaStream_t s) -> int {
     // The checkpoints of the preceding sci_unrolled_fwd call on this
     // workspace (same arguments) are used as they are.
     const int64_t hw = H * W, nbhw = N * B * hw, nhw = N * hw, nf = N * B;
@@ -469,6 +538,7 @@ int sci_unrolled_bwd(const float *logits, const float *lambdas, const float *x_t
                                   grad_logits, 1.f, (int)N, (int)B, hw);
     SCI_LAUNCHED("k_init_bwd");
     return SCI_OK;
+    });
 }
 
 }  // extern "C"

@@ -120,3 +120,23 @@ def config0():
 def config1():
     """2048 x 2048 x 24, Bernoulli(0.5), noise sigma = 0.01 max(y)."""
     return video_config(2048, 2048, 24, noise_rel=0.01)
+
+
+def batch_config(n=64, seed=0, sizes=(128, 256, 512, 1024), frames=(8, 16, 24, 32)):
+    """Uneven batch: item i has H = W drawn from ``sizes``, B from ``frames``,
+    its own Bernoulli(p) mask with p ~ U[0.3, 0.7], the video scene generator
+    and no noise; seeds (1000+i, 1000+i+1, 1000+i+2).  Yields
+    (orig, mask, meas) one item at a time (the largest is 1024^2 x 32)."""
+    rng = np.random.default_rng(seed)
+    shapes = [(int(rng.choice(sizes)), int(rng.choice(frames)), float(rng.uniform(0.3, 0.7)))
+              for _ in range(n)]
+    for i, (s, b, p) in enumerate(shapes):
+        yield video_config(s, s, b, p=p, seeds=(1000 + i, 1000 + i + 1, 1000 + i + 2))
+
+
+def batch_shapes(n=64, seed=0, sizes=(128, 256, 512, 1024), frames=(8, 16, 24, 32)):
+    """The (H, W, B, p) of ``batch_config`` without generating the data."""
+    rng = np.random.default_rng(seed)
+    return [(s, s, b, p) for s, b, p in
+            ((int(rng.choice(sizes)), int(rng.choice(frames)), float(rng.uniform(0.3, 0.7)))
+             for _ in range(n))]

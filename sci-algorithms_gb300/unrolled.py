@@ -21,36 +21,56 @@ from . import _dev
 from ._lib import call
 
 
+class _Buffers:
+    """Fixed device buffers of one workspace: inputs are copied in and
+    outputs read out of them, so the cached CUDA graphs of the forward and
+    reverse passes (keyed by pointers) are replayed on every call."""
+
+    def __init__(self, N, B, H, W, K, dev):
+        self.logits = torch.empty((B, H, W), dtype=torch.float32, device=dev)
+        self.lambdas = torch.empty((K,), dtype=torch.float32, device=dev)
+        self.x_true = torch.empty((N, B, H, W), dtype=torch.float32, device=dev)
+        self.loss = torch.zeros(1, dtype=torch.float64, device=dev)
+        self.glog = torch.empty((B, H, W), dtype=torch.float32, device=dev)
+        self.glam = torch.zeros(K, dtype=torch.float64, device=dev)
+
+
+_BUFFERS = {}
+
+
+def _buffers(ws, N, B, H, W, K):
+    key = (ws.data_ptr(), N, B, H, W, K)
+    b = _BUFFERS.get(key)
+    if b is None:
+        b = _BUFFERS[key] = _Buffers(N, B, H, W, K, ws.device)
+    return b
+
+
 class UnrolledGapTV(torch.autograd.Function):
     @staticmethod
     def forward(ctx, logits, lambdas, x_true, K, tv_iters, tv_weight, ws=None):
         N, B, H, W = x_true.shape
         if ws is None:
-            n = ctypes.c_size_t()
-            call("sci_unrolled_workspace_bytes", N, B, H, W, K, tv_iters, ctypes.byref(n))
-            ws = _dev.workspace(n.value, x_true.device)
-        logits = logits.detach().contiguous()
-        lambdas = lambdas.detach().to(torch.float32).contiguous()
-        x_true = x_true.detach().contiguous()
-        loss = torch.zeros(1, dtype=torch.float64, device=x_true.device)
-        call("sci_unrolled_fwd", logits.data_ptr(), lambdas.data_ptr(), x_true.data_ptr(), N, B,
-             H, W, K, tv_iters, float(tv_weight), loss.data_ptr(), None, ws.data_ptr(),
-             ws.numel(), _dev.stream_handle())
-        ctx.save_for_backward(logits, lambdas, x_true)
-        ctx.ws = ws
+            ws = unrolled_workspace(N, B, H, W, K, tv_iters, x_true.device)
+        bf = _buffers(ws, N, B, H, W, K)
+        bf.logits.copy_(logits.detach())
+        bf.lambdas.copy_(lambdas.detach())
+        bf.x_true.copy_(x_true.detach())
+        call("sci_unrolled_fwd", bf.logits.data_ptr(), bf.lambdas.data_ptr(),
+             bf.x_true.data_ptr(), N, B, H, W, K, tv_iters, float(tv_weight), bf.loss.data_ptr(),
+             None, ws.data_ptr(), ws.numel(), _dev.stream_handle())
+        ctx.ws, ctx.bf = ws, bf
         ctx.cfg = (N, B, H, W, K, tv_iters, float(tv_weight))
-        return (loss / x_true.numel()).to(torch.float32).reshape(())
+        return (bf.loss / x_true.numel()).to(torch.float32).reshape(())
 
     @staticmethod
     def backward(ctx, grad):
-        logits, lambdas, x_true = ctx.saved_tensors
         N, B, H, W, K, T, w = ctx.cfg
-        gl = torch.empty_like(logits)
-        glam = torch.zeros(K, dtype=torch.float64, device=logits.device)
-        call("sci_unrolled_bwd", logits.data_ptr(), lambdas.data_ptr(), x_true.data_ptr(), N, B,
-             H, W, K, T, w, float(grad.item()), gl.data_ptr(), glam.data_ptr(),
-             ctx.ws.data_ptr(), ctx.ws.numel(), _dev.stream_handle())
-        return gl, glam.to(torch.float32), None, None, None, None, None
+        bf, ws = ctx.bf, ctx.ws
+        call("sci_unrolled_bwd", bf.logits.data_ptr(), bf.lambdas.data_ptr(),
+             bf.x_true.data_ptr(), N, B, H, W, K, T, w, float(grad.item()), bf.glog.data_ptr(),
+             bf.glam.data_ptr(), ws.data_ptr(), ws.numel(), _dev.stream_handle())
+        return bf.glog.clone(), bf.glam.to(torch.float32), None, None, None, None, None
 
 
 def unrolled_loss(logits, lambdas, x_true, K=20, tv_iters=5, tv_weight=0.1, ws=None):
