@@ -49,6 +49,19 @@ def dist_env():
     return rank, world, local
 
 
+def max_over_ranks(value, device):
+    """Max of a per-rank float over the job (identity for one rank).  The
+    ranks are independent replicas; this timing reduction is the only
+    cross-rank communication."""
+    import torch
+    import torch.distributed as dist
+    if not (dist.is_available() and dist.is_initialized()) or dist.get_world_size() == 1:
+        return float(value)
+    t = torch.tensor([float(value)], dtype=torch.float64, device=device)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
 def base_config():
     return {"workload": WORKLOAD, "H": H, "W": W, "B": B, "iters": ITERS,
             "tv_iter_max": TV_ITERS, "tv_weight": "0.2->0.05 geometric", "lambda": 1.0,
@@ -205,12 +218,7 @@ def run_gpu(args):
             fn()
         e1.record(stream)
         barrier()
-        ms = e0.elapsed_time(e1) / steps
-        if world > 1:
-            t = torch.tensor([ms], device=dev)
-            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-            ms = float(t.item())
-        return ms
+        return max_over_ranks(e0.elapsed_time(e1) / steps, dev)
 
     clocks = Clocks(local)
     clocks.start()
@@ -254,11 +262,7 @@ def run_gpu(args):
     for _ in range(e2e_steps):
         gap.run_host(y_host, x_host)
     barrier()
-    ms_e2e = (time.perf_counter() - t0) * 1e3 / e2e_steps
-    if world > 1:
-        t = torch.tensor([ms_e2e], device=dev)
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_e2e = float(t.item())
+    ms_e2e = max_over_ranks((time.perf_counter() - t0) * 1e3 / e2e_steps, dev)
 
     extras = {} if args.no_extras else side_workloads(dev)
 
