@@ -258,7 +258,7 @@ def run_gpu(args):
         gap.run_host(y_host, x_host)
     barrier()
     t0 = time.perf_counter()
-    e2e_steps = max(3, args.steps // 2)
+    e2e_steps = max(5, args.steps)
     for _ in range(e2e_steps):
         gap.run_host(y_host, x_host)
     barrier()
@@ -283,7 +283,9 @@ def run_gpu(args):
                          "traffic": ncu_traffic("k_tv_main"),
                          "algorithmic_bytes_per_launch": tv_bytes, "ms_per_launch": ms_tv},
             "kernels": {"tv_ms": ms_tv, "tv_gbs": tv_gbs, "proj_ms": ms_proj,
+                        "proj_kernel": "k_proj_gap_tma<128> (bulk-copy staged)",
                         "proj_gbs": proj_gbs, "proj_frac": proj_gbs / peak,
+                        "proj_traffic": ncu_traffic("k_proj_gap_tma"),
                         "per_iteration_algorithmic_bytes": per_iter_bytes,
                         "per_iteration_gbs": per_iter_bytes * ITERS / (ms_gap * 1e-3) / 1e9},
             "admm": {"value": world * ITERS * 1e3 / ms_admm, "unit": "iter/s",

@@ -42,6 +42,13 @@ int sci_version(void);
  * truncated to n bytes).  Returns the full message length. */
 int sci_last_error(char *buf, size_t n);
 
+/* Reads the device status word into *status and, with clear != 0, resets
+ * it.  Bit 0 is set when a bounded device-side wait of a bulk-copy kernel
+ * (the GAP projection of sci_proj_gap with a packed mask) gave up; the
+ * results of such a launch are not valid.  Synchronous.  No counterpart in
+ * the reference (library plumbing). */
+int sci_device_status(unsigned int *status, int clear);
+
 /* ---------------------------------------------------------- L1 operators */
 
 /* y = sum_b phi_b .* x_b.
@@ -139,6 +146,34 @@ int sci_tv_chambolle_noalloc(const float *f, float *u, float *resid,
                              float weight, float eps, int n_iter_max,
                              int *steps, void *stream);
 
+/* ------------------------------------- MATLAB-twin TV denoisers (next row) */
+
+/* The denoisers the MATLAB GAP loop selects with its tvm switch
+ * (PnP_SCI/matlab/algorithms/gapdenoise.m:92-112), by kind: */
+#define SCI_TVM_ATV_CLIPA 1   /* TV_denoising.m(v, lambda, iters)          */
+#define SCI_TVM_ATV_CLIPB 2   /* TV_denoising_clip_LB.m                    */
+#define SCI_TVM_ATV_CHAM 3    /* tvdenoise_cham_ATV2D.m                    */
+#define SCI_TVM_ATV_FGP 4     /* fgp_denoise_ATV2D.m                       */
+#define SCI_TVM_ITV2D_CHAM 5  /* tvdenoise_cham_ITV2D.m                    */
+#define SCI_TVM_ITV2D_FGP 6   /* fgp_denoise_ITV2D.m                       */
+#define SCI_TVM_ITV3D_CHAM 7  /* tvdenoise_cham_ITV3D.m (norm over frames) */
+#define SCI_TVM_ITV3D_FGP 8   /* fgp_denoise_ITV3D.m (norm over frames)    */
+
+/* Bytes of device workspace sci_tv_matlab needs. */
+int sci_tv_matlab_workspace_bytes(int kind, int64_t nframes, int64_t H,
+                                  int64_t W, size_t *bytes);
+
+/* u = denoiser `kind`(f, lambda, iters) on the planar stack of nframes
+ * H x W frames (H, W >= 2), with the file's own parameter: lambda is the
+ * clip bound / ROF weight of TV_denoising*.m and fgp_denoise_*.m, and the
+ * fidelity weight of tvdenoise_cham_*.m (gapdenoise.m passes tvweight and
+ * 1/tvweight respectively; 5 iterations, 2 for the FGP files).  A
+ * one-frame stack takes MATLAB's 2-D branch of the file.
+ * Replaces the calls at gapdenoise.m:94-108. */
+int sci_tv_matlab(int kind, const float *f, float *u, int64_t nframes,
+                  int64_t H, int64_t W, float lambda, int iters,
+                  void *workspace, size_t workspace_bytes, void *stream);
+
 /* -------------------------------------------------- metrics (diagnostics) */
 
 /* out[0] += sum_i (a_i - b_i)^2 in float64 (PSNR numerator for
@@ -162,6 +197,10 @@ typedef struct sci_solve_opts {
     double *sqerr;           /* nullable device double[iters]: sum sq. err. */
     int *tv_steps;           /* nullable device int[iters * B]              */
     int use_graph;           /* 1: capture the loop in a CUDA graph (cached) */
+    int tvm;                 /* 0: scikit-image Chambolle (tv_iter_max steps,
+                              * stop test eps); SCI_TVM_*: that MATLAB
+                              * denoiser with tv_iter_max iterations and
+                              * weights as gapdenoise.m's tvweight           */
 } sci_solve_opts;
 
 /* Workspace bytes for sci_gap_tv / sci_admm_tv. */

@@ -9,7 +9,8 @@ sm_103a CUDA kernels behind the C ABI of ``include/sci_gb300.h``
 """
 from .buildlib import build  # noqa: F401
 from .utils import A_, At_, psnr, make_ops, MaskOperator  # noqa: F401
-from .tv import denoise_tv_chambolle, tv_frames  # noqa: F401
+from .tv import (TVM, denoise_tv_chambolle, denoise_tv_matlab, tv_frames,  # noqa: F401
+                 tv_matlab_frames)
 from .pnp_sci_algo import (admmdenoise_cacti, gap_denoise, admm_denoise,  # noqa: F401
                            GAP_TV_rec, ADMM_TV_rec)
 from .solver import Solver  # noqa: F401

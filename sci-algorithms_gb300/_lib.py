@@ -39,7 +39,8 @@ class SolveOpts(ctypes.Structure):
                 ("orig", c_vp),
                 ("sqerr", c_vp),
                 ("tv_steps", c_vp),
-                ("use_graph", ctypes.c_int)]
+                ("use_graph", ctypes.c_int),
+                ("tvm", ctypes.c_int)]
 
 
 class BatchItem(ctypes.Structure):
@@ -53,6 +54,7 @@ class BatchItem(ctypes.Structure):
 _SIGS = {
     "sci_version": [],
     "sci_last_error": [ctypes.c_char_p, c_sz],
+    "sci_device_status": [ctypes.POINTER(ctypes.c_uint), ctypes.c_int],
     "sci_A": [c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_vp],
     "sci_At": [c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_vp],
     "sci_phisum": [c_vp, c_vp, c_i64, c_i64, c_i64, ctypes.c_int, c_vp],
@@ -68,6 +70,9 @@ _SIGS = {
                          c_vp, c_vp, c_vp, c_sz, c_vp],
     "sci_tv_chambolle_noalloc": [c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_f, c_f,
                                  ctypes.c_int, c_vp, c_vp],
+    "sci_tv_matlab_workspace_bytes": [ctypes.c_int, c_i64, c_i64, c_i64, ctypes.POINTER(c_sz)],
+    "sci_tv_matlab": [ctypes.c_int, c_vp, c_vp, c_i64, c_i64, c_i64, c_f, ctypes.c_int, c_vp,
+                      c_sz, c_vp],
     "sci_sqerr_accum": [c_vp, c_vp, c_i64, c_vp, c_vp],
     "sci_solver_workspace_bytes": [c_i64, c_i64, c_i64, ctypes.POINTER(SolveOpts),
                                    ctypes.POINTER(c_sz)],

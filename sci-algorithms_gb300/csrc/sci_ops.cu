@@ -7,6 +7,7 @@
 // HBM-bound: one pass reads x and the mask once and writes the result once;
 // the second sweep over the frames inside the projection is served by L1/L2.
 #include <cstdarg>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 
@@ -30,6 +31,10 @@ int cuda_status(cudaError_t e, const char *what) {
     set_error("CUDA error %d (%s) in %s", (int)e, cudaGetErrorString(e), what);
     return SCI_ERR_CUDA;
 }
+
+int launch_proj_gap_tma(const float *x, const uint32_t *bits, const float *y, float *y1,
+                        const float *phisum, float *xo, float lam, bool acc, int B, int64_t hw,
+                        cudaStream_t s);
 
 // Grid for a grid-stride loop over `n` work units of one thread each.
 static inline dim3 grid_for(int64_t n, int threads) {
@@ -558,13 +563,17 @@ int sci_proj_gap(const float *x, const float *phi, const uint32_t *mask_bits, co
                     x, M, y, y1, phisum, x_out, lambda, Bi, hw);                            \
         }                                                                                   \
     } while (0)
+    const char *tma = getenv("SCI_PROJ_TMA");
+    if (mask_bits && !(tma && atoi(tma) == 0)) {
+        // bulk-copy staged kernel; SCI_ERR_UNSUPPORTED: alignment or B
+        const int e = launch_proj_gap_tma(x, mask_bits, y, y1, phisum, x_out, lambda,
+                                          accelerate != 0, Bi, hw, s);
+        if (e != SCI_ERR_UNSUPPORTED) return e;
+    }
     if (mask_bits) {
         Mask<1> M{mask_bits, hw};
         if (accelerate) launch_gap_smem<1, true>(x, M, y, y1, phisum, x_out, lambda, Bi, hw, s);
         else launch_gap_smem<1, false>(x, M, y, y1, phisum, x_out, lambda, Bi, hw, s);
-    } else if (mask_bits) {
-        Mask<1> M{mask_bits, hw};
-        LAUNCH_GAP(1, M);
     } else {
         Mask<0> M{phi, hw};
         LAUNCH_GAP(0, M);

@@ -1,0 +1,232 @@
+// GAP projection with bulk-copy (TMA) staging of the frame stack.
+//
+// Same arithmetic as k_proj_gap_smem (PnP_SCI/python/pnp_sci_algo.py:640-645
+// with a packed binary mask): per pixel yb = sum_b phi_b x_b (in frame
+// order, fused multiply-adds), ACC: y1 += y - yb, r = (y1 - yb) / Phi_sum,
+// else r = (y - yb) / Phi_sum; x_out_b = x_b + lambda (r phi_b).
+//
+// Layout and schedule.  A tile is TP consecutive pixels of all B frames:
+// B rows of TP floats, each contiguous in HBM.  One thread per block issues
+// the B row copies of a tile with cp.async.bulk into shared memory and
+// arms an mbarrier with the byte count; the block waits on it, each thread
+// reduces 4 pixels over the frames from shared memory and writes the 4
+// updated pixels of every frame with 16-byte streaming stores.  Tiles are
+// double-buffered (two tiles in flight per block), blocks are persistent
+// (grid = resident blocks), and a buffer is refilled only after the whole
+// block has finished reading it.  x is read from HBM once and x_out written
+// once: 8 bytes per pixel and frame, plus 20 bytes per pixel of maps.
+//
+// Waits are bounded: a wait that gives up sets bit 0 of the device status
+// word (sci_device_status), waits a bounded time for the block's copies in
+// flight and ends the block.
+#include <algorithm>
+#include <cstdlib>
+
+#include "sci_common.cuh"
+
+namespace sci {
+
+__device__ unsigned int g_device_status;
+
+namespace {
+
+constexpr int kWaitPolls = 1 << 22;  // mbarrier polls before a wait gives up
+
+__device__ __forceinline__ uint32_t smem_u32(const void *p) {
+    return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+                 : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+                 "r"(bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
+    uint32_t ok;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\t"
+        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(ok)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    return ok != 0;
+}
+
+// Bounded wait for phase `parity` of `bar` to complete.
+__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
+    for (int i = 0; i < kWaitPolls; ++i)
+        if (mbar_try_wait(bar, parity)) return true;
+    return false;
+}
+
+__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes,
+                                         uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
+        ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
+        : "memory");
+}
+
+__device__ __forceinline__ float bit(uint32_t w, int b) { return ((w >> b) & 1u) ? 1.0f : 0.0f; }
+
+// Issues the copies of tile t into buffer `buf` (thread 0 only).  The
+// per-pixel maps are read with plain loads: staging them as well (28 KB
+// instead of 24 KB per block at 24 frames) measured slower, 150 vs 141 us.
+template <int TP>
+__device__ __forceinline__ void issue_tile(float *xs, uint64_t *bars, int buf, int64_t t,
+                                           const float *x, int B, int64_t hw) {
+    const int64_t p0 = t * TP;
+    const int64_t rem = hw - p0;
+    const unsigned n = (unsigned)(rem < TP ? rem : TP);
+    float *dst = xs + (int64_t)buf * B * TP;
+    mbar_expect_tx(bars + buf, (unsigned)B * n * 4u);
+    for (int b = 0; b < B; ++b) bulk_g2s(dst + b * TP, x + b * hw + p0, n * 4u, bars + buf);
+}
+
+template <int TP, bool ACC>
+__global__ void __launch_bounds__(TP / 4) k_proj_gap_tma(
+    const float *__restrict__ x, const uint32_t *__restrict__ bits, const float *__restrict__ y,
+    float *__restrict__ y1, const float *__restrict__ phisum, float *__restrict__ xo, float lam,
+    int B, int64_t hw) {
+    extern __shared__ __align__(128) float xs[];  // [2][B][TP]
+    __shared__ __align__(8) uint64_t bars[2];
+    const int tid = threadIdx.x;
+    const int64_t ntiles = (hw + TP - 1) / TP;
+    const int64_t G = gridDim.x;
+    if (tid == 0) {
+        mbar_init(bars + 0, 1);
+        mbar_init(bars + 1, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    const int64_t t0 = blockIdx.x;
+    if (tid == 0) {
+        if (t0 < ntiles) issue_tile<TP>(xs, bars, 0, t0, x, B, hw);
+        if (t0 + G < ntiles) issue_tile<TP>(xs, bars, 1, t0 + G, x, B, hw);
+    }
+    int i = 0;
+    for (int64_t t = t0; t < ntiles; t += G, ++i) {
+        const int buf = i & 1;
+        const unsigned parity = (unsigned)(i >> 1) & 1u;
+        const bool ok = mbar_wait(bars + buf, parity);
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) {
+                atomicOr(&g_device_status, 1u);
+                // let the copies in flight land before the block's shared
+                // memory is released
+                mbar_wait(bars + buf, parity);
+                if (t + G < ntiles) mbar_wait(bars + (buf ^ 1), (unsigned)((i + 1) >> 1) & 1u);
+            }
+            return;
+        }
+        const int64_t p0 = t * TP;
+        const int q = tid * 4;
+        if (p0 + q < hw) {  // hw % 4 == 0: all 4 pixels are inside
+            const int64_t p = p0 + q;
+            const float *xb = xs + (int64_t)buf * B * TP + q;
+            const uint4 w = __ldg(reinterpret_cast<const uint4 *>(bits + p));
+            float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll 4
+            for (int b = 0; b < B; ++b) {
+                const float4 v = *reinterpret_cast<const float4 *>(xb + b * TP);
+                s.x = fmaf(v.x, bit(w.x, b), s.x);
+                s.y = fmaf(v.y, bit(w.y, b), s.y);
+                s.z = fmaf(v.z, bit(w.z, b), s.z);
+                s.w = fmaf(v.w, bit(w.w, b), s.w);
+            }
+            const float4 yv = ldg4(y + p), ps = ldg4(phisum + p);
+            float4 r;
+            if (ACC) {
+                float4 tt = *reinterpret_cast<const float4 *>(y1 + p);
+                tt.x = tt.x + (yv.x - s.x);
+                tt.y = tt.y + (yv.y - s.y);
+                tt.z = tt.z + (yv.z - s.z);
+                tt.w = tt.w + (yv.w - s.w);
+                st4(y1 + p, tt);
+                r = make_float4(__fdiv_rn(tt.x - s.x, ps.x), __fdiv_rn(tt.y - s.y, ps.y),
+                                __fdiv_rn(tt.z - s.z, ps.z), __fdiv_rn(tt.w - s.w, ps.w));
+            } else {
+                r = make_float4(__fdiv_rn(yv.x - s.x, ps.x), __fdiv_rn(yv.y - s.y, ps.y),
+                                __fdiv_rn(yv.z - s.z, ps.z), __fdiv_rn(yv.w - s.w, ps.w));
+            }
+#pragma unroll 4
+            for (int b = 0; b < B; ++b) {
+                const float4 v = *reinterpret_cast<const float4 *>(xb + b * TP);
+                float4 o;
+                o.x = fmaf(lam, r.x * bit(w.x, b), v.x);
+                o.y = fmaf(lam, r.y * bit(w.y, b), v.y);
+                o.z = fmaf(lam, r.z * bit(w.z, b), v.z);
+                o.w = fmaf(lam, r.w * bit(w.w, b), v.w);
+                st4_cs(xo + b * hw + p, o);
+            }
+        }
+        __syncthreads();  // every thread is done with this buffer
+        if (tid == 0 && t + 2 * G < ntiles) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue_tile<TP>(xs, bars, buf, t + 2 * G, x, B, hw);
+        }
+    }
+}
+
+template <int TP>
+int launch_tp(const float *x, const uint32_t *bits, const float *y, float *y1,
+              const float *phisum, float *xo, float lam, bool acc, int B, int64_t hw,
+              cudaStream_t s) {
+    const size_t smem = sizeof(float) * 2 * (size_t)B * TP;
+    const int64_t ntiles = (hw + TP - 1) / TP;
+    // resident blocks per SM: 227 KB of shared memory (+1 KB reserved per block)
+    const int64_t per_sm =
+        std::max<int64_t>(1, std::min<int64_t>(16, (227 * 1024) / (int64_t)(smem + 1024)));
+    const unsigned g = (unsigned)std::min<int64_t>(ntiles, per_sm * kSMs);
+    auto kern = acc ? k_proj_gap_tma<TP, true> : k_proj_gap_tma<TP, false>;
+    // above 48 KB of dynamic shared memory needs the opt-in attribute; a
+    // host-side call, also valid while the stream is being captured
+    SCI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    kern<<<g, TP / 4, smem, s>>>(x, bits, y, y1, phisum, xo, lam, B, hw);
+    SCI_LAUNCHED("k_proj_gap_tma");
+    return SCI_OK;
+}
+
+}  // namespace
+
+// Packed mask, B <= 32, 16-byte aligned planes with hw % 4 == 0.  Returns
+// SCI_OK, or a negative code when the caller must use another kernel.
+int launch_proj_gap_tma(const float *x, const uint32_t *bits, const float *y, float *y1,
+                        const float *phisum, float *xo, float lam, bool acc, int B, int64_t hw,
+                        cudaStream_t s) {
+    const uintptr_t a = reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(bits) |
+                        reinterpret_cast<uintptr_t>(y) | reinterpret_cast<uintptr_t>(y1) |
+                        reinterpret_cast<uintptr_t>(phisum) | reinterpret_cast<uintptr_t>(xo);
+    if ((a & 15u) || hw % 4 || B < 1 || B > 32) return SCI_ERR_UNSUPPORTED;
+    // pixels per tile (SCI_PROJ_TP overrides).  Measured at 2048 x 2048 x
+    // 24: 128 (one warp, 24 KB, 9 blocks per SM) 141 us, 256 146 us, 512 153 us.
+    const char *e = getenv("SCI_PROJ_TP");
+    const int tp = e ? atoi(e) : 128;
+    if (tp == 512) return launch_tp<512>(x, bits, y, y1, phisum, xo, lam, acc, B, hw, s);
+    if (tp == 256) return launch_tp<256>(x, bits, y, y1, phisum, xo, lam, acc, B, hw, s);
+    return launch_tp<128>(x, bits, y, y1, phisum, xo, lam, acc, B, hw, s);
+}
+
+}  // namespace sci
+
+extern "C" int sci_device_status(unsigned int *status, int clear) {
+    SCI_CHECK_ARG(status, "sci_device_status: null pointer");
+    unsigned int v = 0;
+    cudaError_t e = cudaMemcpyFromSymbol(&v, sci::g_device_status, sizeof(v));
+    if (e != cudaSuccess) return sci::cuda_status(e, "cudaMemcpyFromSymbol");
+    if (clear && v) {
+        const unsigned int z = 0;
+        e = cudaMemcpyToSymbol(sci::g_device_status, &z, sizeof(z));
+        if (e != cudaSuccess) return sci::cuda_status(e, "cudaMemcpyToSymbol");
+    }
+    *status = v;
+    return SCI_OK;
+}

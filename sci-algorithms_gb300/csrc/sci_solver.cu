@@ -23,6 +23,10 @@ int tv_launch_impl(const float *f, float *u, float *resid, int64_t nf, int64_t H
                    void *workspace, size_t ws_bytes, cudaStream_t s, int force_R, int flags,
                    const uint32_t *proj_bits, const float *proj_c, float proj_lam);
 bool tv_proj_supported(int64_t nf, int64_t W, int K);
+int tvx_launch(int kind, const float *f, float *u, float *resid, int64_t nf, int64_t H,
+               int64_t W, float lam, int iters, int *steps, void *ws, size_t ws_bytes,
+               cudaStream_t s);
+size_t tvx_workspace_bytes(int kind, int64_t nf, int64_t H, int64_t W);
 
 namespace {
 
@@ -34,7 +38,9 @@ struct SolverWs {
 
 size_t round256(size_t b) { return (b + 255) & ~size_t(255); }
 
-size_t solver_layout(bool admm, int64_t B, int64_t H, int64_t W, int K, SolverWs *w,
+// tvm: 0 = scikit-image Chambolle (K steps with the stop test), 1..8 = the
+// MATLAB denoisers of sci_tv_matlab (K iterations).
+size_t solver_layout(bool admm, int64_t B, int64_t H, int64_t W, int K, int tvm, SolverWs *w,
                      char *base) {
     const size_t hw = (size_t)(H * W), n = (size_t)B * hw;
     size_t off = 0;
@@ -54,7 +60,7 @@ size_t solver_layout(bool admm, int64_t B, int64_t H, int64_t W, int K, SolverWs
         ob0 = take(sizeof(float) * n);
         ob1 = take(sizeof(float) * n);
     }
-    const size_t tvb = tv_workspace_bytes(B, H, W, K);
+    const size_t tvb = tvm ? tvx_workspace_bytes(tvm, B, H, W) : tv_workspace_bytes(B, H, W, K);
     const size_t otv = take(tvb);
     if (w) {
         w->y1 = admm ? nullptr : reinterpret_cast<float *>(base + oy1);
@@ -128,6 +134,7 @@ struct Args {
         put_bytes(k, o.iters);
         put_bytes(k, o.tv_iter_max);
         put_bytes(k, o.eps);
+        put_bytes(k, o.tvm);
         put_bytes(k, o.accelerate);
         put_bytes(k, o.gamma);
         put_bytes(k, o.orig);
@@ -148,12 +155,25 @@ int enqueue(const Args &a, cudaStream_t s) {
     const int64_t B = a.B, H = a.H, W = a.W, hw = H * W, n = B * hw;
     const int K = o.tv_iter_max;
     SolverWs w;
-    solver_layout(a.admm, B, H, W, K, &w, static_cast<char *>(a.ws));
+    solver_layout(a.admm, B, H, W, K, o.tvm, &w, static_cast<char *>(a.ws));
+    // the denoising step of iteration `it` (pnp_sci_algo.py:650, :812-813;
+    // MATLAB twin: gapdenoise.m:92-112, whose Chambolle files take 1/tvweight)
+    auto denoise = [&](const float *in, float *out, float *resid, int it) -> int {
+        int *steps = o.tv_steps ? o.tv_steps + (int64_t)it * B : nullptr;
+        if (o.tvm) {
+            const bool inv = o.tvm == 3 || o.tvm == 5 || o.tvm == 7;
+            const float lam = inv ? 1.0f / o.weights[it] : o.weights[it];
+            return tvx_launch(o.tvm, in, out, resid, B, H, W, lam, K, steps, w.tv, w.tv_bytes,
+                              s);
+        }
+        return tv_launch(in, out, resid, B, H, W, hw, o.weights[it], o.eps, K, steps, nullptr,
+                         w.tv, w.tv_bytes, s, 0);
+    };
     if (o.sqerr) SCI_CUDA(cudaMemsetAsync(o.sqerr, 0, sizeof(double) * o.iters, s));
     const bool aligned = ((reinterpret_cast<uintptr_t>(a.x0) | reinterpret_cast<uintptr_t>(a.x_out) |
                            reinterpret_cast<uintptr_t>(a.y) | reinterpret_cast<uintptr_t>(a.phisum) |
                            reinterpret_cast<uintptr_t>(a.bits)) & 15u) == 0;
-    if (!a.admm && a.bits && aligned && hw % 4 == 0 && tv_proj_supported(B, W, K)) {
+    if (!a.admm && !o.tvm && a.bits && aligned && hw % 4 == 0 && tv_proj_supported(B, W, K)) {
         // Fused iteration: a read-only pass forms the residual map c (and
         // y1); the TV kernel applies x + lambda (c phi_b) while it loads x.
         // x ping-pongs between x_out and xp; start so the last iterate
@@ -189,9 +209,7 @@ int enqueue(const Args &a, cudaStream_t s) {
             int e = sci_proj_gap(a.x_out, a.phi, a.bits, a.y, w.y1, a.phisum, w.xp, o.lambdas[it],
                                  o.accelerate, B, H, W, s);
             if (e) return e;
-            e = tv_launch(w.xp, a.x_out, nullptr, B, H, W, hw, o.weights[it], o.eps, K,
-                          o.tv_steps ? o.tv_steps + (int64_t)it * B : nullptr, nullptr, w.tv,
-                          w.tv_bytes, s, 0);
+            e = denoise(w.xp, a.x_out, nullptr, it);
             if (e) return e;
             if (o.orig && o.sqerr) {
                 e = sci_sqerr_accum(o.orig, a.x_out, n, o.sqerr + it, s);
@@ -211,9 +229,7 @@ int enqueue(const Args &a, cudaStream_t s) {
                               want_x ? a.x_out : nullptr, o.lambdas[it], gamma, B, H, W, s);
         if (e) return e;
         // theta = TV(x - b);  b = b - (x - theta) = theta - v
-        e = tv_launch(w.v, w.theta, bnext, B, H, W, hw, o.weights[it], o.eps, K,
-                      o.tv_steps ? o.tv_steps + (int64_t)it * B : nullptr, nullptr, w.tv,
-                      w.tv_bytes, s, 0);
+        e = denoise(w.v, w.theta, bnext, it);
         if (e) return e;
         if (o.orig && o.sqerr) {
             e = sci_sqerr_accum(o.orig, a.x_out, n, o.sqerr + it, s);
@@ -235,7 +251,10 @@ int solve(const Args &a, void *stream) {
     for (int i = 0; i < o.iters; ++i)
         SCI_CHECK_ARG(o.weights[i] > 0.f, "solver: tv_weight[%d] = %g must be > 0", i,
                       (double)o.weights[i]);
-    const size_t need = solver_layout(a.admm, a.B, a.H, a.W, o.tv_iter_max, nullptr, nullptr);
+    SCI_CHECK_ARG(o.tvm >= 0 && o.tvm <= 8, "solver: tvm must be 0..8 (got %d)", o.tvm);
+    SCI_CHECK_ARG(!o.tvm || (a.H >= 2 && a.W >= 2), "solver: the MATLAB TVs need H, W >= 2");
+    const size_t need =
+        solver_layout(a.admm, a.B, a.H, a.W, o.tv_iter_max, o.tvm, nullptr, nullptr);
     SCI_CHECK_ARG(a.ws && a.ws_bytes >= need, "solver: workspace of %zu bytes needed, got %zu",
                   need, a.ws_bytes);
     cudaStream_t s = as_stream(stream);
@@ -294,10 +313,12 @@ extern "C" {
 
 int sci_solver_workspace_bytes(int64_t B, int64_t H, int64_t W, const sci_solve_opts *opts,
                                size_t *bytes) {
-    SCI_CHECK_ARG(opts && bytes && B >= 1 && H >= 1 && W >= 1 && opts->tv_iter_max >= 1,
+    SCI_CHECK_ARG(opts && bytes && B >= 1 && H >= 1 && W >= 1 && opts->tv_iter_max >= 1 &&
+                      opts->tvm >= 0 && opts->tvm <= 8,
                   "sci_solver_workspace_bytes: bad argument");
-    const size_t g = solver_layout(false, B, H, W, opts->tv_iter_max, nullptr, nullptr);
-    const size_t a = solver_layout(true, B, H, W, opts->tv_iter_max, nullptr, nullptr);
+    const int t = opts->tvm;
+    const size_t g = solver_layout(false, B, H, W, opts->tv_iter_max, t, nullptr, nullptr);
+    const size_t a = solver_layout(true, B, H, W, opts->tv_iter_max, t, nullptr, nullptr);
     *bytes = g > a ? g : a;
     return SCI_OK;
 }

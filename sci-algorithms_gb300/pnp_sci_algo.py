@@ -3,7 +3,10 @@
 Mirrors ``PnP_SCI/python/pnp_sci_algo.py``: ``admmdenoise_cacti``
 (``:479-534``), ``gap_denoise`` (``:536-706``), ``admm_denoise``
 (``:708-864``) and the legacy ``GAP_TV_rec`` / ``ADMM_TV_rec``
-(``:866-907``), for ``denoiser='tv'`` with ``tvm='tv_chambolle'``.
+(``:866-907``), for ``denoiser='tv'``: ``tvm='tv_chambolle'`` (the
+scikit-image TV of the Python reference) or one of the MATLAB twin's TV
+denoisers (``tvm`` names of ``PnP_SCI/matlab/algorithms/gapdenoise.m:92-112``,
+with gapdenoise's parameters and iteration counts).
 
 * When ``A`` / ``At`` are the bound methods of one ``MaskOperator`` (from
   ``make_ops(mask)``), the whole iteration loop runs natively
@@ -31,7 +34,7 @@ import torch
 from . import _dev
 from .metrics import frame_psnr, frame_ssim
 from .solver import Solver
-from .tv import tv_frames, tv_workspace
+from .tv import TVM, tv_frames, tv_matlab_frames, tv_matlab_workspace, tv_workspace, tvm_kind
 from .cassi import CassiOperator, CassiSolver
 from .utils import MaskOperator, operator_of, psnr_from_mse, sum_sq_err
 
@@ -39,8 +42,7 @@ from .utils import MaskOperator, operator_of, psnr_from_mse, sum_sq_err
 def _check_plugin(denoiser, tvm="tv_chambolle"):
     if str(denoiser).lower() != "tv":
         raise ValueError("Unsupported denoiser {}!".format(denoiser))
-    if tvm != "tv_chambolle":
-        raise ValueError("Unsupported TV denoiser {}!".format(tvm))
+    tvm_kind(tvm)  # raises ValueError for an unknown name
 
 
 def _total_iters(iter_max, sigma):
@@ -59,12 +61,14 @@ def _metrics(x_planar, X_orig, like):
 
 
 def _solve(projmeth, y, Phi_sum, A, At, iters, _lambda, tv_weight, tv_iter_max, eps,
-           accelerate, gamma, x0, X_orig, show_iqa, use_graph):
+           accelerate, gamma, x0, X_orig, show_iqa, use_graph, tvm="tv_chambolle"):
     """Shared body of gap_denoise / admm_denoise (native or plug-in)."""
     op = operator_of(A, At)
     y_d = _dev.plane(y)
     ps_d = _dev.plane(Phi_sum)
     want_iqa = show_iqa and X_orig is not None
+    if isinstance(op, CassiOperator) and tvm != "tv_chambolle":
+        raise ValueError("the spectral (CASSI) solver runs the scikit-image TV only")
     if isinstance(op, CassiOperator) and projmeth == "gap":
         solver = CassiSolver(op, iters, _lambda, tv_weight, tv_iter_max, eps, accelerate)
         x0_d = None if x0 is None else _dev.planar(x0)
@@ -73,7 +77,7 @@ def _solve(projmeth, y, Phi_sum, A, At, iters, _lambda, tv_weight, tv_iter_max, 
         return x, (solver.psnr_all() if want_iqa else [])
     if isinstance(op, MaskOperator):
         solver = Solver(op, projmeth, iters, _lambda, tv_weight, tv_iter_max, eps, accelerate,
-                        gamma, use_graph=use_graph)
+                        gamma, use_graph=use_graph, tvm=tvm)
         x0_d = None if x0 is None else _dev.planar(x0)
         orig_d = _dev.planar(X_orig) if want_iqa else None
         x = solver.run(y_d, x0=x0_d, phisum=ps_d, orig=orig_d)
@@ -82,14 +86,15 @@ def _solve(projmeth, y, Phi_sum, A, At, iters, _lambda, tv_weight, tv_iter_max, 
     if not (callable(A) and callable(At)):
         raise TypeError("A and At must be callables (or make_ops(mask))")
     return _solve_plugin(projmeth, y_d, ps_d, A, At, iters, _lambda, tv_weight, tv_iter_max,
-                         eps, accelerate, gamma, x0, X_orig if want_iqa else None)
+                         eps, accelerate, gamma, x0, X_orig if want_iqa else None, tvm)
 
 
 def _solve_plugin(projmeth, y, ps, A, At, iters, _lambda, tv_weight, tv_iter_max, eps,
-                  accelerate, gamma, x0, X_orig):
+                  accelerate, gamma, x0, X_orig, tvm="tv_chambolle"):
     """Iteration loop with foreign A / At callables (CUDA tensors in/out)."""
     lam = _dev.schedule(_lambda, iters)
     wts = _dev.schedule(tv_weight, iters)
+    kind = tvm_kind(tvm)
 
     def fwd(xp):
         return _dev.plane(A(xp.permute(1, 2, 0)))
@@ -99,7 +104,17 @@ def _solve_plugin(projmeth, y, ps, A, At, iters, _lambda, tv_weight, tv_iter_max
 
     x = adj(y) if x0 is None else _dev.planar(x0)
     B, H, W = x.shape
-    ws = tv_workspace(B, H, W, tv_iter_max, x.device)
+    if kind:
+        ws = tv_matlab_workspace(kind, B, H, W, x.device)
+        _, param, tv_iters = TVM[tvm]
+
+    def denoise(v, k):
+        if kind:
+            return tv_matlab_frames(v, kind, param(float(wts[k])), tv_iters, workspace=ws)
+        return tv_frames(v, float(wts[k]), tv_iter_max, eps, workspace=ws)
+
+    if not kind:
+        ws = tv_workspace(B, H, W, tv_iter_max, x.device)
     orig = None if X_orig is None else _dev.planar(X_orig)
     psnr_all = []
     if projmeth == "gap":
@@ -111,7 +126,7 @@ def _solve_plugin(projmeth, y, ps, A, At, iters, _lambda, tv_weight, tv_iter_max
                 xp = x + float(lam[k]) * adj((y1 - yb) / ps)
             else:
                 xp = x + float(lam[k]) * adj((y - yb) / ps)
-            x = tv_frames(xp.contiguous(), float(wts[k]), tv_iter_max, eps, workspace=ws)
+            x = denoise(xp.contiguous(), k)
             if orig is not None:
                 psnr_all.append(psnr_from_mse(sum_sq_err(orig, x) / x.numel()))
         return x, psnr_all
@@ -122,9 +137,8 @@ def _solve_plugin(projmeth, y, ps, A, At, iters, _lambda, tv_weight, tv_iter_max
         yb = fwd(t)
         x = t + float(lam[k]) * adj((y - yb) / (ps + gamma))
         v = (x - b).contiguous()
-        resid = torch.empty_like(v)
-        theta = tv_frames(v, float(wts[k]), tv_iter_max, eps, resid=resid, workspace=ws)
-        b = resid  # b - (x - theta) = theta - (x - b)
+        theta = denoise(v, k)
+        b = theta - v  # b - (x - theta) = theta - (x - b)
         if orig is not None:
             psnr_all.append(psnr_from_mse(sum_sq_err(orig, x.contiguous()) / x.numel()))
     return x, psnr_all
@@ -141,7 +155,7 @@ def gap_denoise(y, Phi_sum, A, At, _lambda=1, accelerate=True, denoiser='tv', it
     _check_plugin(denoiser, tvm)
     iters = _total_iters(iter_max, sigma)
     x, psnr_all = _solve("gap", y, Phi_sum, A, At, iters, _lambda, tv_weight, tv_iter_max, eps,
-                         accelerate, 0.0, x0, X_orig, show_iqa, use_graph)
+                         accelerate, 0.0, x0, X_orig, show_iqa, use_graph, tvm)
     psnr_, ssim_ = _metrics(x, X_orig, y)
     return _dev.unplanar(x, y), psnr_, ssim_, psnr_all
 
@@ -149,12 +163,12 @@ def gap_denoise(y, Phi_sum, A, At, _lambda=1, accelerate=True, denoiser='tv', it
 def admm_denoise(y, Phi_sum, A, At, _lambda=1, gamma=0.01, denoiser='tv', iter_max=50,
                  noise_estimate=False, sigma=None, tv_weight=0.1, tv_iter_max=5,
                  multichannel=True, x0=None, model=None, X_orig=None, show_iqa=True,
-                 eps=2.e-4, use_graph=True):
+                 tvm='tv_chambolle', eps=2.e-4, use_graph=True):
     """ADMM with the TV denoiser (``pnp_sci_algo.py:708-864``); returns x."""
-    _check_plugin(denoiser)
+    _check_plugin(denoiser, tvm)
     iters = _total_iters(iter_max, sigma)
     x, psnr_all = _solve("admm", y, Phi_sum, A, At, iters, _lambda, tv_weight, tv_iter_max,
-                         eps, True, gamma, x0, X_orig, show_iqa, use_graph)
+                         eps, True, gamma, x0, X_orig, show_iqa, use_graph, tvm)
     psnr_, ssim_ = _metrics(x, X_orig, y)
     return _dev.unplanar(x, y), psnr_, ssim_, psnr_all
 

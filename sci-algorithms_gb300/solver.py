@@ -15,6 +15,7 @@ import torch
 
 from . import _dev
 from ._lib import SolveOpts, call
+from .tv import TVM, tvm_kind
 
 
 def _fptr(a):
@@ -26,7 +27,7 @@ class Solver:
 
     def __init__(self, op, projmeth="gap", iters=50, lambdas=1.0, tv_weight=0.1,
                  tv_iter_max=5, eps=2e-4, accelerate=True, gamma=0.01, gammas=None,
-                 use_graph=True, use_bits=True):
+                 use_graph=True, use_bits=True, tvm="tv_chambolle"):
         if projmeth not in ("gap", "admm"):
             raise ValueError("Unsupported projection method %s" % projmeth)
         self.op = op
@@ -44,7 +45,10 @@ class Solver:
         o.iters = self.iters
         o.lambdas = _fptr(self._lam)
         o.weights = _fptr(self._w)
-        o.tv_iter_max = int(tv_iter_max)
+        # tvm: the scikit-image Chambolle TV, or a MATLAB-twin denoiser with
+        # gapdenoise.m's iteration count (tv_iter_max does not apply to it)
+        o.tvm = tvm_kind(tvm)
+        o.tv_iter_max = int(tv_iter_max) if o.tvm == 0 else TVM[tvm][2]
         o.eps = float(eps)
         o.accelerate = 1 if accelerate else 0
         o.gamma = float(gamma)
@@ -60,6 +64,7 @@ class Solver:
         self.x = torch.empty((self.B, self.H, self.W), dtype=torch.float32, device=op.dev)
         self.sqerr = None
         self.tv_steps = None
+        self._y_dev = None  # run_host's device copy of the measurement
 
     def run(self, y, x0=None, phisum=None, orig=None, tv_steps=False, out=None):
         """Solve on the device.  y: (H, W) float32 CUDA; x0: (B, H, W) or None
@@ -103,7 +108,12 @@ class Solver:
     def run_host(self, y_host, x_host=None):
         """End to end: copy a pinned host measurement (H, W) in, solve, copy
         the result (B, H, W) back into pinned ``x_host`` (allocated if None)."""
-        y = y_host.to(self.op.dev, non_blocking=True)
+        # a buffer of the solver's own, so that every call replays the same
+        # cached graph (its key holds the device pointers)
+        if self._y_dev is None:
+            self._y_dev = torch.empty((self.H, self.W), dtype=torch.float32, device=self.op.dev)
+        y = self._y_dev
+        y.copy_(y_host, non_blocking=True)
         x = self.run(y)
         if x_host is None:
             x_host = torch.empty(x.shape, dtype=torch.float32, pin_memory=True)

@@ -66,3 +66,62 @@ def denoise_tv_chambolle(image, weight=0.1, eps=2.e-4, n_iter_max=200, multichan
     if not _dev.is_torch(image):
         out = out.astype(np.asarray(image).dtype, copy=False)
     return out
+
+
+# ------------------------------------------------- MATLAB-twin TV denoisers
+# gapdenoise.m:92-112: tvm name -> (kind of sci_tv_matlab, the file's
+# parameter as a function of tvweight, iterations)
+TVM = {
+    "ATV_ClipA": (1, lambda w: w, 5),
+    "ATV_ClipB": (2, lambda w: w, 5),
+    "ATV_cham": (3, lambda w: 1.0 / w, 5),
+    "ATV_FGP": (4, lambda w: w, 2),
+    "ITV2D_cham": (5, lambda w: 1.0 / w, 5),
+    "ITV2D_FGP": (6, lambda w: w, 2),
+    "ITV3D_cham": (7, lambda w: 1.0 / w, 5),
+    "ITV3D_FGP": (8, lambda w: w, 2),
+}
+
+
+def tvm_kind(tvm):
+    """The sci_tv_matlab kind of a tvm name ('tv_chambolle' -> 0)."""
+    if tvm == "tv_chambolle":
+        return 0
+    if tvm not in TVM:
+        raise ValueError("Unsupported TV denoiser {}!".format(tvm))
+    return TVM[tvm][0]
+
+
+def tv_matlab_workspace(kind, nframes, H, W, dev=None):
+    n = ctypes.c_size_t()
+    call("sci_tv_matlab_workspace_bytes", int(kind), nframes, H, W, ctypes.byref(n))
+    return _dev.workspace(n.value, dev)
+
+
+def tv_matlab_frames(f, tvm, lam, iters, u=None, workspace=None):
+    """A MATLAB-twin denoiser (tvm name or kind) with the file's own
+    parameters on a planar (nframes, H, W) float32 CUDA tensor."""
+    if f.dim() != 3 or f.dtype != torch.float32 or not f.is_cuda or not f.is_contiguous():
+        raise ValueError("tv_matlab_frames expects a contiguous float32 CUDA tensor (F, H, W)")
+    kind = tvm if isinstance(tvm, int) else tvm_kind(tvm)
+    nf, H, W = f.shape
+    if u is None:
+        u = torch.empty_like(f)
+    if workspace is None:
+        workspace = tv_matlab_workspace(kind, nf, H, W, f.device)
+    call("sci_tv_matlab", kind, f.data_ptr(), u.data_ptr(), nf, H, W, float(lam), int(iters),
+         workspace.data_ptr(), workspace.numel(), _dev.stream_handle())
+    return u
+
+
+def denoise_tv_matlab(v, tvm, tvweight):
+    """The denoising step of gapdenoise.m:92-112 for `tvm` on an H x W x B
+    stack (numpy or torch), with gapdenoise's parameters and iteration
+    counts."""
+    tvm_kind(tvm)  # ValueError for an unknown name
+    kind, param, iters = TVM[tvm]
+    f = _dev.planar(v)
+    out = _dev.unplanar(tv_matlab_frames(f, kind, param(float(tvweight)), iters), v)
+    if not _dev.is_torch(v):
+        out = out.astype(np.asarray(v).dtype, copy=False)
+    return out

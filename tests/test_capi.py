@@ -90,8 +90,9 @@ def test_schedule_and_layout_helpers():
     assert _total_iters([10, 10, 5], [1, 2, 3]) == 25
     with pytest.raises(ValueError):
         _check_plugin("ffdnet")
+    _check_plugin("tv", "ATV_ClipA")  # the MATLAB twin's TV names are accepted
     with pytest.raises(ValueError):
-        _check_plugin("tv", "ATV_ClipA")
+        _check_plugin("tv", "ATV_ClipC")
     assert _flip("updown", 1) and not _flip("updown", 0)
     assert _flip("downup", 0) and not _flip("plain", 1)
 

@@ -1,4 +1,6 @@
 """GPU parity of the mask operators and projections against the oracle."""
+import ctypes
+
 import numpy as np
 import pytest
 import torch
@@ -103,6 +105,47 @@ def test_proj_gap_matches_reference_step(accelerate, packed, W):
     assert rel(_dev.unplanar(out, x), xr) < RTOL
     if accelerate:
         assert rel(y1d.cpu().numpy(), y1r) < RTOL
+
+
+def device_status():
+    v = ctypes.c_uint(0)
+    call("sci_device_status", ctypes.byref(v), 1)
+    return v.value
+
+
+@pytest.mark.parametrize("tile", ["256", "128", "512"])
+@pytest.mark.parametrize("B,H,W", [(1, 16, 16), (8, 37, 64), (24, 130, 260), (32, 64, 96),
+                                   (24, 512, 512), (8, 37, 61)])
+def test_proj_gap_bulk_copy_kernel_is_bitwise_equal(monkeypatch, B, H, W, tile):
+    """The bulk-copy (TMA) staged projection against the register/shared
+    memory kernel: identical x_out and y1, including partial last tiles,
+    32 frames, grids with several tiles per block, and W % 4 != 0 (which
+    the bulk-copy path declines)."""
+    rng = np.random.default_rng(B * 1000 + W)
+    mask = (rng.random((H, W, B)) < 0.5).astype(np.float64)
+    op = sci.MaskOperator(mask)
+    assert op.bits is not None
+    x = _dev.planar(rng.random((H, W, B)))
+    y = _dev.plane(rng.random((H, W)) * 4)
+    msum = mask.sum(axis=2)
+    msum[msum == 0] = 1
+    ps = _dev.plane(msum)
+    monkeypatch.setenv("SCI_PROJ_TP", tile)
+    outs = []
+    for tma in ("1", "0"):
+        monkeypatch.setenv("SCI_PROJ_TMA", tma)
+        for acc in (1, 0):
+            y1 = _dev.plane(np.full((H, W), 0.25))
+            out = torch.empty_like(x)
+            call("sci_proj_gap", x.data_ptr(), None, op.bits.data_ptr(), y.data_ptr(),
+                 y1.data_ptr(), ps.data_ptr(), out.data_ptr(), 0.7, acc, B, H, W,
+                 _dev.stream_handle())
+            torch.cuda.synchronize()
+            outs.append((out.clone(), y1.clone()))
+    for (a, ya), (b, yb) in zip(outs[:2], outs[2:]):
+        assert torch.equal(a, b)
+        assert torch.equal(ya, yb)
+    assert device_status() == 0
 
 
 @pytest.mark.parametrize("packed", [True, False])
