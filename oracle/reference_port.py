@@ -298,3 +298,124 @@ def ADMM_TV_rec(y, Phi, A, At, Phi_sum, maxiter, step_size, weight, row, col,
         weight = 0.999 * weight
         eta = 0.998 * eta
     return v
+
+
+# ---------------------------------------------------------------- Bayer loops
+BAYER = [[0, 0], [0, 1], [1, 0], [1, 1]]  # pnp_sci_algo.py:112 (RGGB sub-lattices)
+
+
+def _bayer_split(y_bayer, Phi_bayer, x0_bayer):
+    """The channel set-up of pnp_sci_algo.py:120-140 / :353-379: float32
+    sub-lattice measurements, masks, Phi_sum (zeros -> 1) and x0."""
+    nrow, ncol, nmask = Phi_bayer.shape
+    yall = np.zeros([nrow // 2, ncol // 2, 4], dtype=np.float32)
+    Phiall = np.zeros([nrow // 2, ncol // 2, nmask, 4], dtype=np.float32)
+    Phi_sumall = np.zeros([nrow // 2, ncol // 2, 4], dtype=np.float32)
+    x0all = np.zeros([nrow // 2, ncol // 2, nmask, 4], dtype=np.float32)
+    for ib, b in enumerate(BAYER):
+        yall[..., ib] = y_bayer[b[0]::2, b[1]::2]
+        Phiall[..., ib] = Phi_bayer[b[0]::2, b[1]::2]
+        Phib_sum = np.sum(Phiall[..., ib], axis=2)
+        Phib_sum[Phib_sum == 0] = 1
+        Phi_sumall[..., ib] = Phib_sum
+        if x0_bayer is None:
+            x0all[..., ib] = At_(yall[..., ib], Phiall[..., ib])
+        else:
+            x0all[..., ib] = x0_bayer[b[0]::2, b[1]::2]
+    return yall, Phiall, Phi_sumall, x0all
+
+
+def _bayer_join(xall, like):
+    x_bayer = np.zeros_like(like)
+    for ib, b in enumerate(BAYER):
+        x_bayer[b[0]::2, b[1]::2] = xall[..., ib]
+    return x_bayer
+
+
+def gap_denoise_bayer(y_bayer, Phi_bayer, _lambda=1, accelerate=True, denoiser='tv',
+                      iter_max=50, noise_estimate=True, sigma=None, tv_weight=0.1,
+                      tv_iter_max=5, multichannel=True, x0_bayer=None, X_orig=None,
+                      model=None, show_iqa=True):
+    """``PnP_SCI/python/pnp_sci_algo.py:20-265`` with ``denoiser='tv'``.
+
+    Four independent GAP(-acc) projections on the sub-lattice channels
+    (``:149-157``, in place on float32 arrays), then one Chambolle TV over
+    the nmask*4 frames (``:161-165``).  PSNR per iteration on the
+    re-assembled Bayer image (``:241-246``)."""
+    if denoiser.lower() != 'tv':
+        raise ValueError('oracle supports denoiser="tv"')
+    if not isinstance(sigma, list):
+        sigma = [sigma]
+    if not isinstance(iter_max, list):
+        iter_max = [iter_max] * len(sigma)
+    nrow, ncol, nmask = Phi_bayer.shape
+    yall, Phiall, Phi_sumall, x0all = _bayer_split(y_bayer, Phi_bayer, x0_bayer)
+    y1all = np.zeros_like(yall)
+    xall = x0all
+    psnr_all = []
+    for idx, nsig in enumerate(sigma):
+        for it in range(iter_max[idx]):
+            for ib in range(4):
+                yb = A_(xall[..., ib], Phiall[..., ib])
+                if accelerate:
+                    y1all[..., ib] += (yall[..., ib] - yb)
+                    xall[..., ib] += _lambda * (At_((y1all[..., ib] - yb) / Phi_sumall[..., ib],
+                                                    Phiall[..., ib]))
+                else:
+                    xall[..., ib] += _lambda * (At_((yall[..., ib] - yb) / Phi_sumall[..., ib],
+                                                    Phiall[..., ib]))
+            xall_vch = xall.reshape([nrow // 2, ncol // 2, nmask * 4])
+            xall_vch = denoise_tv_chambolle(xall_vch, tv_weight, n_iter_max=tv_iter_max,
+                                            multichannel=multichannel)
+            xall = xall_vch.reshape([nrow // 2, ncol // 2, nmask, 4])
+            if show_iqa and X_orig is not None:
+                psnr_all.append(compare_psnr(X_orig, _bayer_join(xall, Phi_bayer),
+                                             data_range=1.))
+    x_bayer = _bayer_join(xall, Phi_bayer)
+    psnr_, ssim_ = [], []
+    if X_orig is not None:
+        for imask in range(nmask):
+            psnr_.append(compare_psnr(X_orig[:, :, imask], x_bayer[:, :, imask], data_range=1.))
+            ssim_.append(compare_ssim(X_orig[:, :, imask], x_bayer[:, :, imask], data_range=1.))
+    return x_bayer, psnr_, ssim_, psnr_all
+
+
+def admm_denoise_bayer(y_bayer, Phi_bayer, _lambda=1, gamma=0.01, denoiser='tv',
+                       iter_max=50, noise_estimate=True, sigma=None, tv_weight=0.1,
+                       tv_iter_max=5, multichannel=True, x0_bayer=None, X_orig=None,
+                       model=None, show_iqa=True):
+    """``PnP_SCI/python/pnp_sci_algo.py:268-476`` with ``denoiser='tv'``.
+
+    The reference reads the multiplier ``ball`` before assigning it
+    (``:400``; it initialises ``b``, ``:389``), so it cannot run; this
+    restatement starts ``ball`` at zero, as admm_denoise does (``:802``).
+    Per iteration: four ADMM projections x = theta + b + lambda At((y -
+    A(theta + b)) / (Phi_sum + gamma)) (``:399-401``), theta = TV(x - b)
+    over the nmask*4 frames (``:407-410``), b = b - (x - theta) (``:442``).
+    Returns the Bayer image of x and the PSNR per iteration."""
+    if denoiser.lower() != 'tv':
+        raise ValueError('oracle supports denoiser="tv"')
+    if not isinstance(sigma, list):
+        sigma = [sigma]
+    if not isinstance(iter_max, list):
+        iter_max = [iter_max] * len(sigma)
+    nrow, ncol, nmask = Phi_bayer.shape
+    yall, Phiall, Phi_sumall, x0all = _bayer_split(y_bayer, Phi_bayer, x0_bayer)
+    xall = x0all.copy()
+    thetaall = x0all.copy()
+    ball = np.zeros_like(x0all)
+    psnr_all = []
+    for idx, nsig in enumerate(sigma):
+        for it in range(iter_max[idx]):
+            for ib in range(4):
+                yb = A_(thetaall[..., ib] + ball[..., ib], Phiall[..., ib])
+                xall[..., ib] = thetaall[..., ib] + ball[..., ib] + _lambda * (
+                    At_((yall[..., ib] - yb) / (Phi_sumall[..., ib] + gamma), Phiall[..., ib]))
+            thetaall_vch = (xall - ball).reshape([nrow // 2, ncol // 2, nmask * 4])
+            thetaall_vch = denoise_tv_chambolle(thetaall_vch, tv_weight,
+                                                n_iter_max=tv_iter_max, multichannel=multichannel)
+            thetaall = thetaall_vch.reshape([nrow // 2, ncol // 2, nmask, 4])
+            ball = ball - (xall - thetaall)
+            if show_iqa and X_orig is not None:
+                psnr_all.append(psnr(X_orig, _bayer_join(xall, Phi_bayer)))
+    return _bayer_join(xall, Phi_bayer), psnr_all

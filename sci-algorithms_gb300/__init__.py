@@ -14,6 +14,7 @@ from .tv import (TVM, denoise_tv_chambolle, denoise_tv_matlab, tv_frames,  # noq
 from .pnp_sci_algo import (admmdenoise_cacti, gap_denoise, admm_denoise,  # noqa: F401
                            GAP_TV_rec, ADMM_TV_rec)
 from .solver import Solver  # noqa: F401
+from .bayer import gap_denoise_bayer, admm_denoise_bayer  # noqa: F401
 from .cassi import CassiOperator, CassiSolver, make_cassi_ops  # noqa: F401
 from .unrolled import (UnrolledGapTV, unrolled_loss, unrolled_workspace,  # noqa: F401
                        torch_unrolled_loss)

@@ -16,7 +16,8 @@ here, so stand-in modules are registered first:
   ``colour_demosaicing`` denoisers (never called on the TV path).
 
 Everything else -- ``A_``, ``At_``, ``psnr``, ``gap_denoise``,
-``admm_denoise``, ``admmdenoise_cacti``, ``ADMM_TV_rec`` -- is the
+``admm_denoise``, ``admmdenoise_cacti``, ``ADMM_TV_rec``,
+``gap_denoise_bayer`` -- is the
 reference's code, run on the seeded inputs below in float64.  Each fixture
 stores the inputs and the reference's outputs; ``tests/test_oracle.py``
 checks ``oracle.reference_port`` against them bit for bit, and the GPU tests
@@ -194,6 +195,26 @@ def main(ref_root):
     v = ref.ADMM_TV_rec(meas, mask, A_, At_, msum, 6, 1.0, 0.1, 20, 20, 4, 0.01, orig)
     g = ref.GAP_TV_rec(meas, mask, A_, At_, msum, 5, 1.0, 0.1, 20, 20, 4, orig)
     out["legacy"] = dict(meas=meas, mask=mask, orig=orig, admm=v, gap=g)
+
+    # --- Bayer GAP-TV (pnp_sci_algo.py:20-265): an RGGB mosaic measured
+    # through a full-resolution mask; four sub-lattice problems
+    orig, mask = small_video(24, 32, 6, seed=80)
+    meas = np.sum(orig * mask, axis=2)
+    for acc in (True, False):
+        xb, psnr_, ssim_, psnrall_ = ref.gap_denoise_bayer(
+            meas, mask, _lambda=1, accelerate=acc, denoiser='tv', iter_max=8,
+            tv_weight=0.1, tv_iter_max=5, X_orig=orig)
+        out["bayer_gap" + ("_acc" if acc else "")] = dict(
+            meas=meas, mask=mask, orig=orig, x=np.asarray(xb, np.float64),
+            psnr=np.array(psnr_), ssim=np.array(ssim_), psnrall=np.array(psnrall_),
+            accelerate=acc)
+    # admm_denoise_bayer (:268-476) reads `ball` before assigning it (:400)
+    # and raises; its restatement in the oracle starts the multiplier at 0.
+    try:
+        ref.admm_denoise_bayer(meas, mask, iter_max=1, X_orig=orig)
+        raise RuntimeError("admm_denoise_bayer ran; regenerate its fixture")
+    except NameError:
+        pass
 
     for name, rec in out.items():
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **rec)

@@ -64,6 +64,37 @@ def test_legacy_loops_bit_exact(golden):
     assert np.array_equal(f, g["gap"])
 
 
+@pytest.mark.parametrize("case", ["bayer_gap", "bayer_gap_acc"])
+def test_bayer_gap_bit_exact(golden, case):
+    g = golden(case)
+    x, psnr_, ssim_, psnrall_ = port.gap_denoise_bayer(
+        g["meas"], g["mask"], _lambda=1, accelerate=bool(g["accelerate"]), iter_max=8,
+        tv_weight=0.1, tv_iter_max=5, X_orig=g["orig"])
+    assert np.array_equal(np.asarray(x, np.float64), g["x"])
+    assert np.array_equal(np.array(psnr_), g["psnr"])
+    assert np.array_equal(np.array(ssim_), g["ssim"])
+    assert np.array_equal(np.array(psnrall_), g["psnrall"])
+
+
+def test_bayer_admm_is_four_channel_admm(golden):
+    """The ADMM Bayer restatement (the reference's raises at :400) is the
+    per-channel admm_denoise on the four sub-lattices."""
+    g = golden("bayer_gap")
+    y, mask = g["meas"], g["mask"]
+    x, psnr_all = port.admm_denoise_bayer(y, mask, gamma=0.02, iter_max=6, tv_weight=0.1,
+                                          X_orig=g["orig"])
+    assert len(psnr_all) == 6
+    for b0, b1 in port.BAYER:
+        m = mask[b0::2, b1::2].astype(np.float32)
+        yc = y[b0::2, b1::2].astype(np.float32)
+        ms = m.sum(axis=2)
+        ms[ms == 0] = 1
+        xc, _, _, _ = port.admm_denoise(yc, ms, lambda v: port.A_(v, m),
+                                        lambda r: port.At_(r, m), gamma=0.02, iter_max=6,
+                                        tv_weight=0.1)
+        assert np.allclose(x[b0::2, b1::2], xc, rtol=0, atol=1e-5)
+
+
 def test_config0_inputs_and_digest(golden):
     import hashlib
     g = golden("config0")
