@@ -38,6 +38,7 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
 H, W, B, ITERS, TV_ITERS = 2048, 2048, 24, 60, 5
+STACK = (H, W, B)  # the headline stack, for functions whose locals reuse the names
 METRIC = "GAP-TV iter/s & HBM GB/s vs peak; unrolled fwd+bwd ms vs autograd at 1e-4 rel"
 WORKLOAD = "gap_tv_2048x2048x24"
 
@@ -348,7 +349,8 @@ def run_kernel(args):
 
 
 def side_workloads(dev):
-    """The spectral (CASSI) and differentiable workloads, timed with events."""
+    """The spectral (CASSI), differentiable, batched, MATLAB-TV and Bayer
+    workloads, timed with events."""
     import torch
     import sci_algorithms_gb300 as sci
     from sci_algorithms_gb300 import _dev
@@ -423,6 +425,43 @@ def side_workloads(dev):
                       "elements": elems, "ms_per_batch": ms_b,
                       "element_iters_per_s": elems * 50 / (ms_b * 1e-3),
                       "chunk_rows": sorted(set(bsol.chunk_rows()))}
+    del bsol, meas
+
+    # the MATLAB twin's TV denoisers (gapdenoise.m tvm switch, its
+    # parameters) on the 2048 x 2048 x 24 stack, and a GAP solve with the
+    # MATLAB default ATV_ClipA
+    Hs, Ws, Bs = STACK
+    x = _dev.planar(sci.datasets.video_scene(Hs, Ws, Bs, seed=0), dev)
+    u = torch.empty_like(x)
+    tvs = {}
+    for name, (kind, param, iters) in sci.TVM.items():
+        wsm = sci.tv.tv_matlab_workspace(kind, Bs, Hs, Ws, iters, dev)
+        ms_t = ev_time(lambda: sci.tv_matlab_frames(x, kind, param(0.07), iters, u=u,
+                                                    workspace=wsm), 5)
+        tvs[name] = {"ms": ms_t, "gbs_8N": 8.0 * x.numel() / (ms_t * 1e-3) / 1e9}
+        del wsm
+    orig, mask, meas1 = sci.datasets.video_config(Hs, Ws, Bs, noise_rel=0.01)
+    del orig
+    op = sci.MaskOperator(mask)
+    y1 = _dev.plane(meas1, dev)
+    sol = sci.Solver(op, "gap", ITERS, 1.0, 0.07, tvm="ATV_ClipA")
+    ms_c = ev_time(lambda: sol.run(y1), 3, warm=1)
+    out["matlab_tv"] = {"workload": "tv_matlab_2048x2048x24", "per_denoiser": tvs,
+                        "gap_atv_clipa_iter_per_s": ITERS * 1e3 / ms_c}
+    del sol, op, x, u
+
+    # Bayer GAP-TV: a 2048 x 2048 mosaic of 24 frames (four 1024 x 1024 x 24
+    # sub-lattice problems), 60 iterations
+    yb = torch.from_numpy(meas1).float().to(dev)
+    mb = torch.from_numpy(mask).float().to(dev)
+    del mask
+    # one API call per solve: the sub-lattice split, mask packing and solver
+    # set-up are inside the timed region (direct launches, no graph capture)
+    ms_bay = ev_time(lambda: sci.gap_denoise_bayer(yb, mb, iter_max=ITERS, tv_weight=0.1,
+                                                   show_iqa=False, use_graph=False), 3, warm=1)
+    out["bayer"] = {"workload": "gap_tv_bayer_2048x2048x24", "iters": ITERS,
+                    "value": ITERS * 1e3 / ms_bay, "unit": "iter/s",
+                    "ms_per_call_incl_setup": ms_bay}
     return out
 
 

@@ -159,9 +159,10 @@ int sci_tv_chambolle_noalloc(const float *f, float *u, float *resid,
 #define SCI_TVM_ITV3D_CHAM 7  /* tvdenoise_cham_ITV3D.m (norm over frames) */
 #define SCI_TVM_ITV3D_FGP 8   /* fgp_denoise_ITV3D.m (norm over frames)    */
 
-/* Bytes of device workspace sci_tv_matlab needs. */
+/* Bytes of device workspace sci_tv_matlab needs for up to `iters`
+ * iterations. */
 int sci_tv_matlab_workspace_bytes(int kind, int64_t nframes, int64_t H,
-                                  int64_t W, size_t *bytes);
+                                  int64_t W, int iters, size_t *bytes);
 
 /* u = denoiser `kind`(f, lambda, iters) on the planar stack of nframes
  * H x W frames (H, W >= 2), with the file's own parameter: lambda is the

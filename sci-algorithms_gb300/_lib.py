@@ -70,7 +70,8 @@ _SIGS = {
                          c_vp, c_vp, c_vp, c_sz, c_vp],
     "sci_tv_chambolle_noalloc": [c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_f, c_f,
                                  ctypes.c_int, c_vp, c_vp],
-    "sci_tv_matlab_workspace_bytes": [ctypes.c_int, c_i64, c_i64, c_i64, ctypes.POINTER(c_sz)],
+    "sci_tv_matlab_workspace_bytes": [ctypes.c_int, c_i64, c_i64, c_i64, ctypes.c_int,
+                                      ctypes.POINTER(c_sz)],
     "sci_tv_matlab": [ctypes.c_int, c_vp, c_vp, c_i64, c_i64, c_i64, c_f, ctypes.c_int, c_vp,
                       c_sz, c_vp],
     "sci_sqerr_accum": [c_vp, c_vp, c_i64, c_vp, c_vp],

@@ -26,7 +26,7 @@ bool tv_proj_supported(int64_t nf, int64_t W, int K);
 int tvx_launch(int kind, const float *f, float *u, float *resid, int64_t nf, int64_t H,
                int64_t W, float lam, int iters, int *steps, void *ws, size_t ws_bytes,
                cudaStream_t s);
-size_t tvx_workspace_bytes(int kind, int64_t nf, int64_t H, int64_t W);
+size_t tvx_workspace_bytes(int kind, int64_t nf, int64_t H, int64_t W, int iters);
 
 namespace {
 
@@ -60,7 +60,8 @@ size_t solver_layout(bool admm, int64_t B, int64_t H, int64_t W, int K, int tvm,
         ob0 = take(sizeof(float) * n);
         ob1 = take(sizeof(float) * n);
     }
-    const size_t tvb = tvm ? tvx_workspace_bytes(tvm, B, H, W) : tv_workspace_bytes(B, H, W, K);
+    const size_t tvb =
+        tvm ? tvx_workspace_bytes(tvm, B, H, W, K) : tv_workspace_bytes(B, H, W, K);
     const size_t otv = take(tvb);
     if (w) {
         w->y1 = admm ? nullptr : reinterpret_cast<float *>(base + oy1);

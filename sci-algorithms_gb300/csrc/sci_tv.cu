@@ -106,16 +106,26 @@ static int choose_cpl(int64_t W) {
 // flags & 1: run all n_iter_max steps without the stop test (the unrolled,
 // differentiable form).  proj (nullable): apply the GAP projection
 // f = x + lam (c phi_b) while loading the input x (see tv_proj_supported).
-int tv_launch_impl(const float *f, float *u, float *resid, int64_t nf, int64_t H, int64_t W,
-                   int64_t fs, float weight, float eps, int K, int *steps, double *energy_out,
-                   void *workspace, size_t ws_bytes, cudaStream_t s, int force_R, int flags,
-                   const uint32_t *proj_bits, const float *proj_c, float proj_lam) {
-    const bool no_stop = (flags & 1) != 0;
+// Update rule of a pipeline run: RULE_SKIMAGE takes tau = 1/4 and
+// tau / weight; the MATLAB rules their own constants and run without the
+// stop test (see sci_tv.cuh).
+struct RuleArgs {
+    int rule = tv::RULE_SKIMAGE;
+    float tau = 0.f, tw = 0.f, c1 = 0.f, c2 = 0.f;
+};
+
+static int tv_launch_core(const float *f, float *u, float *resid, int64_t nf, int64_t H,
+                          int64_t W, int64_t fs, float weight, float eps, int K, int *steps,
+                          double *energy_out, void *workspace, size_t ws_bytes, cudaStream_t s,
+                          int force_R, int flags, const uint32_t *proj_bits, const float *proj_c,
+                          float proj_lam, const RuleArgs &ra) {
+    const bool no_stop = (flags & 1) != 0 || ra.rule != tv::RULE_SKIMAGE;
     const bool proj = proj_bits != nullptr;
     using namespace tv;
     SCI_CHECK_ARG(f && u && nf >= 1 && H >= 1 && W >= 1, "tv: bad arguments");
     SCI_CHECK_ARG(K >= 1, "tv: n_iter_max must be >= 1");
     SCI_CHECK_ARG(weight > 0.f, "tv: weight must be > 0 (got %g)", (double)weight);
+    SCI_CHECK_ARG(!proj || ra.rule == RULE_SKIMAGE, "tv: on-load projection needs the default rule");
     SCI_CHECK_ARG(f != u, "tv: input and output must not alias");
     SCI_CHECK_ARG(H <= (1 << 30) && W <= (1 << 30) && nf <= (1 << 30), "tv: sizes too large");
     const size_t need = ws_layout(nf, H, W, K, nullptr, nullptr);
@@ -169,8 +179,15 @@ int tv_launch_impl(const float *f, float *u, float *resid, int64_t nf, int64_t H
         P.W = (int)W;
         P.K = K;
         P.a = a;
-        P.tau = 0.25f;
-        P.tw = 0.25f / weight;
+        if (ra.rule == RULE_SKIMAGE) {
+            P.tau = 0.25f;
+            P.tw = 0.25f / weight;
+        } else {
+            P.tau = ra.tau;
+            P.tw = ra.tw;
+            P.c1 = ra.c1;
+            P.c2 = ra.c2;
+        }
         P.weight = weight;
         P.eps = eps;
         P.cpl = cpl;
@@ -190,7 +207,13 @@ int tv_launch_impl(const float *f, float *u, float *resid, int64_t nf, int64_t H
         P.vec = vec ? 1 : 0;
         const int per_frame_blocks = (P.nbands * P.nchunks + WPB - 1) / WPB;
         P.gpf = std::max(1, std::min(per_frame_blocks, 16));
-        if (proj) {
+        if (ra.rule == RULE_CHAM_ITV) {
+            launch_rule1(P, SG, PIN, FINAL, s);
+        } else if (ra.rule == RULE_CHAM_ATV) {
+            launch_rule2(P, SG, PIN, FINAL, s);
+        } else if (ra.rule == RULE_CLIP) {
+            launch_rule3(P, SG, PIN, FINAL, s);
+        } else if (proj) {
             launch_main_proj(P, SG, s);
         } else if (SG == SMAX) {
             if (lag == 2) launch_main4_lag2(P, PIN, FINAL, s);
@@ -211,6 +234,32 @@ int tv_launch_impl(const float *f, float *u, float *resid, int64_t nf, int64_t H
         pi ^= 1;
     }
     return SCI_OK;
+}
+
+int tv_launch_impl(const float *f, float *u, float *resid, int64_t nf, int64_t H, int64_t W,
+                   int64_t fs, float weight, float eps, int K, int *steps, double *energy_out,
+                   void *workspace, size_t ws_bytes, cudaStream_t s, int force_R, int flags,
+                   const uint32_t *proj_bits, const float *proj_c, float proj_lam) {
+    return tv_launch_core(f, u, resid, nf, H, W, fs, weight, eps, K, steps, energy_out,
+                          workspace, ws_bytes, s, force_R, flags, proj_bits, proj_c, proj_lam,
+                          RuleArgs{});
+}
+
+// A MATLAB-rule run of `updates` dual updates (rule, tau, tw, c1, c2 as in
+// sci_tv.cuh); the workspace is tv_workspace_bytes(nf, H, W, updates + 1).
+int tv_launch_rule(int rule, const float *f, float *u, float *resid, int64_t nf, int64_t H,
+                   int64_t W, int updates, float tau, float tw, float c1, float c2, int *steps,
+                   void *workspace, size_t ws_bytes, cudaStream_t s) {
+    SCI_CHECK_ARG(rule >= tv::RULE_CHAM_ITV && rule <= tv::RULE_CLIP && updates >= 0,
+                  "tv: bad rule arguments");
+    RuleArgs ra;
+    ra.rule = rule;
+    ra.tau = tau;
+    ra.tw = tw;
+    ra.c1 = c1;
+    ra.c2 = c2;
+    return tv_launch_core(f, u, resid, nf, H, W, H * W, 1.0f, 0.f, updates + 1, steps, nullptr,
+                          workspace, ws_bytes, s, 0, 1, nullptr, nullptr, 0.f, ra);
 }
 
 int tv_launch_flags(const float *f, float *u, float *resid, int64_t nf, int64_t H, int64_t W,

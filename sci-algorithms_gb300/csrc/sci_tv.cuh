@@ -81,7 +81,23 @@ struct Pass {
     const float *cmap;    // [H][W] (y1 - A x) / Phi_sum
     float lam;
     int frame_fast;       // work-item order: 1 = frames of one tile adjacent
+    // MATLAB-twin update rules (RULE != 0; no stop test): c1 is lambda of
+    // the anisotropic Chambolle projection (RULE_CHAM_ATV) or the clip
+    // bound (RULE_CLIP); c2 scales div p in u = f - c2 div p (RULE_CLIP)
+    float c1, c2;
 };
+
+// Dual update rules of the pipeline (the dual p is held as p / lambda for
+// the MATLAB Chambolle files, and as -z for the clip files):
+//   RULE_SKIMAGE   scikit-image: p' = (p - tau g) / (1 + tw |g|)
+//   RULE_CHAM_ITV  tvdenoise_cham_ITV2D.m: the same with tau = dt,
+//                  tw = dt lambda; div p takes no p at the first row /
+//                  column (MATLAB's il / iu index vectors)
+//   RULE_CHAM_ATV  tvdenoise_cham_ATV2D.m (stacks): t = p - tau g,
+//                  p' = t / max(1, lambda |t|) per component; same div
+//   RULE_CLIP      TV_denoising*.m: p' = clamp(p - tau g, -c1, c1) per
+//                  component (tau = 1/alpha), u = f - c2 div p
+enum { RULE_SKIMAGE = 0, RULE_CHAM_ITV = 1, RULE_CHAM_ATV = 2, RULE_CLIP = 3 };
 
 
 // ------------------------------------------------------------ lane vectors
@@ -215,11 +231,12 @@ struct Lane {
 
 // div p of a row: (pr - pr_up) + (pc - pc_left), with pc_left shifted in
 // from the lane on the left.
-template <int CPL>
+template <int CPL, int RULE = RULE_SKIMAGE>
 __device__ __forceinline__ Row<CPL> divergence(const Row<CPL> &prn, const Row<CPL> &pcn,
                                                const Row<CPL> &pru, bool first_col) {
     float pcl = __shfl_up_sync(FULL, hi(pcn.q[CPL / 2 - 1]), 1);
-    if (first_col) pcl = 0.f;
+    // column 0: scikit-image takes p_0, the MATLAB Chambolle files p_0 - p_0
+    if (first_col) pcl = (RULE == RULE_CHAM_ITV || RULE == RULE_CHAM_ATV) ? lo(pcn.q[0]) : 0.f;
     Row<CPL> d;
 #pragma unroll
     for (int j = 0; j < CPL / 2; ++j) {
@@ -231,7 +248,8 @@ __device__ __forceinline__ Row<CPL> divergence(const Row<CPL> &prn, const Row<CP
 
 // One pipeline step: input row r enters, stage k handles row r-k.
 // GEN: rows may be outside [r0, r1) or touch the frame's first/last row.
-template <int S, int CPL, bool PIN, bool OUT_U, bool ENERGY, int MODE, bool GEN, int PROJ>
+template <int S, int CPL, bool PIN, bool OUT_U, bool ENERGY, int MODE, bool GEN, int PROJ,
+          int RULE = RULE_SKIMAGE>
 __device__ __forceinline__ void step(const Pass &P, const St<S, CPL> &in, St<S, CPL> &out,
                                      int r, int rs, int r0, int r1, const Lane<CPL> &L,
                                      const float *fb, const float *pinb, float *ob, float *rb,
@@ -265,9 +283,13 @@ __device__ __forceinline__ void step(const Pass &P, const St<S, CPL> &in, St<S, 
     if (PIN) {
         const Row<CPL> qr = act0 ? in.nr : zrow<CPL>();
         const Row<CPL> qc = act0 ? in.nc : zrow<CPL>();
-        const Row<CPL> d = divergence<CPL>(qr, qc, in.pr[0], L.first_col);
+        // row 0 (MATLAB rules): no p from the row above, p_0 - p_0
+        const bool row0 = (RULE == RULE_CHAM_ITV || RULE == RULE_CHAM_ATV) && r == 0;
+        const Row<CPL> d = divergence<CPL, RULE>(qr, qc, row0 ? qr : in.pr[0], L.first_col);
 #pragma unroll
-        for (int j = 0; j < NQ; ++j) ucur.q[j] = sub2(fr.q[j], d.q[j]);
+        for (int j = 0; j < NQ; ++j)
+            ucur.q[j] = (RULE == RULE_CLIP) ? fma2(mk2(-P.c2, -P.c2), d.q[j], fr.q[j])
+                                            : sub2(fr.q[j], d.q[j]);
         if (ENERGY && act0 && (!GEN || (r >= r0 && r < r1))) {
 #pragma unroll
             for (int j = 0; j < NQ; ++j)
@@ -315,22 +337,40 @@ __device__ __forceinline__ void step(const Pass &P, const St<S, CPL> &in, St<S, 
             gc.q[j] = sub2(right, up.q[j]);
             if (MODE != INTERIOR) gc.q[j] = mul2(gc.q[j], L.gmask.q[j]);
             gr.q[j] = last_row ? mk2(0.f, 0.f) : sub2(ucur.q[j], up.q[j]);
-            const f2 s = fma2(gr.q[j], gr.q[j], mul2(gc.q[j], gc.q[j]));
-            n.q[j] = mk2(sqrt_approx(lo(s)), sqrt_approx(hi(s)));
-            const f2 den = fma2(tw2, n.q[j], one2);
-            ri.q[j] = mk2(rcp_approx(lo(den)), rcp_approx(hi(den)));
             const bool p0zero = (k == 1 && !PIN);
             const f2 qr = p0zero ? mk2(0.f, 0.f) : in.pr[k - 1].q[j];
             const f2 qc = p0zero ? mk2(0.f, 0.f) : in.pc[k - 1].q[j];
-            prn.q[j] = mul2(fma2(nt2, gr.q[j], qr), ri.q[j]);
-            pcn.q[j] = mul2(fma2(nt2, gc.q[j], qc), ri.q[j]);
+            if constexpr (RULE == RULE_SKIMAGE || RULE == RULE_CHAM_ITV) {
+                const f2 s = fma2(gr.q[j], gr.q[j], mul2(gc.q[j], gc.q[j]));
+                n.q[j] = mk2(sqrt_approx(lo(s)), sqrt_approx(hi(s)));
+                const f2 den = fma2(tw2, n.q[j], one2);
+                ri.q[j] = mk2(rcp_approx(lo(den)), rcp_approx(hi(den)));
+                prn.q[j] = mul2(fma2(nt2, gr.q[j], qr), ri.q[j]);
+                pcn.q[j] = mul2(fma2(nt2, gc.q[j], qc), ri.q[j]);
+            } else if constexpr (RULE == RULE_CHAM_ATV) {
+                const f2 tr = fma2(nt2, gr.q[j], qr), tc = fma2(nt2, gc.q[j], qc);
+                const float l = P.c1;
+                prn.q[j] = mk2(lo(tr) * rcp_approx(fmaxf(1.f, l * fabsf(lo(tr)))),
+                               hi(tr) * rcp_approx(fmaxf(1.f, l * fabsf(hi(tr)))));
+                pcn.q[j] = mk2(lo(tc) * rcp_approx(fmaxf(1.f, l * fabsf(lo(tc)))),
+                               hi(tc) * rcp_approx(fmaxf(1.f, l * fabsf(hi(tc)))));
+            } else {  // RULE_CLIP
+                const f2 tr = fma2(nt2, gr.q[j], qr), tc = fma2(nt2, gc.q[j], qc);
+                const float c = P.c1;
+                prn.q[j] = mk2(fminf(fmaxf(lo(tr), -c), c), fminf(fmaxf(hi(tr), -c), c));
+                pcn.q[j] = mk2(fminf(fmaxf(lo(tc), -c), c), fminf(fmaxf(hi(tc), -c), c));
+            }
         }
         out.pr[k] = prn;
         if (k < S) out.pc[k] = pcn;
-        const Row<CPL> d = divergence<CPL>(prn, pcn, in.pr[k], L.first_col);
+        // row 0 is also reached by fast steps (chunk 0, r = S)
+        const bool row0 = (RULE == RULE_CHAM_ITV || RULE == RULE_CHAM_ATV) && i == 0;
+        const Row<CPL> d = divergence<CPL, RULE>(prn, pcn, row0 ? prn : in.pr[k], L.first_col);
         Row<CPL> uk;
 #pragma unroll
-        for (int j = 0; j < NQ; ++j) uk.q[j] = sub2(fi.q[j], d.q[j]);
+        for (int j = 0; j < NQ; ++j)
+            uk.q[j] = (RULE == RULE_CLIP) ? fma2(mk2(-P.c2, -P.c2), d.q[j], fi.q[j])
+                                          : sub2(fi.q[j], d.q[j]);
         if (ENERGY && (!GEN || (i >= r0 && i < r1))) {
 #pragma unroll
             for (int j = 0; j < NQ; ++j) {
@@ -366,7 +406,8 @@ __device__ __forceinline__ void step(const Pass &P, const St<S, CPL> &in, St<S, 
     }
 }
 
-template <int S, int CPL, bool PIN, bool OUT_U, bool ENERGY, int MODE, int PROJ>
+template <int S, int CPL, bool PIN, bool OUT_U, bool ENERGY, int MODE, int PROJ,
+          int RULE = RULE_SKIMAGE>
 __device__ __forceinline__ void run(const Pass &P, int frame, int chunk, int band, int lane) {
     const int H = P.H, W = P.W;
     Lane<CPL> L;
@@ -413,16 +454,16 @@ __device__ __forceinline__ void run(const Pass &P, int frame, int chunk, int ban
     while (r <= rlast) {
         if (r == rfb && r + 1 <= rfe) {
             for (; r + 1 <= rfe; r += 2) {
-                step<S, CPL, PIN, OUT_U, ENERGY, MODE, false, PROJ>(P, A, B, r, rs, r0, r1, L, fb,
-                                                                     pinb, ob, rb, ek, frame);
-                step<S, CPL, PIN, OUT_U, ENERGY, MODE, false, PROJ>(P, B, A, r + 1, rs, r0, r1, L,
-                                                                     fb, pinb, ob, rb, ek, frame);
+                step<S, CPL, PIN, OUT_U, ENERGY, MODE, false, PROJ, RULE>(
+                    P, A, B, r, rs, r0, r1, L, fb, pinb, ob, rb, ek, frame);
+                step<S, CPL, PIN, OUT_U, ENERGY, MODE, false, PROJ, RULE>(
+                    P, B, A, r + 1, rs, r0, r1, L, fb, pinb, ob, rb, ek, frame);
             }
             continue;
         }
         // prologue (halo rows, first S steps) and epilogue (chunk tail, last row)
-        step<S, CPL, PIN, OUT_U, ENERGY, MODE, true, PROJ>(P, A, B, r, rs, r0, r1, L, fb, pinb, ob,
-                                                            rb, ek, frame);
+        step<S, CPL, PIN, OUT_U, ENERGY, MODE, true, PROJ, RULE>(P, A, B, r, rs, r0, r1, L, fb,
+                                                                  pinb, ob, rb, ek, frame);
         A = B;
         ++r;
     }
@@ -672,7 +713,8 @@ __device__ __forceinline__ void run2(const Pass &P, int frame, int chunk, int ba
     }
 }
 
-template <int S, int CPL, bool PIN, bool OUT_U, bool ENERGY, int LAG = 1, int PROJ = 0>
+template <int S, int CPL, bool PIN, bool OUT_U, bool ENERGY, int LAG = 1, int PROJ = 0,
+          int RULE = RULE_SKIMAGE>
 __device__ __forceinline__ void run_mode(const Pass &P, int frame, int chunk, int band, int lane) {
     const int c0 = band * P.own - P.hl;
     const bool interior = P.vec && c0 >= 0 && c0 + 32 * CPL - 1 <= P.W - 1;
@@ -680,8 +722,10 @@ __device__ __forceinline__ void run_mode(const Pass &P, int frame, int chunk, in
         if (interior) run2<S, CPL, PIN, OUT_U, ENERGY, INTERIOR>(P, frame, chunk, band, lane);
         else run2<S, CPL, PIN, OUT_U, ENERGY, EDGE>(P, frame, chunk, band, lane);
     } else {
-        if (interior) run<S, CPL, PIN, OUT_U, ENERGY, INTERIOR, PROJ>(P, frame, chunk, band, lane);
-        else run<S, CPL, PIN, OUT_U, ENERGY, EDGE, PROJ>(P, frame, chunk, band, lane);
+        if (interior)
+            run<S, CPL, PIN, OUT_U, ENERGY, INTERIOR, PROJ, RULE>(P, frame, chunk, band, lane);
+        else
+            run<S, CPL, PIN, OUT_U, ENERGY, EDGE, PROJ, RULE>(P, frame, chunk, band, lane);
     }
 }
 
@@ -732,12 +776,15 @@ template <int CPL>
 constexpr int min_blocks() { return CPL == 2 ? 4 : 3; }
 
 // Main launch of one pass: every frame not yet stopped runs all SG updates.
-template <int SG, bool PIN, bool FINAL, int CPL, int LAG = 1, int PROJ = 0>
+template <int SG, bool PIN, bool FINAL, int CPL, int LAG = 1, int PROJ = 0,
+          int RULE = RULE_SKIMAGE>
 __global__ void __launch_bounds__(WPB * 32, min_blocks<CPL>()) k_tv_main(Pass P) {
     int frame, chunk, band;
     if (!decode_item(P, frame, chunk, band)) return;
     if (PIN && P.done[frame] >= 0) return;  // stopped in an earlier pass
-    run_mode<SG, CPL, PIN, FINAL, true, LAG, PROJ>(P, frame, chunk, band, threadIdx.x & 31);
+    // the MATLAB rules have no stop test and need no energies
+    run_mode<SG, CPL, PIN, FINAL, RULE == RULE_SKIMAGE, LAG, PROJ, RULE>(P, frame, chunk, band,
+                                                                         threadIdx.x & 31);
 }
 
 // Stop-test launch of one pass over the same work items as the main launch:
@@ -779,6 +826,33 @@ void launch_main4_lag2(const Pass &P, bool pin, bool final_pass, cudaStream_t s)
 void launch_main_proj(const Pass &P, int SG, cudaStream_t s);
 void launch_fixup_proj(const Pass &P, cudaStream_t s);
 void launch_main123(const Pass &P, int SG, bool pin, cudaStream_t s);
+void launch_rule1(const Pass &P, int SG, bool pin, bool final_pass, cudaStream_t s);
+void launch_rule2(const Pass &P, int SG, bool pin, bool final_pass, cudaStream_t s);
+void launch_rule3(const Pass &P, int SG, bool pin, bool final_pass, cudaStream_t s);
+
+// Main kernels of one MATLAB-rule pass (4 columns per lane, no stop test).
+template <int RULE>
+void launch_rule_impl(const Pass &P, int SG, bool pin, bool final_pass, cudaStream_t s) {
+    const unsigned g = (unsigned)(((int64_t)P.nbands * P.nchunks * P.nf + WPB - 1) / WPB);
+    const unsigned T = WPB * 32;
+#define SCI_RULE_CASE(SGV)                                                            \
+    case SGV:                                                                         \
+        if (!pin && final_pass) k_tv_main<SGV, false, true, 4, 1, 0, RULE><<<g, T, 0, s>>>(P); \
+        else if (pin && final_pass) k_tv_main<SGV, true, true, 4, 1, 0, RULE><<<g, T, 0, s>>>(P); \
+        break;
+    switch (SG) {
+        SCI_RULE_CASE(1)
+        SCI_RULE_CASE(2)
+        SCI_RULE_CASE(3)
+        default:
+            if (!pin && final_pass) k_tv_main<4, false, true, 4, 1, 0, RULE><<<g, T, 0, s>>>(P);
+            else if (!pin) k_tv_main<4, false, false, 4, 1, 0, RULE><<<g, T, 0, s>>>(P);
+            else if (final_pass) k_tv_main<4, true, true, 4, 1, 0, RULE><<<g, T, 0, s>>>(P);
+            else k_tv_main<4, true, false, 4, 1, 0, RULE><<<g, T, 0, s>>>(P);
+            break;
+    }
+#undef SCI_RULE_CASE
+}
 void launch_fixup(const Pass &P, bool pin, cudaStream_t s);
 
 inline unsigned pass_blocks(const Pass &P) {

@@ -14,19 +14,31 @@
 // branch for it: ClipB then runs ClipA's update and ATV_cham the isotropic
 // per-frame update.  The host maps those cases to kinds 1 and 5.
 //
-// Design: one kernel per iteration over the whole stack, one thread per
-// pixel (kinds 7 and 8: one thread per pixel position, looping over the
-// frames for the coupled norm).  A thread recomputes the few primal values
-// its dual update needs from the neighbouring duals (served by L1), so an
-// iteration reads the input and the duals once and writes the duals once.
-// The last dual update of the FGP loop and of the clip loops does not reach
-// the returned value and is not computed.
+// Design.  The clip files and the per-frame Chambolle files are the same
+// shape of recurrence as the scikit-image TV (u = f - c div p, a dual
+// update from the forward differences of u), so kinds 1, 2, 3 and 5 run on
+// the temporally blocked TV pipeline (sci_tv.cuh, RULE_CLIP /
+// RULE_CHAM_ATV / RULE_CHAM_ITV): the stack crosses HBM once per 4 dual
+// updates.  The FGP files (two dual fields and a momentum) and ITV3D_cham
+// (a norm summed over all frames of a pixel) run one kernel per iteration
+// over the stack, one thread per pixel (kinds 7 and 8: per pixel position,
+// looping over the frames); a thread recomputes the few primal values its
+// dual update needs from the neighbouring duals (served by L1).  The last
+// dual update of the FGP loop does not reach the returned value and is not
+// computed.
 #include <cmath>
 #include <utility>
 
 #include "sci_common.cuh"
+#include "sci_tv.cuh"
 
 namespace sci {
+
+int tv_launch_rule(int rule, const float *f, float *u, float *resid, int64_t nf, int64_t H,
+                   int64_t W, int updates, float tau, float tw, float c1, float c2, int *steps,
+                   void *workspace, size_t ws_bytes, cudaStream_t s);
+size_t tv_workspace_bytes(int64_t nf, int64_t H, int64_t W, int K);
+
 namespace tvx {
 
 enum Kind {
@@ -38,61 +50,6 @@ struct Geo {
     int H, W;
     int64_t hw;
 };
-
-__device__ __forceinline__ float clipv(float v, float c) {
-    // sign(v) .* min(|v|, c)
-    return v > 0.f ? fminf(v, c) : (v < 0.f ? -fminf(-v, c) : 0.f);
-}
-
-// ------------------------------------------------------------ clip family
-// x0 at (i, j) from y0 and the duals zh (valid j <= W-2), zv (i <= H-2):
-// dht(zh)_j = -zh_0 (j = 0), -(zh_j - zh_{j-1}), zh_{W-2} (j = W-1).
-template <int KIND>
-__device__ __forceinline__ float clip_x0(const float *f, const float *zh, const float *zv,
-                                         const Geo &g, int i, int j) {
-    const int64_t p = (int64_t)i * g.W + j;
-    const float dht = (j == 0) ? -zh[p] : (j == g.W - 1 ? zh[p - 1] : -(zh[p] - zh[p - 1]));
-    const float dvt = (i == 0) ? -zv[p] : (i == g.H - 1 ? zv[p - g.W] : -(zv[p] - zv[p - g.W]));
-    const float y0 = f[p];
-    if (KIND == CLIP_A) return ((y0 - dht) + (y0 - dvt)) * 0.5f;  // (x0h + x0v)./2
-    return (y0 - dht) - dvt;
-}
-
-template <int KIND>
-__global__ void k_clip_update(const float *__restrict__ f, const float *__restrict__ zh,
-                              const float *__restrict__ zv, float *__restrict__ zh2,
-                              float *__restrict__ zv2, Geo g, float bound) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i >= g.H || j >= g.W) return;
-    const int64_t fo = (int64_t)blockIdx.z * g.hw;
-    f += fo, zh += fo, zv += fo, zh2 += fo, zv2 += fo;
-    const float x = clip_x0<KIND>(f, zh, zv, g, i, j);
-    const int64_t p = (int64_t)i * g.W + j;
-    const float ia = 1.f / 5.f;  // 1/alpha
-    if (j < g.W - 1) {
-        const float xr = clip_x0<KIND>(f, zh, zv, g, i, j + 1);
-        zh2[p] = clipv(zh[p] + ia * (xr - x), bound);
-    }
-    if (i < g.H - 1) {
-        const float xd = clip_x0<KIND>(f, zh, zv, g, i + 1, j);
-        zv2[p] = clipv(zv[p] + ia * (xd - x), bound);
-    }
-}
-
-template <int KIND>
-__global__ void k_clip_out(const float *__restrict__ f, const float *__restrict__ zh,
-                           const float *__restrict__ zv, float *__restrict__ u,
-                           float *__restrict__ resid, Geo g) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i >= g.H || j >= g.W) return;
-    const int64_t fo = (int64_t)blockIdx.z * g.hw;
-    const int64_t p = (int64_t)i * g.W + j;
-    const float x = clip_x0<KIND>(f + fo, zh + fo, zv + fo, g, i, j);
-    u[fo + p] = x;
-    if (resid) resid[fo + p] = x - f[fo + p];
-}
 
 // -------------------------------------------------------- Chambolle family
 // divp = p1 - p1(:,il) + p2 - p2(iu,:): no p at the first column / row.
@@ -119,55 +76,53 @@ __device__ __forceinline__ void cham_grad(const float *f, const float *p1, const
     z2 = (i < g.H - 1) ? zat(i + 1, j, p + g.W) - z : 0.f;
 }
 
-template <int KIND>
-__global__ void k_cham_update(const float *__restrict__ f, const float *__restrict__ p1,
-                              const float *__restrict__ p2, float *__restrict__ q1,
-                              float *__restrict__ q2, Geo g, float lam, float dt, int first) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i >= g.H || j >= g.W) return;
-    const int64_t fo = (int64_t)blockIdx.z * g.hw;
-    f += fo, p1 += fo, p2 += fo, q1 += fo, q2 += fo;
-    const int64_t p = (int64_t)i * g.W + j;
-    float z1, z2;
-    cham_grad(f, p1, p2, g, i, j, lam, first != 0, z1, z2);
-    const float a = first ? 0.f : p1[p], b = first ? 0.f : p2[p];
-    if (KIND == CHAM_ATV) {
-        const float t1 = a + dt * z1, t2 = b + dt * z2;
-        q1[p] = t1 / fmaxf(1.f, fabsf(t1));
-        q2[p] = t2 / fmaxf(1.f, fabsf(t2));
-    } else {
-        const float denom = 1.f + dt * sqrtf(z1 * z1 + z2 * z2);
-        q1[p] = (a + dt * z1) / denom;
-        q2[p] = (b + dt * z2) / denom;
-    }
+// Frame-coupled kernels (ITV3D): a block covers 32 pixels of one row with
+// FL frame lanes (threadIdx.y); lane l handles frames l, l+FL, ... (at most
+// FMAX per lane, kept in registers), the per-pixel sum over frames is
+// reduced in shared memory in a fixed order, then every lane updates its
+// frames.
+constexpr int FL = 8, FMAX = 4;  // frame lanes; frames per lane (nf <= 32)
+
+__device__ __forceinline__ float lane_reduce(float v, float (*red)[32]) {
+    red[threadIdx.y][threadIdx.x] = v;
+    __syncthreads();
+    float s = 0.f;
+#pragma unroll
+    for (int l = 0; l < FL; ++l) s += red[l][threadIdx.x];
+    __syncthreads();
+    return s;
 }
 
-// ITV3D: denom = 1 + dt sqrt(sum over frames of z1^2 + z2^2), one thread
-// per pixel position.
-__global__ void k_cham_update_coupled(const float *__restrict__ f, const float *__restrict__ p1,
-                                      const float *__restrict__ p2, float *__restrict__ q1,
-                                      float *__restrict__ q2, Geo g, int nf, float lam, float dt,
-                                      int first) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i >= g.H || j >= g.W) return;
+// ITV3D: denom = 1 + dt sqrt(sum over frames of z1^2 + z2^2).
+__global__ void __launch_bounds__(32 * FL) k_cham_update_coupled(
+    const float *__restrict__ f, const float *__restrict__ p1, const float *__restrict__ p2,
+    float *__restrict__ q1, float *__restrict__ q2, Geo g, int nf, float lam, float dt,
+    int first) {
+    __shared__ float red[FL][32];
+    const int j = blockIdx.x * 32 + threadIdx.x, i = blockIdx.y;
+    const bool in = j < g.W;
     const int64_t p = (int64_t)i * g.W + j;
-    float s = 0.f;
-    for (int b = 0; b < nf; ++b) {
-        const int64_t fo = (int64_t)b * g.hw;
-        float z1, z2;
-        cham_grad(f + fo, p1 + fo, p2 + fo, g, i, j, lam, first != 0, z1, z2);
-        s += z1 * z1 + z2 * z2;
+    float z1[FMAX], z2[FMAX], s = 0.f;
+#pragma unroll
+    for (int t = 0; t < FMAX; ++t) {
+        const int b = threadIdx.y + t * FL;
+        z1[t] = z2[t] = 0.f;
+        if (in && b < nf) {
+            const int64_t fo = (int64_t)b * g.hw;
+            cham_grad(f + fo, p1 + fo, p2 + fo, g, i, j, lam, first != 0, z1[t], z2[t]);
+            s += z1[t] * z1[t] + z2[t] * z2[t];
+        }
     }
-    const float denom = 1.f + dt * sqrtf(s);
-    for (int b = 0; b < nf; ++b) {
-        const int64_t fo = (int64_t)b * g.hw;
-        float z1, z2;
-        cham_grad(f + fo, p1 + fo, p2 + fo, g, i, j, lam, first != 0, z1, z2);
-        const float a = first ? 0.f : p1[fo + p], c = first ? 0.f : p2[fo + p];
-        q1[fo + p] = (a + dt * z1) / denom;
-        q2[fo + p] = (c + dt * z2) / denom;
+    const float denom = 1.f + dt * sqrtf(lane_reduce(s, red));
+#pragma unroll
+    for (int t = 0; t < FMAX; ++t) {
+        const int b = threadIdx.y + t * FL;
+        if (in && b < nf) {
+            const int64_t q = (int64_t)b * g.hw + p;
+            const float a = first ? 0.f : p1[q], c = first ? 0.f : p2[q];
+            q1[q] = (a + dt * z1[t]) / denom;
+            q2[q] = (c + dt * z2[t]) / denom;
+        }
     }
 }
 
@@ -240,34 +195,38 @@ __global__ void k_fgp_update(const float *__restrict__ xo, float *__restrict__ P
     s2[p] = b + mom * (b - o2);
 }
 
-__global__ void k_fgp_update_coupled(const float *__restrict__ xo, float *__restrict__ P1,
-                                     float *__restrict__ P2, const float *__restrict__ r1,
-                                     const float *__restrict__ r2, float *__restrict__ s1,
-                                     float *__restrict__ s2, Geo g, int nf, float lam, float c,
-                                     float mom, int first) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i >= g.H || j >= g.W) return;
+__global__ void __launch_bounds__(32 * FL) k_fgp_update_coupled(
+    const float *__restrict__ xo, float *__restrict__ P1, float *__restrict__ P2,
+    const float *__restrict__ r1, const float *__restrict__ r2, float *__restrict__ s1,
+    float *__restrict__ s2, Geo g, int nf, float lam, float c, float mom, int first) {
+    __shared__ float red[FL][32];
+    const int j = blockIdx.x * 32 + threadIdx.x, i = blockIdx.y;
+    const bool in = j < g.W;
     const int64_t p = (int64_t)i * g.W + j;
-    float s = 0.f;
-    for (int b = 0; b < nf; ++b) {
-        const int64_t fo = (int64_t)b * g.hw;
-        float a, c2;
-        fgp_step(xo + fo, r1 + fo, r2 + fo, g, i, j, lam, c, first != 0, a, c2);
-        s += a * a + c2 * c2;
+    float a[FMAX], b2[FMAX], s = 0.f;
+#pragma unroll
+    for (int t = 0; t < FMAX; ++t) {
+        const int b = threadIdx.y + t * FL;
+        a[t] = b2[t] = 0.f;
+        if (in && b < nf) {
+            const int64_t fo = (int64_t)b * g.hw;
+            fgp_step(xo + fo, r1 + fo, r2 + fo, g, i, j, lam, c, first != 0, a[t], b2[t]);
+            s += a[t] * a[t] + b2[t] * b2[t];
+        }
     }
-    const float A = sqrtf(fmaxf(s, 1.f));
-    for (int b = 0; b < nf; ++b) {
-        const int64_t fo = (int64_t)b * g.hw;
-        float a, c2;
-        fgp_step(xo + fo, r1 + fo, r2 + fo, g, i, j, lam, c, first != 0, a, c2);
-        a = a / A;
-        c2 = c2 / A;
-        const float o1 = first ? 0.f : P1[fo + p], o2 = first ? 0.f : P2[fo + p];
-        P1[fo + p] = a;
-        P2[fo + p] = c2;
-        s1[fo + p] = a + mom * (a - o1);
-        s2[fo + p] = c2 + mom * (c2 - o2);
+    const float A = sqrtf(fmaxf(lane_reduce(s, red), 1.f));
+#pragma unroll
+    for (int t = 0; t < FMAX; ++t) {
+        const int b = threadIdx.y + t * FL;
+        if (in && b < nf) {
+            const int64_t q = (int64_t)b * g.hw + p;
+            const float u1 = a[t] / A, u2 = b2[t] / A;
+            const float o1 = first ? 0.f : P1[q], o2 = first ? 0.f : P2[q];
+            P1[q] = u1;
+            P2[q] = u2;
+            s1[q] = u1 + mom * (u1 - o1);
+            s2[q] = u2 + mom * (u2 - o2);
+        }
     }
 }
 
@@ -289,17 +248,21 @@ __global__ void k_fill(int *a, int v, int n) {
     if (i < n) a[i] = v;
 }
 
-int planes(int kind) {
-    switch (kind) {
-        case FGP_ATV: case FGP_ITV2D: case FGP_ITV3D: return 6;
-        default: return 4;
-    }
+// Kinds run on the TV pipeline, and its update rule.
+bool on_pipeline(int kind) {
+    return kind == CLIP_A || kind == CLIP_B || kind == CHAM_ATV || kind == CHAM_ITV2D;
 }
 
 }  // namespace tvx
 
-size_t tvx_workspace_bytes(int kind, int64_t nf, int64_t H, int64_t W) {
-    return sizeof(float) * (size_t)tvx::planes(kind) * (size_t)(nf * H * W);
+// Workspace of kind `kind` run with at most `iters` iterations (the
+// pipeline kinds carry p through the workspace when they need more than 4
+// dual updates).
+size_t tvx_workspace_bytes(int kind, int64_t nf, int64_t H, int64_t W, int iters) {
+    using namespace tvx;
+    if (on_pipeline(kind)) return tv_workspace_bytes(nf, H, W, iters + 1);
+    const int planes = (kind == FGP_ATV || kind == FGP_ITV2D || kind == FGP_ITV3D) ? 6 : 4;
+    return sizeof(float) * (size_t)planes * (size_t)(nf * H * W);
 }
 
 // kind 1..8 as above; lambda and iters are the denoiser's own parameters
@@ -311,9 +274,11 @@ int tvx_launch(int kind, const float *f, float *u, float *resid, int64_t nf, int
     SCI_CHECK_ARG(kind >= CLIP_A && kind <= FGP_ITV3D, "tv_matlab: unknown kind %d", kind);
     SCI_CHECK_ARG(f && u && f != u && nf >= 1 && H >= 2 && W >= 2 && iters >= 1,
                   "tv_matlab: bad arguments (H, W >= 2, iters >= 1, f != u)");
-    SCI_CHECK_ARG(nf <= 65535 && H <= (1 << 24) && W <= (1 << 24), "tv_matlab: sizes too large");
+    SCI_CHECK_ARG(nf <= 65535 && H <= 65535 && W <= (1 << 24), "tv_matlab: sizes too large");
+    SCI_CHECK_ARG(nf <= FL * FMAX || (kind != CHAM_ITV3D && kind != FGP_ITV3D),
+                  "tv_matlab: the ITV3D kinds take at most %d frames", FL * FMAX);
     SCI_CHECK_ARG(lam > 0.f, "tv_matlab: lambda must be > 0");
-    const size_t need = tvx_workspace_bytes(kind, nf, H, W);
+    const size_t need = tvx_workspace_bytes(kind, nf, H, W, iters);
     SCI_CHECK_ARG(ws && ws_bytes >= need, "tv_matlab: workspace of %zu bytes needed, got %zu",
                   need, ws_bytes);
     // one frame: MATLAB's 2-D branches
@@ -323,7 +288,9 @@ int tvx_launch(int kind, const float *f, float *u, float *resid, int64_t nf, int
     Geo g{(int)H, (int)W, hw};
     const dim3 blk(32, 8);
     const dim3 grd((unsigned)((W + 31) / 32), (unsigned)((H + 7) / 8), (unsigned)nf);
-    const dim3 grd1((unsigned)((W + 31) / 32), (unsigned)((H + 7) / 8), 1);
+    // frame-coupled kernels: 32 pixels x FL frame lanes per block, one row
+    const dim3 blkc(32, FL);
+    const dim3 grdc((unsigned)((W + 31) / 32), (unsigned)H, 1);
     float *w0 = static_cast<float *>(ws);
     float *a1 = w0, *a2 = w0 + n, *b1 = w0 + 2 * n, *b2 = w0 + 3 * n;
     if (steps) {
@@ -332,43 +299,28 @@ int tvx_launch(int kind, const float *f, float *u, float *resid, int64_t nf, int
     }
     switch (kind) {
         case CLIP_A:
-        case CLIP_B: {
-            // TV_denoising.m:23-33 / TV_denoising_clip_LB.m:23-34
-            const float bound = kind == CLIP_A ? lam / 2 : lam;
-            SCI_CUDA(cudaMemsetAsync(a1, 0, sizeof(float) * 2 * n, s));
-            float *zh = a1, *zv = a2, *zh2 = b1, *zv2 = b2;
-            for (int it = 0; it + 1 < iters; ++it) {
-                if (kind == CLIP_A)
-                    k_clip_update<CLIP_A><<<grd, blk, 0, s>>>(f, zh, zv, zh2, zv2, g, bound);
-                else
-                    k_clip_update<CLIP_B><<<grd, blk, 0, s>>>(f, zh, zv, zh2, zv2, g, bound);
-                SCI_LAUNCHED("k_clip_update");
-                std::swap(zh, zh2);
-                std::swap(zv, zv2);
-            }
-            if (kind == CLIP_A) k_clip_out<CLIP_A><<<grd, blk, 0, s>>>(f, zh, zv, u, resid, g);
-            else k_clip_out<CLIP_B><<<grd, blk, 0, s>>>(f, zh, zv, u, resid, g);
-            SCI_LAUNCHED("k_clip_out");
-            return SCI_OK;
-        }
-        case CHAM_ATV:
+        case CLIP_B:
+            // TV_denoising.m:23-33 / TV_denoising_clip_LB.m:23-34: x0 of the
+            // last iteration sees iters-1 dual updates; 1/alpha = 1/5
+            return tv_launch_rule(tv::RULE_CLIP, f, u, resid, nf, H, W, iters - 1, 0.2f, 0.f,
+                                  kind == CLIP_A ? lam / 2 : lam, kind == CLIP_A ? 0.5f : 1.f,
+                                  nullptr, ws, ws_bytes, s);
         case CHAM_ITV2D:
+            // tvdenoise_cham_ITV2D.m:62-93: every iteration's update is live
+            return tv_launch_rule(tv::RULE_CHAM_ITV, f, u, resid, nf, H, W, iters, 0.125f,
+                                  0.125f * lam, 0.f, 0.f, nullptr, ws, ws_bytes, s);
+        case CHAM_ATV:
+            // tvdenoise_cham_ATV2D.m:72-88
+            return tv_launch_rule(tv::RULE_CHAM_ATV, f, u, resid, nf, H, W, iters, 0.125f, 0.f,
+                                  lam, 0.f, nullptr, ws, ws_bytes, s);
         case CHAM_ITV3D: {
-            // tvdenoise_cham_*.m:62-93
-            const float dt = kind == CHAM_ITV3D ? 0.25f : 0.125f;
+            // tvdenoise_cham_ITV3D.m:74-91
+            const float dt = 0.25f;
             float *p1 = a1, *p2 = a2, *q1 = b1, *q2 = b2;
             for (int it = 0; it < iters; ++it) {
-                const int first = it == 0;
-                if (kind == CHAM_ITV3D)
-                    k_cham_update_coupled<<<grd1, blk, 0, s>>>(f, p1, p2, q1, q2, g, (int)nf, lam,
-                                                               dt, first);
-                else if (kind == CHAM_ATV)
-                    k_cham_update<CHAM_ATV><<<grd, blk, 0, s>>>(f, p1, p2, q1, q2, g, lam, dt,
-                                                                first);
-                else
-                    k_cham_update<CHAM_ITV2D><<<grd, blk, 0, s>>>(f, p1, p2, q1, q2, g, lam, dt,
-                                                                  first);
-                SCI_LAUNCHED("k_cham_update");
+                k_cham_update_coupled<<<grdc, blkc, 0, s>>>(f, p1, p2, q1, q2, g, (int)nf, lam,
+                                                            dt, it == 0);
+                SCI_LAUNCHED("k_cham_update_coupled");
                 std::swap(p1, q1);
                 std::swap(p2, q2);
             }
@@ -388,8 +340,8 @@ int tvx_launch(int kind, const float *f, float *u, float *resid, int64_t nf, int
                 const float mom = (float)((tk - 1.0) / tkp1);
                 const int first = it == 0;
                 if (kind == FGP_ITV3D)
-                    k_fgp_update_coupled<<<grd1, blk, 0, s>>>(f, P1, P2, r1, r2, s1, s2, g,
-                                                              (int)nf, lam, c, mom, first);
+                    k_fgp_update_coupled<<<grdc, blkc, 0, s>>>(f, P1, P2, r1, r2, s1, s2, g,
+                                                               (int)nf, lam, c, mom, first);
                 else if (kind == FGP_ATV)
                     k_fgp_update<FGP_ATV><<<grd, blk, 0, s>>>(f, P1, P2, r1, r2, s1, s2, g, lam,
                                                               c, mom, first);
@@ -412,11 +364,12 @@ int tvx_launch(int kind, const float *f, float *u, float *resid, int64_t nf, int
 
 extern "C" {
 
-int sci_tv_matlab_workspace_bytes(int kind, int64_t nframes, int64_t H, int64_t W,
+int sci_tv_matlab_workspace_bytes(int kind, int64_t nframes, int64_t H, int64_t W, int iters,
                                   size_t *bytes) {
-    SCI_CHECK_ARG(bytes && kind >= 1 && kind <= 8 && nframes >= 1 && H >= 1 && W >= 1,
+    SCI_CHECK_ARG(bytes && kind >= 1 && kind <= 8 && nframes >= 1 && H >= 1 && W >= 1 &&
+                      iters >= 1,
                   "sci_tv_matlab_workspace_bytes: bad argument");
-    *bytes = sci::tvx_workspace_bytes(kind, nframes, H, W);
+    *bytes = sci::tvx_workspace_bytes(kind, nframes, H, W, iters);
     return SCI_OK;
 }
 

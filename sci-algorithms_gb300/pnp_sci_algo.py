@@ -105,8 +105,8 @@ def _solve_plugin(projmeth, y, ps, A, At, iters, _lambda, tv_weight, tv_iter_max
     x = adj(y) if x0 is None else _dev.planar(x0)
     B, H, W = x.shape
     if kind:
-        ws = tv_matlab_workspace(kind, B, H, W, x.device)
         _, param, tv_iters = TVM[tvm]
+        ws = tv_matlab_workspace(kind, B, H, W, tv_iters, x.device)
 
     def denoise(v, k):
         if kind:

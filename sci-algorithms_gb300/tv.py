@@ -92,9 +92,9 @@ def tvm_kind(tvm):
     return TVM[tvm][0]
 
 
-def tv_matlab_workspace(kind, nframes, H, W, dev=None):
+def tv_matlab_workspace(kind, nframes, H, W, iters, dev=None):
     n = ctypes.c_size_t()
-    call("sci_tv_matlab_workspace_bytes", int(kind), nframes, H, W, ctypes.byref(n))
+    call("sci_tv_matlab_workspace_bytes", int(kind), nframes, H, W, int(iters), ctypes.byref(n))
     return _dev.workspace(n.value, dev)
 
 
@@ -108,7 +108,7 @@ def tv_matlab_frames(f, tvm, lam, iters, u=None, workspace=None):
     if u is None:
         u = torch.empty_like(f)
     if workspace is None:
-        workspace = tv_matlab_workspace(kind, nf, H, W, f.device)
+        workspace = tv_matlab_workspace(kind, nf, H, W, iters, f.device)
     call("sci_tv_matlab", kind, f.data_ptr(), u.data_ptr(), nf, H, W, float(lam), int(iters),
          workspace.data_ptr(), workspace.numel(), _dev.stream_handle())
     return u

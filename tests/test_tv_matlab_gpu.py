@@ -138,3 +138,20 @@ def test_cacti_driver_with_matlab_tv_and_steps():
     s = sci.Solver(op, "gap", 4, 1.0, 0.07, tvm="ITV2D_FGP")
     s.run(_dev.plane(meas), tv_steps=True)
     assert torch.all(s.tv_steps == 2)
+
+
+@pytest.mark.parametrize("tvm,lam", [("ATV_ClipA", 0.1), ("ATV_ClipB", 0.05),
+                                     ("ATV_cham", 12.0), ("ITV2D_cham", 12.0)])
+@pytest.mark.parametrize("iters", [1, 2, 5, 6, 9])
+@pytest.mark.parametrize("H,W,B", [(70, 130, 3), (300, 517, 2)])
+def test_pipeline_kinds_any_iteration_count(tvm, lam, iters, H, W, B):
+    """The clip and per-frame Chambolle files on the temporally blocked
+    pipeline: one pass (<= 4 dual updates), several passes carrying p
+    through the workspace, and the copy for no update; odd widths use the
+    scalar edge path."""
+    f = frames(H, W, B, seed=iters + W)
+    kind = sci.TVM[tvm][0]
+    ref = tm._FN[tm.TVM[tvm][0]](f, lam, iters)
+    u = sci.tv_matlab_frames(_dev.planar(f), kind, lam, iters)
+    torch.cuda.synchronize()
+    assert np.max(np.abs(_dev.unplanar(u, f) - ref)) < ATOL, (tvm, iters)
