@@ -74,11 +74,13 @@ __device__ __forceinline__ f2 mk2(float a, float b) {
 __device__ __forceinline__ float lo(f2 a) {
     float x, y;
     asm("mov.b64 {%0,%1}, %2;" : "=f"(x), "=f"(y) : "l"(a.v));
+    (void)y;
     return x;
 }
 __device__ __forceinline__ float hi(f2 a) {
     float x, y;
     asm("mov.b64 {%0,%1}, %2;" : "=f"(x), "=f"(y) : "l"(a.v));
+    (void)x;
     return y;
 }
 __device__ __forceinline__ f2 add2(f2 a, f2 b) {
