@@ -308,6 +308,33 @@ def run_gpu(args):
         torch.distributed.destroy_process_group()
 
 
+def run_unrolled(args):
+    """Profiling mode: `launches` forward + backward passes of the unrolled
+    GAP-TV workload (16 x 256 x 256 x 8, K = 20)."""
+    import torch
+    import sci_algorithms_gb300 as sci
+    from sci_algorithms_gb300.unrolled import unrolled_loss
+    dev = torch.device("cuda")
+    N, Bu, Hu, Wu, K = 16, 8, 256, 256, 20
+    xs = [sci.datasets.video_scene(Hu, Wu, Bu, seed=n) for n in range(N)]
+    xt = torch.from_numpy(np.stack([np.moveaxis(x, -1, 0) for x in xs])).float().to(dev)
+    g = torch.Generator().manual_seed(0)
+    logits0 = torch.randn((Bu, Hu, Wu), generator=g).to(dev)
+    lam0 = torch.full((K,), 0.1, device=dev)
+    ws = sci.unrolled_workspace(N, Bu, Hu, Wu, K, 5, dev)
+    s = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(args.launches):
+        lg = logits0.clone().requires_grad_(True)
+        lm = lam0.clone().requires_grad_(True)
+        unrolled_loss(lg, lm, xt, K=K, ws=ws).backward()
+    e1.record(s)
+    torch.cuda.synchronize()
+    print(json.dumps({"kernel": "unrolled", "workload": "unrolled_gaptv_16x256x256x8_K20",
+                      "ms_per_fwd_bwd": e0.elapsed_time(e1) / args.launches}))
+
+
 def run_kernel(args):
     """Single-kernel mode for profiling: a few launches of one kernel on a
     2048 x 2048 x F stack (small enough for an ncu capture)."""
@@ -315,6 +342,8 @@ def run_kernel(args):
     import sci_algorithms_gb300 as sci
     from sci_algorithms_gb300 import _dev
     from sci_algorithms_gb300._lib import call
+    if args.kernel == "unrolled":
+        return run_unrolled(args)
     dev = _dev.device()
     F = args.frames
     orig, mask, meas = sci.datasets.video_config(H, W, F, noise_rel=0.01)
@@ -335,7 +364,14 @@ def run_kernel(args):
              y1.data_ptr(), op.phisum.data_ptr(), out.data_ptr(), 1.0, 1, F, H, W,
              s.cuda_stream)
 
-    fn = {"tv": tv_once, "proj": proj_once}[args.kernel]
+    bplanes = torch.zeros_like(x) if args.kernel == "proj_admm" else None
+
+    def proj_admm_once():
+        call("sci_proj_admm", x.data_ptr(), bplanes.data_ptr(), None, op.bits.data_ptr(),
+             y.data_ptr(), op.phisum.data_ptr(), out.data_ptr(), None, 1.0, 0.01, F, H, W,
+             s.cuda_stream)
+
+    fn = {"tv": tv_once, "proj": proj_once, "proj_admm": proj_admm_once}[args.kernel]
     fn()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -475,7 +511,7 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the spectral and differentiable side workloads")
-    ap.add_argument("--kernel", choices=["tv", "proj"], default=None,
+    ap.add_argument("--kernel", choices=["tv", "proj", "proj_admm", "unrolled"], default=None,
                     help="profiling mode: time one kernel on a 2048x2048xFRAMES stack")
     ap.add_argument("--frames", type=int, default=8)
     ap.add_argument("--launches", type=int, default=3)

@@ -12,6 +12,7 @@
 // captured once into a CUDA graph and replayed.  An autotuner times the TV
 // row-chunk height per distinct frame shape on the item's own data.
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
 #include <list>
 #include <map>
@@ -20,9 +21,13 @@
 #include <tuple>
 #include <vector>
 
+#include "sci_bulk.cuh"
 #include "sci_tv.cuh"
 
 namespace sci {
+
+// bit 0: a bounded bulk-copy wait of the batched projection gave up
+__device__ unsigned int g_batch_status;
 
 int tv_launch(const float *f, float *u, float *resid, int64_t nf, int64_t H, int64_t W,
               int64_t fs, float weight, float eps, int K, int *steps, double *energy_out,
@@ -108,6 +113,81 @@ __global__ void __launch_bounds__(PROJ_T) k_batch_proj(const Table *__restrict__
         const float m = ((w >> b) & 1u) ? 1.f : 0.f;
         __stcs(I.xp + b * hw + p, fmaf(I.lam, r * m, xs[b * PROJ_T + t]));
     }
+}
+
+// The same projection with the tile's B rows of 256 floats staged by bulk
+// copies (one mbarrier, 64 threads x 4 pixels); the default for items whose
+// planes are 16-byte aligned with hw % 4 == 0 (all items of a batch, see
+// check()).  Same arithmetic, bit-identical results.
+template <bool ACC>
+__global__ void __launch_bounds__(PROJ_T / 4) k_batch_proj_tma(const Table *__restrict__ T) {
+    extern __shared__ __align__(128) float xs[];  // [B][PROJ_T]
+    __shared__ __align__(8) uint64_t bar;
+    const int g = blockIdx.x;
+    if (g >= T->proj_prefix[T->n]) return;
+    const int i = find_item(T->proj_prefix, T->n, g);
+    const Item &I = T->it[i];
+    const int64_t hw = I.hw;
+    const int B = I.B;
+    const int64_t p0 = (int64_t)(g - T->proj_prefix[i]) * PROJ_T;
+    const unsigned n = (unsigned)(hw - p0 < PROJ_T ? hw - p0 : PROJ_T);
+    const int tid = threadIdx.x;
+    if (tid == 0) {
+        mbar_init(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        mbar_expect_tx(&bar, (unsigned)B * n * 4u);
+        for (int b = 0; b < B; ++b) bulk_g2s(xs + b * PROJ_T, I.x + b * hw + p0, n * 4u, &bar);
+    }
+    __syncthreads();  // the barrier is initialised before anyone waits on it
+    const bool ok = mbar_wait(&bar, 0);
+    if (__syncthreads_or(!ok)) {
+        if (tid == 0) {
+            atomicOr(&g_batch_status, 1u);
+            mbar_wait(&bar, 0);  // let the copies land before the block ends
+        }
+        return;
+    }
+    const int q = tid * 4;
+    if ((unsigned)q >= n) return;
+    const int64_t p = p0 + q;
+    const uint4 w4 = __ldg(reinterpret_cast<const uint4 *>(I.bits + p));
+    const uint32_t wv[4] = {w4.x, w4.y, w4.z, w4.w};
+    const float4 yv = ldg4(I.y + p), psv = ldg4(I.phisum + p);
+    const float yy[4] = {yv.x, yv.y, yv.z, yv.w}, pp[4] = {psv.x, psv.y, psv.z, psv.w};
+    float r[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) {
+        float sacc = 0.f;
+        for (int b = 0; b < B; ++b)
+            sacc = fmaf(xs[b * PROJ_T + q + e], ((wv[e] >> b) & 1u) ? 1.f : 0.f, sacc);
+        if (ACC) {
+            const float tt = I.y1[p + e] + (yy[e] - sacc);
+            I.y1[p + e] = tt;
+            r[e] = __fdiv_rn(tt - sacc, pp[e]);
+        } else {
+            r[e] = __fdiv_rn(yy[e] - sacc, pp[e]);
+        }
+    }
+    for (int b = 0; b < B; ++b) {
+        const float4 xv = *reinterpret_cast<const float4 *>(xs + b * PROJ_T + q);
+        float4 o;
+        o.x = fmaf(I.lam, r[0] * (((wv[0] >> b) & 1u) ? 1.f : 0.f), xv.x);
+        o.y = fmaf(I.lam, r[1] * (((wv[1] >> b) & 1u) ? 1.f : 0.f), xv.y);
+        o.z = fmaf(I.lam, r[2] * (((wv[2] >> b) & 1u) ? 1.f : 0.f), xv.z);
+        o.w = fmaf(I.lam, r[3] * (((wv[3] >> b) & 1u) ? 1.f : 0.f), xv.w);
+        st4_cs(I.xp + b * hw + p, o);
+    }
+}
+
+unsigned batch_device_status(bool clear) {
+    unsigned v = 0;
+    if (cudaMemcpyFromSymbol(&v, g_batch_status, sizeof(v)) != cudaSuccess) return 0;
+    if (clear && v) {
+        const unsigned z = 0;
+        cudaMemcpyToSymbol(g_batch_status, &z, sizeof(z));
+    }
+    return v;
 }
 
 // TV pass (FIX = 0) or its stop-test launch (FIX = 1) over all items' tiles.
@@ -264,9 +344,24 @@ int enqueue(const Table &T, Table *dT, const Layout &L, char *ws, int n, int ite
     for (int i = 0; i < n; ++i)
         if (accelerate) SCI_CUDA(cudaMemsetAsync(T.it[i].y1, 0, 4 * T.it[i].hw, s));
     const size_t ebytes = L.tvscratch - L.energy;
+    // bulk-copy projection unless a mask is not 16-byte aligned (the other
+    // planes are checked by check(); SCI_PROJ_TMA=0 selects the plain kernel)
+    int maxB = 1;
+    bool bulk = true;
+    for (int i = 0; i < n; ++i) {
+        maxB = std::max(maxB, T.it[i].B);
+        bulk = bulk && (reinterpret_cast<uintptr_t>(T.it[i].bits) & 15u) == 0;
+    }
+    if (const char *e = getenv("SCI_PROJ_TMA")) bulk = bulk && atoi(e) != 0;
     for (int it = 0; it < iters; ++it) {
-        if (accelerate) k_batch_proj<true><<<pb, PROJ_T, 0, s>>>(dT);
-        else k_batch_proj<false><<<pb, PROJ_T, 0, s>>>(dT);
+        const size_t psm = sizeof(float) * (size_t)maxB * PROJ_T;  // <= 32 KB
+        if (bulk) {
+            if (accelerate) k_batch_proj_tma<true><<<pb, PROJ_T / 4, psm, s>>>(dT);
+            else k_batch_proj_tma<false><<<pb, PROJ_T / 4, psm, s>>>(dT);
+        } else {
+            if (accelerate) k_batch_proj<true><<<pb, PROJ_T, 0, s>>>(dT);
+            else k_batch_proj<false><<<pb, PROJ_T, 0, s>>>(dT);
+        }
         SCI_LAUNCHED("k_batch_proj");
         SCI_CUDA(cudaMemsetAsync(ws + L.energy, 0, ebytes, s));
         k_batch_tv<0><<<tb, tv::WPB * 32, 0, s>>>(dT);

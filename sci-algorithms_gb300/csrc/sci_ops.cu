@@ -35,6 +35,9 @@ int cuda_status(cudaError_t e, const char *what) {
 int launch_proj_gap_tma(const float *x, const uint32_t *bits, const float *y, float *y1,
                         const float *phisum, float *xo, float lam, bool acc, int B, int64_t hw,
                         cudaStream_t s);
+int launch_proj_admm_tma(const float *th, const float *bb, const uint32_t *bits, const float *y,
+                         const float *phisum, float *v, float *xo, float lam, float gamma, int B,
+                         int64_t hw, cudaStream_t s);
 
 // Grid for a grid-stride loop over `n` work units of one thread each.
 static inline dim3 grid_for(int64_t n, int threads) {
@@ -622,17 +625,16 @@ int sci_proj_admm(const float *theta, const float *b, const float *phi,
     cudaStream_t s = as_stream(stream);
     const bool vec = vec_ok(hw, {theta, b, phi, mask_bits, y, phisum, v, x_out});
     const int Bi = (int)B;
+    const char *tma = getenv("SCI_PROJ_TMA");
+    if (mask_bits && !(tma && atoi(tma) == 0)) {
+        // bulk-copy staged kernel; SCI_ERR_UNSUPPORTED: alignment or B
+        const int e = launch_proj_admm_tma(theta, b, mask_bits, y, phisum, v, x_out, lambda,
+                                           gamma, Bi, hw, s);
+        if (e != SCI_ERR_UNSUPPORTED) return e;
+    }
     if (mask_bits) {
         Mask<1> M{mask_bits, hw};
         launch_admm_smem<1>(theta, b, M, y, phisum, v, x_out, lambda, gamma, Bi, hw, s);
-    } else if (false) {
-        Mask<1> M{mask_bits, hw};
-        if (vec)
-            k_proj_admm_vec<1><<<grid_for(hw / 4, 256), 256, 0, s>>>(theta, b, M, y, phisum, v,
-                                                                     x_out, lambda, gamma, Bi, hw);
-        else
-            k_proj_admm_scalar<1><<<grid_for(hw, 256), 256, 0, s>>>(theta, b, M, y, phisum, v,
-                                                                    x_out, lambda, gamma, Bi, hw);
     } else {
         Mask<0> M{phi, hw};
         if (vec)

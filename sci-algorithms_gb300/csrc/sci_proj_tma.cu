@@ -21,7 +21,9 @@
 // flight and ends the block.
 #include <algorithm>
 #include <cstdlib>
+#include <type_traits>
 
+#include "sci_bulk.cuh"
 #include "sci_common.cuh"
 
 namespace sci {
@@ -29,50 +31,6 @@ namespace sci {
 __device__ unsigned int g_device_status;
 
 namespace {
-
-constexpr int kWaitPolls = 1 << 22;  // mbarrier polls before a wait gives up
-
-__device__ __forceinline__ uint32_t smem_u32(const void *p) {
-    return (uint32_t)__cvta_generic_to_shared(p);
-}
-
-__device__ __forceinline__ void mbar_init(uint64_t *bar, unsigned count) {
-    asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
-                 : "memory");
-}
-
-__device__ __forceinline__ void mbar_expect_tx(uint64_t *bar, unsigned bytes) {
-    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
-                 "r"(bytes)
-                 : "memory");
-}
-
-__device__ __forceinline__ bool mbar_try_wait(uint64_t *bar, unsigned parity) {
-    uint32_t ok;
-    asm volatile(
-        "{\n\t.reg .pred p;\n\t"
-        "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
-        "selp.u32 %0, 1, 0, p;\n\t}"
-        : "=r"(ok)
-        : "r"(smem_u32(bar)), "r"(parity)
-        : "memory");
-    return ok != 0;
-}
-
-// Bounded wait for phase `parity` of `bar` to complete.
-__device__ __forceinline__ bool mbar_wait(uint64_t *bar, unsigned parity) {
-    for (int i = 0; i < kWaitPolls; ++i)
-        if (mbar_try_wait(bar, parity)) return true;
-    return false;
-}
-
-__device__ __forceinline__ void bulk_g2s(void *dst, const void *src, unsigned bytes,
-                                         uint64_t *bar) {
-    asm volatile(
-        "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];"
-        ::"r"(smem_u32(dst)), "l"(src), "r"(bytes), "r"(smem_u32(bar))
-        : "memory");
-}
 
 __device__ __forceinline__ float bit(uint32_t w, int b) { return ((w >> b) & 1u) ? 1.0f : 0.0f; }
 
@@ -176,6 +134,103 @@ __global__ void __launch_bounds__(TP / 4) k_proj_gap_tma(
     }
 }
 
+// ADMM projection (pnp_sci_algo.py:808-812 with a packed mask), same
+// arithmetic as k_proj_admm_smem: t_b = theta_b + b_b, yb = sum_b t_b phi_b,
+// r = (y - yb) / (Phi_sum + gamma), x_b = t_b + lambda (r phi_b),
+// v_b = x_b - b_b; x written when WANT_X.  A tile stages theta and b (2B
+// rows of TP floats) with the same bulk copies and mbarrier scheme.
+template <int TP>
+__device__ __forceinline__ void issue_tile2(float *xs, uint64_t *bars, int buf, int64_t t,
+                                            const float *th, const float *bb, int B, int64_t hw) {
+    const int64_t p0 = t * TP;
+    const int64_t rem = hw - p0;
+    const unsigned n = (unsigned)(rem < TP ? rem : TP);
+    float *dst = xs + (int64_t)buf * 2 * B * TP;
+    mbar_expect_tx(bars + buf, 2u * (unsigned)B * n * 4u);
+    for (int b = 0; b < B; ++b) {
+        bulk_g2s(dst + b * TP, th + b * hw + p0, n * 4u, bars + buf);
+        bulk_g2s(dst + (B + b) * TP, bb + b * hw + p0, n * 4u, bars + buf);
+    }
+}
+
+template <int TP, bool WANT_X>
+__global__ void __launch_bounds__(TP / 4) k_proj_admm_tma(
+    const float *__restrict__ th, const float *__restrict__ bb, const uint32_t *__restrict__ bits,
+    const float *__restrict__ y, const float *__restrict__ phisum, float *__restrict__ v,
+    float *__restrict__ xo, float lam, float gamma, int B, int64_t hw) {
+    extern __shared__ __align__(128) float xs[];  // [2][2B][TP]
+    __shared__ __align__(8) uint64_t bars[2];
+    const int tid = threadIdx.x;
+    const int64_t ntiles = (hw + TP - 1) / TP;
+    const int64_t G = gridDim.x;
+    if (tid == 0) {
+        mbar_init(bars + 0, 1);
+        mbar_init(bars + 1, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    }
+    __syncthreads();
+    const int64_t t0 = blockIdx.x;
+    if (tid == 0) {
+        if (t0 < ntiles) issue_tile2<TP>(xs, bars, 0, t0, th, bb, B, hw);
+        if (t0 + G < ntiles) issue_tile2<TP>(xs, bars, 1, t0 + G, th, bb, B, hw);
+    }
+    int i = 0;
+    for (int64_t t = t0; t < ntiles; t += G, ++i) {
+        const int buf = i & 1;
+        const unsigned parity = (unsigned)(i >> 1) & 1u;
+        const bool ok = mbar_wait(bars + buf, parity);
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) {
+                atomicOr(&g_device_status, 1u);
+                mbar_wait(bars + buf, parity);
+                if (t + G < ntiles) mbar_wait(bars + (buf ^ 1), (unsigned)((i + 1) >> 1) & 1u);
+            }
+            return;
+        }
+        const int64_t p0 = t * TP;
+        const int q = tid * 4;
+        if (p0 + q < hw) {
+            const int64_t p = p0 + q;
+            const float *tb = xs + (int64_t)buf * 2 * B * TP + q;
+            const float *bs = tb + (int64_t)B * TP;
+            const uint4 w = __ldg(reinterpret_cast<const uint4 *>(bits + p));
+            float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll 4
+            for (int b = 0; b < B; ++b) {
+                const float4 a = *reinterpret_cast<const float4 *>(tb + b * TP);
+                const float4 c = *reinterpret_cast<const float4 *>(bs + b * TP);
+                s.x = fmaf(a.x + c.x, bit(w.x, b), s.x);
+                s.y = fmaf(a.y + c.y, bit(w.y, b), s.y);
+                s.z = fmaf(a.z + c.z, bit(w.z, b), s.z);
+                s.w = fmaf(a.w + c.w, bit(w.w, b), s.w);
+            }
+            const float4 yv = ldg4(y + p), ps = ldg4(phisum + p);
+            const float4 r = make_float4(__fdiv_rn(yv.x - s.x, ps.x + gamma),
+                                         __fdiv_rn(yv.y - s.y, ps.y + gamma),
+                                         __fdiv_rn(yv.z - s.z, ps.z + gamma),
+                                         __fdiv_rn(yv.w - s.w, ps.w + gamma));
+#pragma unroll 4
+            for (int b = 0; b < B; ++b) {
+                const float4 a = *reinterpret_cast<const float4 *>(tb + b * TP);
+                const float4 c = *reinterpret_cast<const float4 *>(bs + b * TP);
+                float4 x;
+                x.x = fmaf(lam, r.x * bit(w.x, b), a.x + c.x);
+                x.y = fmaf(lam, r.y * bit(w.y, b), a.y + c.y);
+                x.z = fmaf(lam, r.z * bit(w.z, b), a.z + c.z);
+                x.w = fmaf(lam, r.w * bit(w.w, b), a.w + c.w);
+                if (WANT_X) st4(xo + b * hw + p, x);
+                st4_cs(v + b * hw + p, make_float4(x.x - c.x, x.y - c.y, x.z - c.z, x.w - c.w));
+            }
+        }
+        __syncthreads();
+        if (tid == 0 && t + 2 * G < ntiles) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            issue_tile2<TP>(xs, bars, buf, t + 2 * G, th, bb, B, hw);
+        }
+    }
+}
+
 template <int TP>
 int launch_tp(const float *x, const uint32_t *bits, const float *y, float *y1,
               const float *phisum, float *xo, float lam, bool acc, int B, int64_t hw,
@@ -215,10 +270,49 @@ int launch_proj_gap_tma(const float *x, const uint32_t *bits, const float *y, fl
     return launch_tp<128>(x, bits, y, y1, phisum, xo, lam, acc, B, hw, s);
 }
 
+// ADMM projection with a packed mask (B <= 32, 16-byte aligned planes,
+// hw % 4 == 0); SCI_ERR_UNSUPPORTED otherwise.  Tiles of TP pixels x 2B
+// rows, double-buffered (48 KB at 24 frames and TP = 128).
+int launch_proj_admm_tma(const float *th, const float *bb, const uint32_t *bits, const float *y,
+                         const float *phisum, float *v, float *xo, float lam, float gamma, int B,
+                         int64_t hw, cudaStream_t s) {
+    const uintptr_t a = reinterpret_cast<uintptr_t>(th) | reinterpret_cast<uintptr_t>(bb) |
+                        reinterpret_cast<uintptr_t>(bits) | reinterpret_cast<uintptr_t>(y) |
+                        reinterpret_cast<uintptr_t>(phisum) | reinterpret_cast<uintptr_t>(v) |
+                        reinterpret_cast<uintptr_t>(xo);
+    if ((a & 15u) || hw % 4 || B < 1 || B > 32) return SCI_ERR_UNSUPPORTED;
+    const char *e = getenv("SCI_PROJ_TP");
+    const int tp = e ? atoi(e) : 128;
+    auto go = [&](auto tpc) -> int {
+        constexpr int TP = decltype(tpc)::value;
+        const size_t smem = sizeof(float) * 2 * 2 * (size_t)B * TP;
+        const int64_t ntiles = (hw + TP - 1) / TP;
+        const int64_t per_sm =
+            std::max<int64_t>(1, std::min<int64_t>(16, (227 * 1024) / (int64_t)(smem + 1024)));
+        const unsigned g = (unsigned)std::min<int64_t>(ntiles, per_sm * kSMs);
+        auto kern = xo ? k_proj_admm_tma<TP, true> : k_proj_admm_tma<TP, false>;
+        SCI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      (int)smem));
+        kern<<<g, TP / 4, smem, s>>>(th, bb, bits, y, phisum, v, xo, lam, gamma, B, hw);
+        SCI_LAUNCHED("k_proj_admm_tma");
+        return SCI_OK;
+    };
+    if (tp == 256) return go(std::integral_constant<int, 256>{});
+    if (tp == 64) return go(std::integral_constant<int, 64>{});
+    return go(std::integral_constant<int, 128>{});
+}
+
+}  // namespace sci
+
+namespace sci {
+namespace batch {
+unsigned batch_device_status(bool clear);  // sci_batch.cu
+}
 }  // namespace sci
 
 extern "C" int sci_device_status(unsigned int *status, int clear) {
     SCI_CHECK_ARG(status, "sci_device_status: null pointer");
+    const unsigned int batch = sci::batch::batch_device_status(clear != 0);
     unsigned int v = 0;
     cudaError_t e = cudaMemcpyFromSymbol(&v, sci::g_device_status, sizeof(v));
     if (e != cudaSuccess) return sci::cuda_status(e, "cudaMemcpyFromSymbol");
@@ -227,6 +321,6 @@ extern "C" int sci_device_status(unsigned int *status, int clear) {
         e = cudaMemcpyToSymbol(sci::g_device_status, &z, sizeof(z));
         if (e != cudaSuccess) return sci::cuda_status(e, "cudaMemcpyToSymbol");
     }
-    *status = v;
+    *status = v | batch;
     return SCI_OK;
 }

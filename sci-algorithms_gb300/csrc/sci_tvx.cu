@@ -93,35 +93,117 @@ __device__ __forceinline__ float lane_reduce(float v, float (*red)[32]) {
     return s;
 }
 
-// ITV3D: denom = 1 + dt sqrt(sum over frames of z1^2 + z2^2).
+// ITV3D: denom = 1 + dt sqrt(sum over frames of z1^2 + z2^2).  A block
+// owns a strip of 32 columns and RB rows and walks down it: per row it
+// loads p1, p2 and f of the next row once (the left neighbour of p1 and
+// the right neighbour of z come by shuffle; lanes 0 and 31 load the strip's
+// halo columns), reduces the norm over the frames in shared memory and
+// writes the updated duals of the row.
+#ifndef SCI_ITV3D_RB
+#define SCI_ITV3D_RB 16
+#endif
+constexpr int RB = SCI_ITV3D_RB;  // rows per block
+
 __global__ void __launch_bounds__(32 * FL) k_cham_update_coupled(
     const float *__restrict__ f, const float *__restrict__ p1, const float *__restrict__ p2,
     float *__restrict__ q1, float *__restrict__ q2, Geo g, int nf, float lam, float dt,
     int first) {
     __shared__ float red[FL][32];
-    const int j = blockIdx.x * 32 + threadIdx.x, i = blockIdx.y;
+    const int lane = threadIdx.x;
+    const int x0 = blockIdx.x * 32, j = x0 + lane;
+    const int i0 = blockIdx.y * RB, i1 = min(i0 + RB, g.H);
     const bool in = j < g.W;
-    const int64_t p = (int64_t)i * g.W + j;
-    float z1[FMAX], z2[FMAX], s = 0.f;
+    const int jc = in ? j : g.W - 1;           // a valid column for the loads
+    const bool right = x0 + 32 < g.W;          // the strip has a right halo column
+    const int jr = right ? x0 + 32 : jc;
+    // z at (i, col) from p1(i, col), p1(i, col-1), p2(i, col), p2(i-1, col), f
+    auto zval = [&](float a, float al, float b, float bu, float fv) {
+        return (((a - al) + b) - bu) - fv * lam;
+    };
+    float zc[FMAX], zr[FMAX], p1c[FMAX], p2c[FMAX], p2r[FMAX];
 #pragma unroll
-    for (int t = 0; t < FMAX; ++t) {
+    for (int t = 0; t < FMAX; ++t) {  // row i0
         const int b = threadIdx.y + t * FL;
-        z1[t] = z2[t] = 0.f;
-        if (in && b < nf) {
-            const int64_t fo = (int64_t)b * g.hw;
-            cham_grad(f + fo, p1 + fo, p2 + fo, g, i, j, lam, first != 0, z1[t], z2[t]);
-            s += z1[t] * z1[t] + z2[t] * z2[t];
+        zc[t] = zr[t] = p1c[t] = p2c[t] = p2r[t] = 0.f;
+        if (b >= nf) continue;
+        const int64_t fo = (int64_t)b * g.hw;
+        const int64_t o = fo + (int64_t)i0 * g.W;
+        if (first) {
+            zc[t] = -f[o + jc] * lam;
+            if (lane == 31 && right) zr[t] = -f[o + jr] * lam;
+            continue;
+        }
+        const float a = p1[o + jc], bb = p2[o + jc];
+        const float al = (jc > 0) ? p1[o + jc - 1] : a;
+        const float bu = (i0 > 0) ? p2[o - g.W + jc] : bb;
+        zc[t] = zval(a, al, bb, bu, f[o + jc]);
+        p1c[t] = a;
+        p2c[t] = bb;
+        if (lane == 31 && right) {
+            const float ar = p1[o + jr], br = p2[o + jr];
+            const float bur = (i0 > 0) ? p2[o - g.W + jr] : br;
+            zr[t] = zval(ar, p1[o + jr - 1], br, bur, f[o + jr]);
+            p2r[t] = br;
         }
     }
-    const float denom = 1.f + dt * sqrtf(lane_reduce(s, red));
+    for (int i = i0; i < i1; ++i) {
+        const bool lastrow = i + 1 >= g.H;
+        float z1[FMAX], z2[FMAX], zn[FMAX], p1n[FMAX], p2n[FMAX], zrn[FMAX], p2rn[FMAX];
+        float s = 0.f;
 #pragma unroll
-    for (int t = 0; t < FMAX; ++t) {
-        const int b = threadIdx.y + t * FL;
-        if (in && b < nf) {
-            const int64_t q = (int64_t)b * g.hw + p;
-            const float a = first ? 0.f : p1[q], c = first ? 0.f : p2[q];
-            q1[q] = (a + dt * z1[t]) / denom;
-            q2[q] = (c + dt * z2[t]) / denom;
+        for (int t = 0; t < FMAX; ++t) {
+            const int b = threadIdx.y + t * FL;
+            // right neighbour of z in this row (all lanes shuffle)
+            float zright = __shfl_down_sync(0xffffffffu, zc[t], 1);
+            if (lane == 31) zright = zr[t];
+            zn[t] = p1n[t] = p2n[t] = zrn[t] = p2rn[t] = 0.f;
+            z1[t] = z2[t] = 0.f;
+            if (b >= nf) continue;
+            const int64_t fo = (int64_t)b * g.hw;
+            if (!lastrow) {  // row i + 1
+                const int64_t o = fo + (int64_t)(i + 1) * g.W;
+                if (first) {
+                    zn[t] = -f[o + jc] * lam;
+                    if (lane == 31 && right) zrn[t] = -f[o + jr] * lam;
+                } else {
+                    const float a = p1[o + jc], bb = p2[o + jc];
+                    float al = __shfl_up_sync(0xffffffffu, a, 1);
+                    if (lane == 0) al = (x0 > 0) ? p1[o + x0 - 1] : a;
+                    if (jc == 0) al = a;  // MATLAB: no p1 at the first column
+                    zn[t] = zval(a, al, bb, p2c[t], f[o + jc]);
+                    p1n[t] = a;
+                    p2n[t] = bb;
+                    if (lane == 31 && right) {
+                        const float ar = p1[o + jr], br = p2[o + jr];
+                        zrn[t] = zval(ar, a, br, p2r[t], f[o + jr]);
+                        p2rn[t] = br;
+                    }
+                }
+            }
+            z1[t] = (j < g.W - 1) ? zright - zc[t] : 0.f;
+            z2[t] = lastrow ? 0.f : zn[t] - zc[t];
+            s += z1[t] * z1[t] + z2[t] * z2[t];
+        }
+        red[threadIdx.y][lane] = s;
+        __syncthreads();
+        float tot = 0.f;
+#pragma unroll
+        for (int l = 0; l < FL; ++l) tot += red[l][lane];
+        __syncthreads();
+        const float denom = 1.f + dt * sqrtf(tot);
+#pragma unroll
+        for (int t = 0; t < FMAX; ++t) {
+            const int b = threadIdx.y + t * FL;
+            if (b < nf && in) {
+                const int64_t q = (int64_t)b * g.hw + (int64_t)i * g.W + j;
+                q1[q] = (p1c[t] + dt * z1[t]) / denom;
+                q2[q] = (p2c[t] + dt * z2[t]) / denom;
+            }
+            zc[t] = zn[t];
+            p1c[t] = p1n[t];
+            p2c[t] = p2n[t];
+            zr[t] = zrn[t];
+            p2r[t] = p2rn[t];
         }
     }
 }
@@ -288,9 +370,11 @@ int tvx_launch(int kind, const float *f, float *u, float *resid, int64_t nf, int
     Geo g{(int)H, (int)W, hw};
     const dim3 blk(32, 8);
     const dim3 grd((unsigned)((W + 31) / 32), (unsigned)((H + 7) / 8), (unsigned)nf);
-    // frame-coupled kernels: 32 pixels x FL frame lanes per block, one row
+    // frame-coupled kernels: 32 pixels x FL frame lanes per block; FGP one
+    // row per block, Chambolle RB rows per block
     const dim3 blkc(32, FL);
     const dim3 grdc((unsigned)((W + 31) / 32), (unsigned)H, 1);
+    const dim3 grds((unsigned)((W + 31) / 32), (unsigned)((H + RB - 1) / RB), 1);
     float *w0 = static_cast<float *>(ws);
     float *a1 = w0, *a2 = w0 + n, *b1 = w0 + 2 * n, *b2 = w0 + 3 * n;
     if (steps) {
@@ -318,7 +402,7 @@ int tvx_launch(int kind, const float *f, float *u, float *resid, int64_t nf, int
             const float dt = 0.25f;
             float *p1 = a1, *p2 = a2, *q1 = b1, *q2 = b2;
             for (int it = 0; it < iters; ++it) {
-                k_cham_update_coupled<<<grdc, blkc, 0, s>>>(f, p1, p2, q1, q2, g, (int)nf, lam,
+                k_cham_update_coupled<<<grds, blkc, 0, s>>>(f, p1, p2, q1, q2, g, (int)nf, lam,
                                                             dt, it == 0);
                 SCI_LAUNCHED("k_cham_update_coupled");
                 std::swap(p1, q1);

@@ -41,6 +41,23 @@ def test_batch_matches_single_solver(autotune):
         assert torch.equal(a, b)
 
 
+@pytest.mark.parametrize("accelerate", [True, False])
+def test_batch_bulk_copy_projection_is_bitwise_equal(monkeypatch, accelerate):
+    """The bulk-copy staged batch projection (the default) against the
+    per-thread shared-memory kernel: identical results after 6 iterations."""
+    shapes = [(64, 64, 8, 0.5), (40, 48, 4, 0.7), (33, 200, 32, 0.45), (96, 256, 12, 0.6),
+              (300, 260, 24, 0.5)]
+    data = make_items(shapes, seed=5)
+    runs = []
+    for tma in ("1", "0"):
+        monkeypatch.setenv("SCI_PROJ_TMA", tma)
+        bs = sci.BatchSolver([d[2] for d in data], [d[1] for d in data], iters=6, tv_weight=0.1,
+                             accelerate=accelerate, autotune=False)
+        runs.append([x.clone() for x in bs.run()])
+    for a, b in zip(*runs):
+        assert torch.equal(a, b)
+
+
 def test_batch_against_oracle():
     shapes = [(48, 64, 8, 0.5), (64, 40, 6, 0.4)]
     data = make_items(shapes, seed=7)

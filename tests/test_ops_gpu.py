@@ -148,6 +148,39 @@ def test_proj_gap_bulk_copy_kernel_is_bitwise_equal(monkeypatch, B, H, W, tile):
     assert device_status() == 0
 
 
+@pytest.mark.parametrize("tile", ["128", "64", "256"])
+@pytest.mark.parametrize("B,H,W", [(1, 16, 16), (8, 37, 64), (24, 130, 260), (32, 64, 96),
+                                   (24, 512, 512)])
+def test_proj_admm_bulk_copy_kernel_is_bitwise_equal(monkeypatch, B, H, W, tile):
+    """The bulk-copy staged ADMM projection against the shared-memory
+    kernel: identical v and x (with and without x), partial last tiles."""
+    rng = np.random.default_rng(B * 7 + W)
+    mask = (rng.random((H, W, B)) < 0.5).astype(np.float64)
+    op = sci.MaskOperator(mask)
+    th = _dev.planar(rng.random((H, W, B)))
+    bb = _dev.planar(0.1 * rng.standard_normal((H, W, B)))
+    y = _dev.plane(rng.random((H, W)) * 4)
+    msum = mask.sum(axis=2)
+    msum[msum == 0] = 1
+    ps = _dev.plane(msum)
+    monkeypatch.setenv("SCI_PROJ_TP", tile)
+    outs = []
+    for tma in ("1", "0"):
+        monkeypatch.setenv("SCI_PROJ_TMA", tma)
+        for want_x in (True, False):
+            v = torch.empty_like(th)
+            x = torch.empty_like(th) if want_x else None
+            call("sci_proj_admm", th.data_ptr(), bb.data_ptr(), None, op.bits.data_ptr(),
+                 y.data_ptr(), ps.data_ptr(), v.data_ptr(), _dev.ptr(x), 0.9, 0.01, B, H, W,
+                 _dev.stream_handle())
+            torch.cuda.synchronize()
+            outs.append((v.clone(), None if x is None else x.clone()))
+    for (va, xa), (vb, xb) in zip(outs[:2], outs[2:]):
+        assert torch.equal(va, vb)
+        assert (xa is None and xb is None) or torch.equal(xa, xb)
+    assert device_status() == 0
+
+
 @pytest.mark.parametrize("packed", [True, False])
 def test_proj_admm_matches_reference_step(packed):
     rng = np.random.default_rng(12)
