@@ -49,6 +49,13 @@ int sci_last_error(char *buf, size_t n);
  * the reference (library plumbing). */
 int sci_device_status(unsigned int *status, int clear);
 
+/* Exercises the error path of the bounded device-side waits: one block
+ * waits, `polls` times at most (1 .. 2^20), on a barrier that expects bytes
+ * no copy delivers, then sets bit 0 of the device status word and returns.
+ * For tests of that path; the context stays usable.  No counterpart in the
+ * reference. */
+int sci_selftest_bounded_wait(unsigned int polls, void *stream);
+
 /* ---------------------------------------------------------- L1 operators */
 
 /* y = sum_b phi_b .* x_b.

@@ -55,6 +55,7 @@ _SIGS = {
     "sci_version": [],
     "sci_last_error": [ctypes.c_char_p, c_sz],
     "sci_device_status": [ctypes.POINTER(ctypes.c_uint), ctypes.c_int],
+    "sci_selftest_bounded_wait": [ctypes.c_uint, c_vp],
     "sci_A": [c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_vp],
     "sci_At": [c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_vp],
     "sci_phisum": [c_vp, c_vp, c_i64, c_i64, c_i64, ctypes.c_int, c_vp],

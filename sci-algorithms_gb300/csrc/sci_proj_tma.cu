@@ -139,26 +139,30 @@ __global__ void __launch_bounds__(TP / 4) k_proj_gap_tma(
 // r = (y - yb) / (Phi_sum + gamma), x_b = t_b + lambda (r phi_b),
 // v_b = x_b - b_b; x written when WANT_X.  A tile stages theta and b (2B
 // rows of TP floats) with the same bulk copies and mbarrier scheme.
-template <int TP>
+template <int TP, bool STAGE_B>
 __device__ __forceinline__ void issue_tile2(float *xs, uint64_t *bars, int buf, int64_t t,
                                             const float *th, const float *bb, int B, int64_t hw) {
     const int64_t p0 = t * TP;
     const int64_t rem = hw - p0;
     const unsigned n = (unsigned)(rem < TP ? rem : TP);
-    float *dst = xs + (int64_t)buf * 2 * B * TP;
-    mbar_expect_tx(bars + buf, 2u * (unsigned)B * n * 4u);
+    constexpr int R = STAGE_B ? 2 : 1;
+    float *dst = xs + (int64_t)buf * R * B * TP;
+    mbar_expect_tx(bars + buf, (unsigned)R * (unsigned)B * n * 4u);
     for (int b = 0; b < B; ++b) {
         bulk_g2s(dst + b * TP, th + b * hw + p0, n * 4u, bars + buf);
-        bulk_g2s(dst + (B + b) * TP, bb + b * hw + p0, n * 4u, bars + buf);
+        if (STAGE_B) bulk_g2s(dst + (B + b) * TP, bb + b * hw + p0, n * 4u, bars + buf);
     }
 }
 
-template <int TP, bool WANT_X>
+// STAGE_B: b is staged with theta; otherwise b is read with 16-byte loads
+// (twice; the second read is served by the caches) and a block needs half
+// the shared memory.
+template <int TP, bool WANT_X, bool STAGE_B>
 __global__ void __launch_bounds__(TP / 4) k_proj_admm_tma(
     const float *__restrict__ th, const float *__restrict__ bb, const uint32_t *__restrict__ bits,
     const float *__restrict__ y, const float *__restrict__ phisum, float *__restrict__ v,
     float *__restrict__ xo, float lam, float gamma, int B, int64_t hw) {
-    extern __shared__ __align__(128) float xs[];  // [2][2B][TP]
+    extern __shared__ __align__(128) float xs[];  // [2][2B or B][TP]
     __shared__ __align__(8) uint64_t bars[2];
     const int tid = threadIdx.x;
     const int64_t ntiles = (hw + TP - 1) / TP;
@@ -172,8 +176,8 @@ __global__ void __launch_bounds__(TP / 4) k_proj_admm_tma(
     __syncthreads();
     const int64_t t0 = blockIdx.x;
     if (tid == 0) {
-        if (t0 < ntiles) issue_tile2<TP>(xs, bars, 0, t0, th, bb, B, hw);
-        if (t0 + G < ntiles) issue_tile2<TP>(xs, bars, 1, t0 + G, th, bb, B, hw);
+        if (t0 < ntiles) issue_tile2<TP, STAGE_B>(xs, bars, 0, t0, th, bb, B, hw);
+        if (t0 + G < ntiles) issue_tile2<TP, STAGE_B>(xs, bars, 1, t0 + G, th, bb, B, hw);
     }
     int i = 0;
     for (int64_t t = t0; t < ntiles; t += G, ++i) {
@@ -192,14 +196,18 @@ __global__ void __launch_bounds__(TP / 4) k_proj_admm_tma(
         const int q = tid * 4;
         if (p0 + q < hw) {
             const int64_t p = p0 + q;
-            const float *tb = xs + (int64_t)buf * 2 * B * TP + q;
+            const float *tb = xs + (int64_t)buf * (STAGE_B ? 2 : 1) * B * TP + q;
             const float *bs = tb + (int64_t)B * TP;
+            auto bload = [&](int b) {
+                return STAGE_B ? *reinterpret_cast<const float4 *>(bs + b * TP)
+                               : ldg4(bb + b * hw + p);
+            };
             const uint4 w = __ldg(reinterpret_cast<const uint4 *>(bits + p));
             float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll 4
             for (int b = 0; b < B; ++b) {
                 const float4 a = *reinterpret_cast<const float4 *>(tb + b * TP);
-                const float4 c = *reinterpret_cast<const float4 *>(bs + b * TP);
+                const float4 c = bload(b);
                 s.x = fmaf(a.x + c.x, bit(w.x, b), s.x);
                 s.y = fmaf(a.y + c.y, bit(w.y, b), s.y);
                 s.z = fmaf(a.z + c.z, bit(w.z, b), s.z);
@@ -213,7 +221,7 @@ __global__ void __launch_bounds__(TP / 4) k_proj_admm_tma(
 #pragma unroll 4
             for (int b = 0; b < B; ++b) {
                 const float4 a = *reinterpret_cast<const float4 *>(tb + b * TP);
-                const float4 c = *reinterpret_cast<const float4 *>(bs + b * TP);
+                const float4 c = bload(b);
                 float4 x;
                 x.x = fmaf(lam, r.x * bit(w.x, b), a.x + c.x);
                 x.y = fmaf(lam, r.y * bit(w.y, b), a.y + c.y);
@@ -226,7 +234,7 @@ __global__ void __launch_bounds__(TP / 4) k_proj_admm_tma(
         __syncthreads();
         if (tid == 0 && t + 2 * G < ntiles) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            issue_tile2<TP>(xs, bars, buf, t + 2 * G, th, bb, B, hw);
+            issue_tile2<TP, STAGE_B>(xs, bars, buf, t + 2 * G, th, bb, B, hw);
         }
     }
 }
@@ -283,14 +291,19 @@ int launch_proj_admm_tma(const float *th, const float *bb, const uint32_t *bits,
     if ((a & 15u) || hw % 4 || B < 1 || B > 32) return SCI_ERR_UNSUPPORTED;
     const char *e = getenv("SCI_PROJ_TP");
     const int tp = e ? atoi(e) : 128;
+    // theta staged, b read with 16-byte loads: staging b as well (twice the
+    // shared memory per block) measured the same, 0.251 ms at 2048^2 x 24
+    const bool stage_b = false;
     auto go = [&](auto tpc) -> int {
         constexpr int TP = decltype(tpc)::value;
-        const size_t smem = sizeof(float) * 2 * 2 * (size_t)B * TP;
+        const size_t smem = sizeof(float) * 2 * (stage_b ? 2 : 1) * (size_t)B * TP;
         const int64_t ntiles = (hw + TP - 1) / TP;
         const int64_t per_sm =
             std::max<int64_t>(1, std::min<int64_t>(16, (227 * 1024) / (int64_t)(smem + 1024)));
         const unsigned g = (unsigned)std::min<int64_t>(ntiles, per_sm * kSMs);
-        auto kern = xo ? k_proj_admm_tma<TP, true> : k_proj_admm_tma<TP, false>;
+        auto kern = stage_b ? (xo ? k_proj_admm_tma<TP, true, true> : k_proj_admm_tma<TP, false, true>)
+                            : (xo ? k_proj_admm_tma<TP, true, false>
+                                  : k_proj_admm_tma<TP, false, false>);
         SCI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
         kern<<<g, TP / 4, smem, s>>>(th, bb, bits, y, phisum, v, xo, lam, gamma, B, hw);
@@ -308,7 +321,39 @@ namespace sci {
 namespace batch {
 unsigned batch_device_status(bool clear);  // sci_batch.cu
 }
+namespace {
+
+// The error path of the bounded waits, on purpose: the barrier expects 16
+// bytes that no copy delivers, so every poll fails; after `polls` polls the
+// kernel records the timeout in the status word and returns.  No copy is in
+// flight, so nothing lands in the block's shared memory after it ends.
+__global__ void k_wait_selftest(unsigned polls) {
+    __shared__ __align__(8) uint64_t bar;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        mbar_expect_tx(&bar, 16u);
+    }
+    __syncthreads();
+    bool ok = false;
+    for (unsigned i = 0; i < polls && !ok; ++i) ok = mbar_try_wait(&bar, 0);
+    if (__syncthreads_or(!ok) && threadIdx.x == 0) atomicOr(&g_device_status, 1u);
+}
+
+}  // namespace
+
+int selftest_bounded_wait(unsigned polls, cudaStream_t s) {
+    SCI_CHECK_ARG(polls >= 1 && polls <= (1u << 20), "selftest: 1 <= polls <= 2^20");
+    k_wait_selftest<<<1, 32, 0, s>>>(polls);
+    SCI_LAUNCHED("k_wait_selftest");
+    return SCI_OK;
+}
+
 }  // namespace sci
+
+extern "C" int sci_selftest_bounded_wait(unsigned int polls, void *stream) {
+    return sci::selftest_bounded_wait(polls, sci::as_stream(stream));
+}
 
 extern "C" int sci_device_status(unsigned int *status, int clear) {
     SCI_CHECK_ARG(status, "sci_device_status: null pointer");

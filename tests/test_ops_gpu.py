@@ -181,6 +181,18 @@ def test_proj_admm_bulk_copy_kernel_is_bitwise_equal(monkeypatch, B, H, W, tile)
     assert device_status() == 0
 
 
+def test_bounded_wait_reports_and_the_context_survives():
+    """A bulk-copy wait that runs out (a barrier nothing completes) sets the
+    status bit instead of hanging; the next kernels run normally."""
+    assert device_status() == 0
+    call("sci_selftest_bounded_wait", 1000, _dev.stream_handle())
+    torch.cuda.synchronize()
+    assert device_status() == 1  # read and cleared
+    assert device_status() == 0
+    # the context is intact: a projection still matches the oracle step
+    test_proj_gap_matches_reference_step(True, True, 64)
+
+
 @pytest.mark.parametrize("packed", [True, False])
 def test_proj_admm_matches_reference_step(packed):
     rng = np.random.default_rng(12)
