@@ -419,3 +419,184 @@ def admm_denoise_bayer(y_bayer, Phi_bayer, _lambda=1, gamma=0.01, denoiser='tv',
             if show_iqa and X_orig is not None:
                 psnr_all.append(psnr(X_orig, _bayer_join(xall, Phi_bayer)))
     return _bayer_join(xall, Phi_bayer), psnr_all
+
+
+# ------------------------------------------------- joint TV + CNN loops
+def box_blur(x):
+    """The stand-in CNN of the joint fixtures: a 3 x 3 box blur of every
+    frame with replicated edges (the FFDNet / FastDVDnet weights are not in
+    the reference tree)."""
+    x = np.asarray(x, np.float64)
+    xp = np.pad(x, ((1, 1), (1, 1), (0, 0)), mode="edge")
+    H, W = x.shape[:2]
+    out = np.zeros_like(x)
+    for di in range(3):
+        for dj in range(3):
+            out += xp[di:di + H, dj:dj + W]
+    return out / 9.0
+
+
+def cnn_stand_in(x, nsig, model=None, gray=True):
+    """(x, nsig, model) -> x, the call shape of ffdnet_vdenoiser /
+    fastdvdnet_denoiser; here the box blur."""
+    return box_blur(x)
+
+
+# PnP_SCI/python/joint_pnp_sci_algo.py.  `cnn(x, nsig, model)` stands where
+# the reference calls ffdnet_vdenoiser(x, nsig, model) /
+# fastdvdnet_denoiser(x, nsig, model, gray=True) (:243, :267, :442, :467).
+def _tv_step(x, tv_weight, tv_iter_max, multichannel, tvm):
+    if tvm not in ('tv_chambolle', 'ITV3D_FGP', 'ITV2D_cham'):
+        raise ValueError('oracle supports the tv_chambolle denoiser')
+    return denoise_tv_chambolle(x, tv_weight, n_iter_max=tv_iter_max, multichannel=multichannel)
+
+
+def joint_admm_denoise(y, Phi_sum, A, At, _lambda=1, gamma=0.0, denoiser='tv', iter_max=50,
+                       sigma=None, tv_weight=0.1, tv_iter_max=5, multichannel=True, x0=None,
+                       X_orig=None, show_iqa=True, tvm='tv_chambolle', **_):
+    """``joint_pnp_sci_algo.py:502-664`` (denoiser='tv'): admm_denoise with
+    theta clipped to [0, 1] after the denoiser (``:640``)."""
+    if x0 is None:
+        x0 = At(y)
+    if not isinstance(sigma, list):
+        sigma = [sigma]
+    if not isinstance(iter_max, list):
+        iter_max = [iter_max] * len(sigma)
+    x = x0
+    theta = x0
+    b = np.zeros_like(x0)
+    psnr_all = []
+    for idx, nsig in enumerate(sigma):
+        for it in range(iter_max[idx]):
+            yb = A(theta + b)
+            x = (theta + b) + _lambda * (At((y - yb) / (Phi_sum + gamma)))
+            theta = _tv_step(x - b, tv_weight, tv_iter_max, multichannel, tvm)
+            theta = np.clip(theta, 0, 1)
+            b = b - (x - theta)
+            if show_iqa and X_orig is not None:
+                psnr_all.append(psnr(X_orig, x))
+    psnr_, ssim_ = _frame_metrics(X_orig, x)
+    return x, psnr_, ssim_, psnr_all
+
+
+def _frame_metrics(X_orig, x):
+    psnr_, ssim_ = [], []
+    if X_orig is not None:
+        for imask in range(x.shape[2]):
+            psnr_.append(compare_psnr(X_orig[:, :, imask], x[:, :, imask], data_range=1.))
+            ssim_.append(compare_ssim(X_orig[:, :, imask], x[:, :, imask], data_range=1.))
+    return psnr_, ssim_
+
+
+def gap_multistep_denoise(y, Phi_sum, A, At, cnn, _lambda=1, accelerate=True,
+                          denoiser='tv+ffdnet', iter_max=50, sigma=None, tv_weight=0.1,
+                          tv_iter_max=5, multichannel=True, x0=None, X_orig=None, model=None,
+                          show_iqa=True, tvm='tv_chambolle', **_):
+    """``joint_pnp_sci_algo.py:309-499``: per iteration the GAP(-acc)
+    projection, the TV, then the CNN at this stage's sigma."""
+    if x0 is None:
+        x0 = At(y)
+    if not isinstance(sigma, list):
+        sigma = [sigma]
+    if not isinstance(iter_max, list):
+        iter_max = [iter_max] * len(sigma)
+    y1 = np.zeros_like(y)
+    x = x0
+    psnr_all = []
+    for idx, nsig in enumerate(sigma):
+        for it in range(iter_max[idx]):
+            yb = A(x)
+            if accelerate:
+                y1 = y1 + (y - yb)
+                x = x + _lambda * (At((y1 - yb) / Phi_sum))
+            else:
+                x = x + _lambda * (At((y - yb) / Phi_sum))
+            x = _tv_step(x, tv_weight, tv_iter_max, multichannel, tvm)
+            x = cnn(x, nsig, model)
+            if show_iqa and X_orig is not None:
+                psnr_all.append(psnr(X_orig, x))
+    psnr_, ssim_ = _frame_metrics(X_orig, x)
+    return x, psnr_, ssim_, psnr_all
+
+
+def admm_multistep_denoise(y, Phi_sum, A, At, cnn, _lambda=1, gamma=0.0,
+                           denoiser='tv+ffdnet', iter_max=50, sigma=None, tv_weight=0.1,
+                           tv_iter_max=5, multichannel=True, x0=None, X_orig=None, model=None,
+                           show_iqa=True, tvm='tv_chambolle', **_):
+    """``joint_pnp_sci_algo.py:118-307``: per iteration the ADMM projection,
+    theta = CNN(TV(x - b)), clipped to [0, 1] (``:289``), b -= x - theta."""
+    if x0 is None:
+        x0 = At(y)
+    if not isinstance(sigma, list):
+        sigma = [sigma]
+    if not isinstance(iter_max, list):
+        iter_max = [iter_max] * len(sigma)
+    x = x0
+    theta = x0
+    b = np.zeros_like(x0)
+    psnr_all = []
+    for idx, nsig in enumerate(sigma):
+        for it in range(iter_max[idx]):
+            yb = A(theta + b)
+            x = (theta + b) + _lambda * (At((y - yb) / (Phi_sum + gamma)))
+            theta = _tv_step(x - b, tv_weight, tv_iter_max, multichannel, tvm)
+            theta = cnn(theta, nsig, model)
+            theta = np.clip(theta, 0, 1)
+            b = b - (x - theta)
+            if show_iqa and X_orig is not None:
+                psnr_all.append(psnr(X_orig, x))
+    psnr_, ssim_ = _frame_metrics(X_orig, x)
+    return x, psnr_, ssim_, psnr_all
+
+
+def joint_admmdenoise_cacti(meas, mask, A, At, cnn, projmeth='admm', v0=None, orig=None,
+                            iframe=0, nframe=1, MAXB=1., maskdirection='plain', denoiser='tv',
+                            iter_max1=50, iter_max2=50, sigma1=None, sigma2=None, **args):
+    """``joint_pnp_sci_algo.py:20-59`` with ``gap_joint_denoise`` /
+    ``admm_joint_denoise`` (``:81-116``): per block, ``iter_max1`` TV-only
+    iterations (sigma1), then ``iter_max2`` TV + CNN iterations (sigma2),
+    the second period starting from the first's x."""
+    nrow, ncol, nmask = mask.shape
+    x_ = np.zeros((nrow, ncol, nmask * nframe), dtype=np.float32)
+    psnr_, ssim_, psnrall_ = [], [], []
+    begin_time = time.time()
+    for kf in range(nframe):
+        flip = (maskdirection.lower() == 'updown' and (kf + iframe) % 2 == 1) or \
+               (maskdirection.lower() == 'downup' and (kf + iframe) % 2 == 0)
+        orig_k = None if orig is None else \
+            orig[:, :, (kf + iframe) * nmask:(kf + iframe + 1) * nmask] / MAXB
+        meas_k = meas[:, :, kf + iframe] / MAXB
+        v0_k = None
+        if v0 is not None:
+            v0_k = v0[:, :, kf * nmask:(kf + 1) * nmask]
+            if flip:
+                v0_k = v0_k[:, :, ::-1]
+        mask_sum = np.sum(mask, axis=2)
+        mask_sum[mask_sum == 0] = 1
+        if projmeth.lower() == 'admm':
+            x, _, _, _ = joint_admm_denoise(meas_k, mask_sum, A, At, x0=v0_k, X_orig=orig_k,
+                                            denoiser='tv', iter_max=iter_max1, sigma=sigma1,
+                                            **args)
+            x_k, psnr_k, ssim_k, psnrall_k = admm_multistep_denoise(
+                meas_k, mask_sum, A, At, cnn, x0=x, X_orig=orig_k, denoiser=denoiser,
+                iter_max=iter_max2, sigma=sigma2, **args)
+        elif projmeth.lower() == 'gap':
+            x, _, _, _ = gap_denoise(meas_k, mask_sum, A, At, x0=v0_k, X_orig=orig_k,
+                                     denoiser='tv', iter_max=iter_max1, sigma=sigma1,
+                                     **{k: v for k, v in args.items() if k not in ('gamma',)})
+            x_k, psnr_k, ssim_k, psnrall_k = gap_multistep_denoise(
+                meas_k, mask_sum, A, At, cnn, x0=x, X_orig=orig_k, denoiser=denoiser,
+                iter_max=iter_max2, sigma=sigma2, **args)
+        else:
+            raise ValueError('Unsupported projection method %s' % projmeth.upper())
+        if flip:
+            x_k = x_k[:, :, ::-1]
+            psnr_k = psnr_k[::-1]
+            ssim_k = ssim_k[::-1]
+            psnrall_k = psnrall_k[::-1]
+        t_ = time.time() - begin_time
+        x_[:, :, kf * nmask:(kf + 1) * nmask] = x_k
+        psnr_.extend(psnr_k)
+        ssim_.extend(ssim_k)
+        psnrall_.append(psnrall_k)
+    return x_, t_, psnr_, ssim_, psnrall_

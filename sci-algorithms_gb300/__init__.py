@@ -15,6 +15,8 @@ from .pnp_sci_algo import (admmdenoise_cacti, gap_denoise, admm_denoise,  # noqa
                            GAP_TV_rec, ADMM_TV_rec)
 from .solver import Solver  # noqa: F401
 from .bayer import gap_denoise_bayer, admm_denoise_bayer  # noqa: F401
+from .joint import (joint_admmdenoise_cacti, gap_joint_denoise, admm_joint_denoise,  # noqa: F401
+                    gap_multistep_denoise, admm_multistep_denoise)
 from .cassi import CassiOperator, CassiSolver, make_cassi_ops  # noqa: F401
 from .unrolled import (UnrolledGapTV, unrolled_loss, unrolled_workspace,  # noqa: F401
                        torch_unrolled_loss)

@@ -137,32 +137,29 @@ __global__ void __launch_bounds__(TP / 4) k_proj_gap_tma(
 // ADMM projection (pnp_sci_algo.py:808-812 with a packed mask), same
 // arithmetic as k_proj_admm_smem: t_b = theta_b + b_b, yb = sum_b t_b phi_b,
 // r = (y - yb) / (Phi_sum + gamma), x_b = t_b + lambda (r phi_b),
-// v_b = x_b - b_b; x written when WANT_X.  A tile stages theta and b (2B
-// rows of TP floats) with the same bulk copies and mbarrier scheme.
-template <int TP, bool STAGE_B>
-__device__ __forceinline__ void issue_tile2(float *xs, uint64_t *bars, int buf, int64_t t,
-                                            const float *th, const float *bb, int B, int64_t hw) {
+// v_b = x_b - b_b; x written when WANT_X.  A tile stages theta (B rows of
+// TP floats) with the same bulk copies and mbarrier scheme.
+// theta rows of one ADMM tile (thread 0 only); b is read with 16-byte loads
+// (twice; the second read is served by the caches).  Staging b as well
+// (twice the shared memory per block) measured the same, 0.251 ms at
+// 2048 x 2048 x 24.
+template <int TP>
+__device__ __forceinline__ void issue_theta(float *xs, uint64_t *bars, int buf, int64_t t,
+                                            const float *th, int B, int64_t hw) {
     const int64_t p0 = t * TP;
     const int64_t rem = hw - p0;
     const unsigned n = (unsigned)(rem < TP ? rem : TP);
-    constexpr int R = STAGE_B ? 2 : 1;
-    float *dst = xs + (int64_t)buf * R * B * TP;
-    mbar_expect_tx(bars + buf, (unsigned)R * (unsigned)B * n * 4u);
-    for (int b = 0; b < B; ++b) {
-        bulk_g2s(dst + b * TP, th + b * hw + p0, n * 4u, bars + buf);
-        if (STAGE_B) bulk_g2s(dst + (B + b) * TP, bb + b * hw + p0, n * 4u, bars + buf);
-    }
+    float *dst = xs + (int64_t)buf * B * TP;
+    mbar_expect_tx(bars + buf, (unsigned)B * n * 4u);
+    for (int b = 0; b < B; ++b) bulk_g2s(dst + b * TP, th + b * hw + p0, n * 4u, bars + buf);
 }
 
-// STAGE_B: b is staged with theta; otherwise b is read with 16-byte loads
-// (twice; the second read is served by the caches) and a block needs half
-// the shared memory.
-template <int TP, bool WANT_X, bool STAGE_B>
+template <int TP, bool WANT_X>
 __global__ void __launch_bounds__(TP / 4) k_proj_admm_tma(
     const float *__restrict__ th, const float *__restrict__ bb, const uint32_t *__restrict__ bits,
     const float *__restrict__ y, const float *__restrict__ phisum, float *__restrict__ v,
     float *__restrict__ xo, float lam, float gamma, int B, int64_t hw) {
-    extern __shared__ __align__(128) float xs[];  // [2][2B or B][TP]
+    extern __shared__ __align__(128) float xs[];  // [2][B][TP]: theta
     __shared__ __align__(8) uint64_t bars[2];
     const int tid = threadIdx.x;
     const int64_t ntiles = (hw + TP - 1) / TP;
@@ -176,8 +173,8 @@ __global__ void __launch_bounds__(TP / 4) k_proj_admm_tma(
     __syncthreads();
     const int64_t t0 = blockIdx.x;
     if (tid == 0) {
-        if (t0 < ntiles) issue_tile2<TP, STAGE_B>(xs, bars, 0, t0, th, bb, B, hw);
-        if (t0 + G < ntiles) issue_tile2<TP, STAGE_B>(xs, bars, 1, t0 + G, th, bb, B, hw);
+        if (t0 < ntiles) issue_theta<TP>(xs, bars, 0, t0, th, B, hw);
+        if (t0 + G < ntiles) issue_theta<TP>(xs, bars, 1, t0 + G, th, B, hw);
     }
     int i = 0;
     for (int64_t t = t0; t < ntiles; t += G, ++i) {
@@ -196,12 +193,8 @@ __global__ void __launch_bounds__(TP / 4) k_proj_admm_tma(
         const int q = tid * 4;
         if (p0 + q < hw) {
             const int64_t p = p0 + q;
-            const float *tb = xs + (int64_t)buf * (STAGE_B ? 2 : 1) * B * TP + q;
-            const float *bs = tb + (int64_t)B * TP;
-            auto bload = [&](int b) {
-                return STAGE_B ? *reinterpret_cast<const float4 *>(bs + b * TP)
-                               : ldg4(bb + b * hw + p);
-            };
+            const float *tb = xs + (int64_t)buf * B * TP + q;
+            auto bload = [&](int b) { return ldg4(bb + b * hw + p); };
             const uint4 w = __ldg(reinterpret_cast<const uint4 *>(bits + p));
             float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll 4
@@ -234,7 +227,7 @@ __global__ void __launch_bounds__(TP / 4) k_proj_admm_tma(
         __syncthreads();
         if (tid == 0 && t + 2 * G < ntiles) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-            issue_tile2<TP, STAGE_B>(xs, bars, buf, t + 2 * G, th, bb, B, hw);
+            issue_theta<TP>(xs, bars, buf, t + 2 * G, th, B, hw);
         }
     }
 }
@@ -279,8 +272,8 @@ int launch_proj_gap_tma(const float *x, const uint32_t *bits, const float *y, fl
 }
 
 // ADMM projection with a packed mask (B <= 32, 16-byte aligned planes,
-// hw % 4 == 0); SCI_ERR_UNSUPPORTED otherwise.  Tiles of TP pixels x 2B
-// rows, double-buffered (48 KB at 24 frames and TP = 128).
+// hw % 4 == 0); SCI_ERR_UNSUPPORTED otherwise.  Tiles of TP pixels x B
+// rows, double-buffered (24 KB at 24 frames and TP = 128).
 int launch_proj_admm_tma(const float *th, const float *bb, const uint32_t *bits, const float *y,
                          const float *phisum, float *v, float *xo, float lam, float gamma, int B,
                          int64_t hw, cudaStream_t s) {
@@ -291,19 +284,14 @@ int launch_proj_admm_tma(const float *th, const float *bb, const uint32_t *bits,
     if ((a & 15u) || hw % 4 || B < 1 || B > 32) return SCI_ERR_UNSUPPORTED;
     const char *e = getenv("SCI_PROJ_TP");
     const int tp = e ? atoi(e) : 128;
-    // theta staged, b read with 16-byte loads: staging b as well (twice the
-    // shared memory per block) measured the same, 0.251 ms at 2048^2 x 24
-    const bool stage_b = false;
     auto go = [&](auto tpc) -> int {
         constexpr int TP = decltype(tpc)::value;
-        const size_t smem = sizeof(float) * 2 * (stage_b ? 2 : 1) * (size_t)B * TP;
+        const size_t smem = sizeof(float) * 2 * (size_t)B * TP;
         const int64_t ntiles = (hw + TP - 1) / TP;
         const int64_t per_sm =
             std::max<int64_t>(1, std::min<int64_t>(16, (227 * 1024) / (int64_t)(smem + 1024)));
         const unsigned g = (unsigned)std::min<int64_t>(ntiles, per_sm * kSMs);
-        auto kern = stage_b ? (xo ? k_proj_admm_tma<TP, true, true> : k_proj_admm_tma<TP, false, true>)
-                            : (xo ? k_proj_admm_tma<TP, true, false>
-                                  : k_proj_admm_tma<TP, false, false>);
+        auto kern = xo ? k_proj_admm_tma<TP, true> : k_proj_admm_tma<TP, false>;
         SCI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
         kern<<<g, TP / 4, smem, s>>>(th, bb, bits, y, phisum, v, xo, lam, gamma, B, hw);

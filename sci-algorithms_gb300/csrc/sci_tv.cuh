@@ -49,9 +49,6 @@ constexpr int WPB = 4;             // warps per block
 #define SCI_TV_PF 2                // input prefetch distance in rows (1 or 2)
 #endif
 constexpr int SMAX = 4;            // dual updates per pass
-#ifndef SCI_TV_FRELOAD
-#define SCI_TV_FRELOAD 0           // 1: stages reload f instead of passing it down
-#endif
 constexpr unsigned FULL = 0xffffffffu;
 
 enum { INTERIOR = 0, EDGE = 1 };  // EDGE: band touches a frame edge, or W % 4 != 0
@@ -312,7 +309,7 @@ __device__ __forceinline__ void step(const Pass &P, const St<S, CPL> &in, St<S, 
             }
         }
     }
-    if (S > 0 && (!SCI_TV_FRELOAD || PROJ != 0)) out.fv[0] = fr;
+    if (S > 0) out.fv[0] = fr;
 
     // ---------------- stages 1..S
 #pragma unroll
@@ -330,13 +327,7 @@ __device__ __forceinline__ void step(const Pass &P, const St<S, CPL> &in, St<S, 
             continue;
         }
         const Row<CPL> &up = in.up[k - 1];  // u_{k-1}(i)
-#if SCI_TV_FRELOAD
-        // f(i) reloaded (an L1/L2 hit: the row entered S - k + 1 steps ago)
-        const Row<CPL> fi = (PROJ == 0) ? load_row<CPL, MODE>(fb + (int64_t)i * W, L.col, W, vec)
-                                        : in.fv[k - 1];
-#else
         const Row<CPL> &fi = in.fv[k - 1];  // f(i)
-#endif
         const float uR = __shfl_down_sync(FULL, lo(up.q[0]), 1);
         const bool last_row = GEN && (i == H - 1);
         Row<CPL> gr, gc, n, ri, prn, pcn;
@@ -409,7 +400,7 @@ __device__ __forceinline__ void step(const Pass &P, const St<S, CPL> &in, St<S, 
                 }
             }
         } else {
-            if (!SCI_TV_FRELOAD || PROJ != 0) out.fv[k] = fi;
+            out.fv[k] = fi;
         }
         ucur = uk;
     }
@@ -781,11 +772,8 @@ __device__ __forceinline__ int find_stop(const Pass &P, int frame) {
     return -1;
 }
 
-#ifndef SCI_TV_MINB4
-#define SCI_TV_MINB4 3  // resident blocks per SM, 4 columns per lane
-#endif
 template <int CPL>
-constexpr int min_blocks() { return CPL == 2 ? 4 : SCI_TV_MINB4; }
+constexpr int min_blocks() { return CPL == 2 ? 4 : 3; }
 
 // Main launch of one pass: every frame not yet stopped runs all SG updates.
 template <int SG, bool PIN, bool FINAL, int CPL, int LAG = 1, int PROJ = 0,

@@ -17,7 +17,8 @@ here, so stand-in modules are registered first:
 
 Everything else -- ``A_``, ``At_``, ``psnr``, ``gap_denoise``,
 ``admm_denoise``, ``admmdenoise_cacti``, ``ADMM_TV_rec``,
-``gap_denoise_bayer`` -- is the
+``gap_denoise_bayer`` and the joint TV + CNN loops of
+``joint_pnp_sci_algo.py`` (with a box-blur stand-in for the CNN) -- is the
 reference's code, run on the seeded inputs below in float64.  Each fixture
 stores the inputs and the reference's outputs; ``tests/test_oracle.py``
 checks ``oracle.reference_port`` against them bit for bit, and the GPU tests
@@ -44,6 +45,11 @@ def _not_on_tv_path(*_a, **_k):
     raise NotImplementedError("stand-in: not on the TV path")
 
 
+# the stand-in CNN of the joint fixtures (a 3 x 3 box blur; the FFDNet /
+# FastDVDnet weights are not in the reference tree)
+cnn_stand_in = port.cnn_stand_in
+
+
 def _install_stand_ins():
     def mod(name, **attrs):
         m = types.ModuleType(name)
@@ -67,10 +73,11 @@ def _install_stand_ins():
     pk = mod("packages")
     pk.__path__ = []
     mod("packages.ffdnet").__path__ = []
-    mod("packages.ffdnet.test_ffdnet_ipol", ffdnet_vdenoiser=_not_on_tv_path,
+    # the CNN denoisers: the box-blur stand-in (used by the joint loops only)
+    mod("packages.ffdnet.test_ffdnet_ipol", ffdnet_vdenoiser=cnn_stand_in,
         ffdnet_rgb_denoise=_not_on_tv_path)
     mod("packages.fastdvdnet").__path__ = []
-    mod("packages.fastdvdnet.test_fastdvdnet", fastdvdnet_denoiser=_not_on_tv_path)
+    mod("packages.fastdvdnet.test_fastdvdnet", fastdvdnet_denoiser=cnn_stand_in)
     mod("packages.colour_demosaicing").__path__ = []
     mod("packages.colour_demosaicing.bayer",
         demosaicing_CFA_Bayer_Menon2007=_not_on_tv_path)
@@ -81,15 +88,16 @@ def load_reference(ref_root):
     _install_stand_ins()
     sys.dont_write_bytecode = True
     src = os.path.join(ref_root, "PnP_SCI", "python")
-    for name in ("utils", "pnp_sci_algo"):
+    for name in ("utils", "pnp_sci_algo", "joint_pnp_sci_algo"):
         sys.modules.pop(name, None)
     sys.path.insert(0, src)
     try:
         import utils as ref_utils  # noqa: F401
         import pnp_sci_algo as ref_algo
+        import joint_pnp_sci_algo as ref_joint
     finally:
         sys.path.remove(src)
-    return ref_utils, ref_algo
+    return ref_utils, ref_algo, ref_joint
 
 
 def digest(a):
@@ -103,7 +111,7 @@ def small_video(H, W, B, seed, p=0.5):
 
 
 def main(ref_root):
-    ref_utils, ref = load_reference(ref_root)
+    ref_utils, ref, joint = load_reference(ref_root)
     A_, At_ = ref_utils.A_, ref_utils.At_
     out = {}
 
@@ -215,6 +223,27 @@ def main(ref_root):
         raise RuntimeError("admm_denoise_bayer ran; regenerate its fixture")
     except NameError:
         pass
+
+    # --- joint TV + CNN loops (joint_pnp_sci_algo.py): the CNN denoisers
+    # are the box-blur stand-in (their weights are not in the tree)
+    jorig, jmask = small_video(24, 32, 8, seed=90)
+    jmeas = np.sum(jorig * jmask, axis=2)[..., None]
+    A = lambda xx: A_(xx, jmask)  # noqa: E731
+    At = lambda yy: At_(yy, jmask)  # noqa: E731
+    for projmeth, den in (("gap", "tv+ffdnet"), ("admm", "tv+fastdvdnet")):
+        args = dict(_lambda=1, tv_weight=0.1, tv_iter_max=5, sigma1=[None], sigma2=[0.05],
+                    iter_max1=5, iter_max2=4)
+        if projmeth == "gap":
+            args["accelerate"] = True
+        else:
+            args["gamma"] = 0.02
+        x_, t_, psnr_, ssim_, psnrall_ = joint.joint_admmdenoise_cacti(
+            jmeas, jmask, A, At, projmeth=projmeth, orig=jorig, denoiser=den, **args)
+        out["joint_" + projmeth] = dict(meas=jmeas, mask=jmask, orig=jorig,
+                                        x=x_.astype(np.float64), psnr=np.array(psnr_),
+                                        ssim=np.array(ssim_), psnrall=np.array(psnrall_),
+                                        denoiser=den, args_json=np.array(json.dumps(args)))
+        print("joint", projmeth, "psnr", np.round(np.mean(psnr_), 3))
 
     for name, rec in out.items():
         np.savez_compressed(os.path.join(HERE, name + ".npz"), **rec)

@@ -95,6 +95,23 @@ def test_bayer_admm_is_four_channel_admm(golden):
         assert np.allclose(x[b0::2, b1::2], xc, rtol=0, atol=1e-5)
 
 
+@pytest.mark.parametrize("case", ["joint_gap", "joint_admm"])
+def test_joint_tv_cnn_loops_bit_exact(golden, case):
+    """joint_admmdenoise_cacti (joint_pnp_sci_algo.py) with the box-blur
+    stand-in CNN, against the reference's own run."""
+    g = golden(case)
+    mask = g["mask"]
+    args = json.loads(str(g["args_json"]))
+    x_, _t, psnr_, ssim_, psnrall_ = port.joint_admmdenoise_cacti(
+        g["meas"], mask, lambda x: port.A_(x, mask), lambda y: port.At_(y, mask),
+        port.cnn_stand_in, projmeth=case.split("_")[1], orig=g["orig"],
+        denoiser=str(g["denoiser"]), **args)
+    assert np.array_equal(x_.astype(np.float64), g["x"])
+    assert np.array_equal(np.array(psnr_), g["psnr"])
+    assert np.array_equal(np.array(ssim_), g["ssim"])
+    assert np.array_equal(np.array(psnrall_), g["psnrall"])
+
+
 def test_config0_inputs_and_digest(golden):
     import hashlib
     g = golden("config0")
