@@ -329,6 +329,58 @@ int sci_unrolled_bwd(const float *logits, const float *lambdas,
                      float grad_loss, float *grad_logits, double *grad_lambdas,
                      void *workspace, size_t workspace_bytes, void *stream);
 
+/* ------------------------------------------- CNN denoiser glue (joint/PnP) */
+/* Input / output tensors of the FFDNet and FastDVDnet denoisers built from,
+ * and turned back into, planar float32 frame stacks (nframes x H x W), so
+ * that all frames of a stack go through one batched network call.  The
+ * convolutions themselves run in the caller's framework.  Layouts:
+ * SCI_CNN_NCHW_F32 planar float32; SCI_CNN_NHWC8_BF16 one 16-byte vector
+ * of 8 bfloat16 channels per pixel (unused channels 0).  sigma is a device
+ * float (the noise level), read at run time so that a captured CUDA graph
+ * replays with a new level. */
+#define SCI_CNN_NCHW_F32 0
+#define SCI_CNN_NHWC8_BF16 1
+
+/* FFDNet input: channel 0 = sigma, channel 1 + 2i + j = pixel (i, j) of
+ * each 2 x 2 cell; out is nframes x 5 x ceil(H/2) x ceil(W/2) (NCHW) or
+ * nframes x ceil(H/2) x ceil(W/2) x 8 (NHWC8).  Odd sizes repeat the last
+ * row / column.  Replaces concatenate_input_noise_map
+ * (PnP_SCI/python/packages/ffdnet/functions.py:17-58) as called per frame
+ * by ffdnet_vdenoiser (packages/ffdnet/test_ffdnet_ipol.py:133-169). */
+int sci_cnn_ffdnet_pack(const float *x, int64_t nframes, int64_t H, int64_t W,
+                        const float *sigma, void *out, int layout, void *stream);
+
+/* out = x - depth_to_space(noise), cropped to H x W, clipped to [0, 1] when
+ * clip != 0.  noise: nframes x 4 x ceil(H/2) x ceil(W/2) float32 (NCHW) or
+ * bfloat16 NHWC with `channels` (4 or 8) channels per pixel.  Replaces
+ * upsamplefeatures (packages/ffdnet/functions.py:60-93) and the
+ * subtraction of test_ffdnet_ipol.py:174. */
+int sci_cnn_ffdnet_unpack_sub(const float *x, const void *noise, int64_t nframes,
+                              int64_t H, int64_t W, int layout, int channels,
+                              int clip, float *out, void *stream);
+
+/* FastDVDnet triplet input for the centre frames g = first .. first +
+ * count - 1 of src (nframes x Hs x Ws): channels [src[g-1], sigma, src[g],
+ * sigma, src[g+1], sigma] (frame indices modulo nframes), reflect-padded at
+ * the bottom / right to Hp x Wp (Hp - Hs < Hs, Wp - Ws < Ws).  out: count x
+ * 6 x Hp x Wp (NCHW) or count x Hp x Wp x 8 (NHWC8).  Replaces the window gather, padding and
+ * noise-map concatenation of fastdvdnet_seqdenoise
+ * (packages/fastdvdnet/fastdvdnet.py:117-131) and DenBlock.forward's input
+ * (packages/fastdvdnet/models.py:201). */
+int sci_cnn_window(const float *src, int64_t nframes, int64_t Hs, int64_t Ws,
+                   int64_t Hp, int64_t Wp, int64_t first, int64_t count,
+                   const float *sigma, void *out, int layout, void *stream);
+
+/* out[k] = src[first + k] (reflect-padded as in sci_cnn_window) - r[k],
+ * k < count, cropped to Ho x Wo, clipped to [0, 1] when clip != 0.  r:
+ * count x 1 x Hp x Wp float32 (NCHW) or bfloat16 NHWC with `channels`
+ * channels (channel 0 used).  Replaces DenBlock's `in1 - x` (packages/fastdvdnet/models.py:205)
+ * and the crop of fastdvdnet.py:136-140. */
+int sci_cnn_center_sub(const float *src, int64_t nframes, int64_t Hs, int64_t Ws,
+                       int64_t first, int64_t count, const void *r, int layout,
+                       int channels, int64_t Hp, int64_t Wp, int64_t Ho, int64_t Wo,
+                       int clip, float *out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

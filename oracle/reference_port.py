@@ -23,6 +23,7 @@ import time
 import numpy as np
 from scipy.ndimage import uniform_filter
 
+from . import cnn as _cnn
 from .tv_chambolle import denoise_tv_chambolle
 
 
@@ -119,20 +120,36 @@ def annealed_weights(w0, w1, n):
 
 
 # ---------------------------------------------------------------- L2 solvers
+def _check_denoiser(denoiser, tvm):
+    d = denoiser.lower()
+    if d not in ('tv', 'ffdnet', 'fastdvdnet') or (d == 'tv' and tvm != 'tv_chambolle'):
+        raise ValueError('oracle supports denoiser "tv" (tv_chambolle), "ffdnet", "fastdvdnet"')
+
+
+def _denoise(x, denoiser, w, eps, tv_iter_max, multichannel, nsig, model):
+    """The denoiser switch of gap_denoise / admm_denoise (pnp_sci_algo.py:647-672)."""
+    d = denoiser.lower()
+    if d == 'ffdnet':
+        return _cnn.ffdnet_vdenoiser(x, nsig, model)
+    if d == 'fastdvdnet':
+        return _cnn.fastdvdnet_denoiser(x, nsig, model, gray=True)
+    return denoise_tv_chambolle(x, w, eps=eps, n_iter_max=tv_iter_max, multichannel=multichannel)
+
+
 def gap_denoise(y, Phi_sum, A, At, _lambda=1, accelerate=True,
                 denoiser='tv', iter_max=50, noise_estimate=False, sigma=None,
                 tv_weight=0.1, tv_iter_max=5, multichannel=True, x0=None,
                 X_orig=None, model=None, show_iqa=True, tvm='tv_chambolle',
                 eps=2.e-4, verbose=False):
-    """``PnP_SCI/python/pnp_sci_algo.py:536-706`` with ``denoiser='tv'``.
+    """``PnP_SCI/python/pnp_sci_algo.py:536-706``.
 
     GAP (``:645``) or accelerated GAP (``:641-643``) projection, then the
-    Chambolle TV (``:650``).  ``tv_weight`` / ``_lambda`` may also be
-    sequences indexed by the global iteration (extension).  Only the
-    'tv' / 'tv_chambolle' plug-in exists here.
+    Chambolle TV (``:650``) or, for ``denoiser`` 'ffdnet' / 'fastdvdnet'
+    (``:667-670``), the CNN of ``oracle.cnn`` with ``model`` its parameter
+    dict at the stage's sigma.  ``tv_weight`` / ``_lambda`` may also be
+    sequences indexed by the global iteration (extension).
     """
-    if denoiser.lower() != 'tv' or tvm != 'tv_chambolle':
-        raise ValueError('oracle supports denoiser="tv", tvm="tv_chambolle"')
+    _check_denoiser(denoiser, tvm)
     if x0 is None:
         x0 = At(y)
     if not isinstance(sigma, list):
@@ -153,8 +170,7 @@ def gap_denoise(y, Phi_sum, A, At, _lambda=1, accelerate=True,
                 x = x + lam * (At((y1 - yb) / Phi_sum))
             else:
                 x = x + lam * (At((y - yb) / Phi_sum))
-            x = denoise_tv_chambolle(x, w, eps=eps, n_iter_max=tv_iter_max,
-                                     multichannel=multichannel)
+            x = _denoise(x, denoiser, w, eps, tv_iter_max, multichannel, nsig, model)
             if show_iqa and X_orig is not None:
                 psnr_all.append(psnr(X_orig, x))
                 if verbose and (k + 1) % 5 == 0:
@@ -176,14 +192,14 @@ def admm_denoise(y, Phi_sum, A, At, _lambda=1, gamma=0.01,
                  tv_weight=0.1, tv_iter_max=5, multichannel=True, x0=None,
                  model=None, X_orig=None, show_iqa=True, eps=2.e-4,
                  verbose=False):
-    """``PnP_SCI/python/pnp_sci_algo.py:708-864`` with ``denoiser='tv'``.
+    """``PnP_SCI/python/pnp_sci_algo.py:708-864``.
 
     yb = A(theta + b); x = theta + b + lambda At((y - yb)/(Phi_sum + gamma))
-    (``:808-809``); theta = TV(x - b) (``:812-813``); b = b - (x - theta)
-    (``:836``).  Returns x, not theta (``:864``).
+    (``:808-809``); theta = TV(x - b) (``:812-813``) or the CNN of
+    ``oracle.cnn`` (``:822-825``); b = b - (x - theta) (``:836``).
+    Returns x, not theta (``:864``).
     """
-    if denoiser.lower() != 'tv':
-        raise ValueError('oracle supports denoiser="tv"')
+    _check_denoiser(denoiser, 'tv_chambolle')
     if x0 is None:
         x0 = At(y)
     if not isinstance(sigma, list):
@@ -201,8 +217,7 @@ def admm_denoise(y, Phi_sum, A, At, _lambda=1, gamma=0.01,
             w = _at(tv_weight, k)
             yb = A(theta + b)
             x = (theta + b) + lam * (At((y - yb) / (Phi_sum + gamma)))
-            theta = denoise_tv_chambolle(x - b, w, eps=eps, n_iter_max=tv_iter_max,
-                                         multichannel=multichannel)
+            theta = _denoise(x - b, denoiser, w, eps, tv_iter_max, multichannel, nsig, model)
             b = b - (x - theta)
             if show_iqa and X_orig is not None:
                 psnr_all.append(psnr(X_orig, x))

@@ -17,6 +17,9 @@ from .solver import Solver  # noqa: F401
 from .bayer import gap_denoise_bayer, admm_denoise_bayer  # noqa: F401
 from .joint import (joint_admmdenoise_cacti, gap_joint_denoise, admm_joint_denoise,  # noqa: F401
                     gap_multistep_denoise, admm_multistep_denoise)
+from .cnn import (FFDNet, FastDVDnet, CnnEngine, ffdnet_vdenoiser,  # noqa: F401
+                  fastdvdnet_denoiser, load_checkpoint, load_reference_state_dict,
+                  reference_state_dict)
 from .cassi import CassiOperator, CassiSolver, make_cassi_ops  # noqa: F401
 from .unrolled import (UnrolledGapTV, unrolled_loss, unrolled_workspace,  # noqa: F401
                        torch_unrolled_loss)

@@ -95,6 +95,13 @@ _SIGS = {
                            c_vp],
     "sci_batch_gap_tv": [ctypes.POINTER(BatchItem), ctypes.c_int, ctypes.c_int, ctypes.c_int,
                          c_f, ctypes.c_int, ctypes.c_int, ctypes.c_int, c_vp, c_sz, c_vp],
+    "sci_cnn_ffdnet_pack": [c_vp, c_i64, c_i64, c_i64, c_vp, c_vp, ctypes.c_int, c_vp],
+    "sci_cnn_ffdnet_unpack_sub": [c_vp, c_vp, c_i64, c_i64, c_i64, ctypes.c_int, ctypes.c_int,
+                                  ctypes.c_int, c_vp, c_vp],
+    "sci_cnn_window": [c_vp, c_i64, c_i64, c_i64, c_i64, c_i64, c_i64, c_i64, c_vp, c_vp,
+                       ctypes.c_int, c_vp],
+    "sci_cnn_center_sub": [c_vp, c_i64, c_i64, c_i64, c_i64, c_i64, c_vp, ctypes.c_int,
+                           ctypes.c_int, c_i64, c_i64, c_i64, c_i64, ctypes.c_int, c_vp, c_vp],
     "sci_unrolled_workspace_bytes": [c_i64, c_i64, c_i64, c_i64, ctypes.c_int, ctypes.c_int,
                                      ctypes.POINTER(c_sz)],
     "sci_unrolled_fwd": [c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_i64, ctypes.c_int,

@@ -8,14 +8,15 @@ period is ``gap_multistep_denoise`` ``:309-499`` / ``admm_multistep_denoise``
 ``:118-307``).  The ADMM loops clip theta to [0, 1] after the denoiser.
 
 Here the projections and the TV are this library's kernels on device
-buffers; the CNN is a plug-in: ``model`` is a callable taking a planar
-(frames, H, W) float32 CUDA tensor and the stage's noise level ``nsig`` and
-returning the denoised stack (it stands where the reference calls
-``ffdnet_vdenoiser(x, nsig, model)`` / ``fastdvdnet_denoiser(x, nsig,
-model, gray=True)``; the networks' weights are not part of the reference
-tree, so none ship here).  ``denoiser`` is 'tv+ffdnet' or 'tv+fastdvdnet';
-both call ``model`` the same way.  The TV is the scikit-image Chambolle
-(``tvm='tv_chambolle'``).
+buffers.  ``model`` is the network the reference passes to
+``ffdnet_vdenoiser(x, nsig, model)`` / ``fastdvdnet_denoiser(x, nsig, model,
+gray=True)``: an FFDNet / FastDVDnet built by this package's classes or by
+the reference's (converted on first use), run by ``cnn.CnnEngine`` over the
+whole frame stack at once; any callable taking a planar (frames, H, W)
+float32 CUDA tensor and the stage's ``nsig`` is accepted as well.
+``denoiser`` is 'tv+ffdnet' or 'tv+fastdvdnet'; ``precision`` ('fp32',
+'tf32', 'bf16') selects the network's arithmetic.  The TV is the
+scikit-image Chambolle.
 """
 import time
 
@@ -99,16 +100,39 @@ def _metrics(x, X_orig):
     return frame_psnr(o, x), frame_ssim(o, x)
 
 
+def cnn_step(denoiser, model, precision=None):
+    """(x_planar, nsig, clip) -> denoised planar stack for a CNN denoiser
+    name ('ffdnet' / 'fastdvdnet', with or without 'tv+').  ``model`` is an
+    FFDNet / FastDVDnet network (this package's or the reference's classes;
+    run by the batched CnnEngine) or any callable (x_planar, nsig) ->
+    x_planar."""
+    d = str(denoiser).lower()
+    kind = "ffdnet" if d.endswith("ffdnet") and "fastdvd" not in d else "fastdvdnet"
+    if isinstance(model, torch.nn.Module):
+        from .cnn import engine_for
+        eng = engine_for(model, kind, precision)
+        return lambda x, nsig, clip: eng(x, nsig, clip)
+    if not callable(model):
+        raise TypeError("model must be an FFDNet / FastDVDnet network or a callable "
+                        "(x_planar, nsig) -> x_planar")
+
+    def run(x, nsig, clip):
+        out = model(x, nsig).contiguous()
+        return out.clamp(0, 1) if clip else out
+    return run
+
+
 def _loop(projmeth, y, Phi_sum, A, At, x0, stages, _lambda, gamma, accelerate, tv_weight,
-          tv_iter_max, eps, X_orig, show_iqa, cnn, model, clip):
-    """One period: per iteration the projection, the TV, optionally the CNN
-    at the stage's sigma, and (ADMM) the [0, 1] clip of theta."""
+          tv_iter_max, eps, X_orig, show_iqa, cnn, clip, tv=True):
+    """One period: per iteration the projection, the TV (``tv``), the CNN
+    step ``cnn`` (x, nsig, clip) at the stage's sigma when given, and (ADMM
+    with ``clip``) the [0, 1] clip of theta."""
     y_d = _dev.plane(y)
     ps_d = _dev.plane(Phi_sum)
     ops = _Ops(A, At, y_d, ps_d)
     x = ops.x0() if x0 is None else _dev.planar(x0).clone()
     B, H, W = x.shape
-    ws = tv_workspace(B, H, W, tv_iter_max, x.device)
+    ws = tv_workspace(B, H, W, tv_iter_max, x.device) if tv else None
     orig = None if (X_orig is None or not show_iqa) else _dev.planar(X_orig)
     psnr_all = []
 
@@ -116,14 +140,19 @@ def _loop(projmeth, y, Phi_sum, A, At, x0, stages, _lambda, gamma, accelerate, t
         if orig is not None:
             psnr_all.append(psnr_from_mse(sum_sq_err(orig, v) / v.numel()))
 
+    def denoise(v, nsig, clip_now):
+        if tv:
+            v = tv_frames(v, tv_weight, tv_iter_max, eps, workspace=ws)
+        if cnn is not None:
+            return cnn(v, nsig, clip_now)
+        return v.clamp(0, 1) if clip_now else v
+
     if projmeth == "gap":
         y1 = torch.zeros_like(y_d)
         for iters, nsig in stages:
             for _ in range(int(iters)):
                 xp = ops.gap(x, y1, _lambda, accelerate)
-                x = tv_frames(xp.contiguous(), tv_weight, tv_iter_max, eps, workspace=ws)
-                if cnn:
-                    x = model(x, nsig).contiguous()
+                x = denoise(xp.contiguous(), nsig, False)
                 record(x)
         return x, psnr_all
     theta = x
@@ -131,38 +160,59 @@ def _loop(projmeth, y, Phi_sum, A, At, x0, stages, _lambda, gamma, accelerate, t
     for iters, nsig in stages:
         for _ in range(int(iters)):
             x, v = ops.admm(theta, b, _lambda, gamma)
-            theta = tv_frames(v, tv_weight, tv_iter_max, eps, workspace=ws)
-            if cnn:
-                theta = model(theta, nsig).contiguous()
-            if clip:
-                theta = theta.clamp(0, 1)
+            theta = denoise(v, nsig, clip)
             b = b - (x - theta)
             record(x)
     return x, psnr_all
 
 
-def _check(denoiser, tvm, model, cnn):
-    if tvm != "tv_chambolle":
-        raise ValueError("the joint loops run the scikit-image TV (tvm='tv_chambolle')")
+# TV names each joint loop accepts (joint_pnp_sci_algo.py): the ADMM loops
+# run the scikit-image Chambolle TV for all three (:296-303, :229-236); the
+# GAP loops call denoise_tv_FGP_ITV3D / denoise_tv_cham_ITV2D, which the
+# module never defines (:782-785, :433-436), so only tv_chambolle runs there.
+_TVM_OK = {"gap": ("tv_chambolle",), "admm": ("tv_chambolle", "ITV3D_FGP", "ITV2D_cham")}
+
+
+def _check(denoiser, tvm, model, cnn, projmeth="gap"):
+    if tvm == "tv_bregman":
+        raise ValueError("tvm='tv_bregman' (scikit-image's split-Bregman TV) is not built")
+    if tvm not in _TVM_OK[projmeth]:
+        raise ValueError("the joint %s loops run tvm in %s" % (projmeth, _TVM_OK[projmeth]))
     if cnn:
         if str(denoiser).lower() not in _CNN:
             raise ValueError("Unsupported denoiser {}!".format(denoiser))
-        if not callable(model):
-            raise TypeError("model must be a callable (x_planar, nsig) -> x_planar")
+        if model is None or not (callable(model) or isinstance(model, torch.nn.Module)):
+            raise TypeError("model must be an FFDNet / FastDVDnet network or a callable "
+                            "(x_planar, nsig) -> x_planar")
     elif str(denoiser).lower() != "tv":
         raise ValueError("Unsupported denoiser {}!".format(denoiser))
+
+
+def cnn_denoise(projmeth, y, Phi_sum, A, At, iter_max, sigma, _lambda=1, gamma=0.0,
+                accelerate=True, denoiser='ffdnet', model=None, x0=None, X_orig=None,
+                show_iqa=True, precision=None):
+    """The CNN-denoiser branches of pnp_sci_algo.py's gap_denoise /
+    admm_denoise (``:667-670``, ``:822-825``): per iteration the projection
+    and the network at the stage's sigma; returns (x_planar, psnr_all)."""
+    if model is None:
+        raise ValueError("denoiser %r needs model= (an FFDNet / FastDVDnet network; the "
+                         "trained weights are not part of the reference tree)" % denoiser)
+    step = cnn_step(denoiser, model, precision)
+    return _loop(projmeth, y, Phi_sum, A, At, x0, _stages(iter_max, sigma), _lambda, gamma,
+                 accelerate, 0.1, 1, 0.0, X_orig, show_iqa, step, False, tv=False)
 
 
 def gap_multistep_denoise(y, Phi_sum, A, At, _lambda=1, gamma=None, accelerate=True,
                           denoiser='tv+ffdnet', iter_max=50, noise_estimate=False, sigma=None,
                           tv_weight=0.1, tv_iter_max=5, multichannel=True, x0=None,
                           X_orig=None, model=None, show_iqa=True, tvm='tv_chambolle',
-                          eps=2.e-4):
+                          eps=2.e-4, precision=None):
     """GAP with TV then CNN per iteration (joint_pnp_sci_algo.py:309-499).
     Returns ``(x, psnr_, ssim_, psnr_all)`` (x like y: numpy or torch)."""
-    _check(denoiser, tvm, model, True)
+    _check(denoiser, tvm, model, True, "gap")
     x, pa = _loop("gap", y, Phi_sum, A, At, x0, _stages(iter_max, sigma), _lambda, 0.0,
-                  accelerate, tv_weight, tv_iter_max, eps, X_orig, show_iqa, True, model, False)
+                  accelerate, tv_weight, tv_iter_max, eps, X_orig, show_iqa,
+                  cnn_step(denoiser, model, precision), False)
     p, s = _metrics(x, X_orig)
     return _dev.unplanar(x, y), p, s, pa
 
@@ -170,12 +220,14 @@ def gap_multistep_denoise(y, Phi_sum, A, At, _lambda=1, gamma=None, accelerate=T
 def admm_multistep_denoise(y, Phi_sum, A, At, _lambda=1, gamma=0.0, accelerate=None,
                            denoiser='tv+ffdnet', iter_max=50, noise_estimate=False, sigma=None,
                            tv_weight=0.1, tv_iter_max=5, multichannel=True, x0=None, model=None,
-                           X_orig=None, show_iqa=True, tvm='tv_chambolle', eps=2.e-4):
+                           X_orig=None, show_iqa=True, tvm='tv_chambolle', eps=2.e-4,
+                           precision=None):
     """ADMM with theta = clip(CNN(TV(x - b))) per iteration
     (joint_pnp_sci_algo.py:118-307).  Returns ``(x, psnr_, ssim_, psnr_all)``."""
-    _check(denoiser, tvm, model, True)
+    _check(denoiser, tvm, model, True, "admm")
     x, pa = _loop("admm", y, Phi_sum, A, At, x0, _stages(iter_max, sigma), _lambda, gamma,
-                  True, tv_weight, tv_iter_max, eps, X_orig, show_iqa, True, model, True)
+                  True, tv_weight, tv_iter_max, eps, X_orig, show_iqa,
+                  cnn_step(denoiser, model, precision), True)
     p, s = _metrics(x, X_orig)
     return _dev.unplanar(x, y), p, s, pa
 
@@ -185,7 +237,7 @@ def _admm_tv_clip(y, Phi_sum, A, At, x0, iter_max, sigma, _lambda=1, gamma=0.0, 
     """The first ADMM period: joint_pnp_sci_algo.py's admm_denoise
     (:502-664, denoiser='tv'), theta clipped to [0, 1]."""
     x, _ = _loop("admm", y, Phi_sum, A, At, x0, _stages(iter_max, sigma), _lambda, gamma, True,
-                 tv_weight, tv_iter_max, eps, X_orig, False, False, None, True)
+                 tv_weight, tv_iter_max, eps, X_orig, False, None, True)
     return x
 
 
@@ -194,8 +246,8 @@ def gap_joint_denoise(y, Phi_sum, A, At, x0=None, X_orig=None, denoiser='tv+ffdn
     """TV-only GAP for ``iter_max1`` iterations, then TV + CNN for
     ``iter_max2`` (joint_pnp_sci_algo.py:100-116)."""
     model = args.pop("model", None)
-    _check(denoiser, args.get("tvm", "tv_chambolle"), model, True)
-    first = {k: v for k, v in args.items() if k not in ("gamma", "show_iqa")}
+    _check(denoiser, args.get("tvm", "tv_chambolle"), model, True, "gap")
+    first = {k: v for k, v in args.items() if k not in ("gamma", "show_iqa", "precision")}
     y_d = _dev.plane(y)  # both periods on device buffers
     x, _, _, _ = gap_denoise(y_d, Phi_sum, A, At, x0=x0, X_orig=X_orig, denoiser='tv',
                              iter_max=iter_max1, sigma=sigma1, show_iqa=False, **first)
@@ -210,7 +262,7 @@ def admm_joint_denoise(y, Phi_sum, A, At, x0=None, X_orig=None, denoiser='tv+ffd
     """TV-only ADMM (theta clipped) for ``iter_max1`` iterations, then TV +
     CNN for ``iter_max2`` (joint_pnp_sci_algo.py:81-97)."""
     model = args.pop("model", None)
-    _check(denoiser, args.get("tvm", "tv_chambolle"), model, True)
+    _check(denoiser, args.get("tvm", "tv_chambolle"), model, True, "admm")
     y_d = _dev.plane(y)
     x = _admm_tv_clip(y_d, Phi_sum, A, At, x0, iter_max1, sigma1, **args)
     x, p, s, pa = admm_multistep_denoise(y_d, Phi_sum, A, At, x0=x.permute(1, 2, 0),

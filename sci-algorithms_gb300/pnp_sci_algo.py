@@ -6,7 +6,8 @@ Mirrors ``PnP_SCI/python/pnp_sci_algo.py``: ``admmdenoise_cacti``
 (``:866-907``), for ``denoiser='tv'``: ``tvm='tv_chambolle'`` (the
 scikit-image TV of the Python reference) or one of the MATLAB twin's TV
 denoisers (``tvm`` names of ``PnP_SCI/matlab/algorithms/gapdenoise.m:92-112``,
-with gapdenoise's parameters and iteration counts).
+with gapdenoise's parameters and iteration counts); and for ``denoiser``
+'ffdnet' / 'fastdvdnet' with ``model`` the network (``cnn.py``).
 
 * When ``A`` / ``At`` are the bound methods of one ``MaskOperator`` (from
   ``make_ops(mask)``), the whole iteration loop runs natively
@@ -18,7 +19,8 @@ with gapdenoise's parameters and iteration counts).
 * Extensions: ``tv_weight`` and ``_lambda`` may be per-iteration sequences;
   ``eps`` is the TV stop tolerance.
 * Behavioural differences, on purpose: an unsupported ``projmeth`` or
-  denoiser raises ``ValueError`` (the reference prints and then fails on an
+  denoiser raises ``ValueError`` ('wavelet' and the colour / Bayer CNN
+  variants are not built) (the reference prints and then fails on an
   unbound name, ``:518-519``), and TV errors propagate (the reference
   swallows ``TypeError``, ``:657-658``).
 
@@ -39,10 +41,24 @@ from .cassi import CassiOperator, CassiSolver
 from .utils import MaskOperator, operator_of, psnr_from_mse, sum_sq_err
 
 
+_CNN_DENOISERS = ("ffdnet", "fastdvdnet")
+
+
 def _check_plugin(denoiser, tvm="tv_chambolle"):
-    if str(denoiser).lower() != "tv":
+    d = str(denoiser).lower()
+    if d in _CNN_DENOISERS:
+        return
+    if d != "tv":
         raise ValueError("Unsupported denoiser {}!".format(denoiser))
     tvm_kind(tvm)  # raises ValueError for an unknown name
+
+
+def _cnn_solve(projmeth, y, Phi_sum, A, At, iter_max, sigma, _lambda, gamma, accelerate,
+               denoiser, model, x0, X_orig, show_iqa, precision):
+    from .joint import cnn_denoise
+    return cnn_denoise(projmeth, y, Phi_sum, A, At, iter_max, sigma, _lambda=_lambda,
+                       gamma=gamma, accelerate=accelerate, denoiser=denoiser, model=model,
+                       x0=x0, X_orig=X_orig if show_iqa else None, precision=precision)
 
 
 def _total_iters(iter_max, sigma):
@@ -147,12 +163,19 @@ def _solve_plugin(projmeth, y, ps, A, At, iters, _lambda, tv_weight, tv_iter_max
 def gap_denoise(y, Phi_sum, A, At, _lambda=1, accelerate=True, denoiser='tv', iter_max=50,
                 noise_estimate=False, sigma=None, tv_weight=0.1, tv_iter_max=5,
                 multichannel=True, x0=None, X_orig=None, model=None, show_iqa=True,
-                tvm='tv_chambolle', eps=2.e-4, use_graph=True):
-    """GAP(-acc) with the TV denoiser (``pnp_sci_algo.py:536-706``).
+                tvm='tv_chambolle', eps=2.e-4, use_graph=True, precision=None):
+    """GAP(-acc) with the TV denoiser (``pnp_sci_algo.py:536-706``), or
+    with FFDNet / FastDVDnet (``denoiser`` 'ffdnet' / 'fastdvdnet', ``model``
+    the network, ``sigma`` the per-stage noise levels, ``:667-670``).
 
     Returns ``(x, psnr_, ssim_, psnr_all)`` like the reference.
     """
     _check_plugin(denoiser, tvm)
+    if str(denoiser).lower() in _CNN_DENOISERS:
+        x, psnr_all = _cnn_solve("gap", y, Phi_sum, A, At, iter_max, sigma, _lambda, 0.0,
+                                 accelerate, denoiser, model, x0, X_orig, show_iqa, precision)
+        psnr_, ssim_ = _metrics(x, X_orig, y)
+        return _dev.unplanar(x, y), psnr_, ssim_, psnr_all
     iters = _total_iters(iter_max, sigma)
     x, psnr_all = _solve("gap", y, Phi_sum, A, At, iters, _lambda, tv_weight, tv_iter_max, eps,
                          accelerate, 0.0, x0, X_orig, show_iqa, use_graph, tvm)
@@ -163,9 +186,15 @@ def gap_denoise(y, Phi_sum, A, At, _lambda=1, accelerate=True, denoiser='tv', it
 def admm_denoise(y, Phi_sum, A, At, _lambda=1, gamma=0.01, denoiser='tv', iter_max=50,
                  noise_estimate=False, sigma=None, tv_weight=0.1, tv_iter_max=5,
                  multichannel=True, x0=None, model=None, X_orig=None, show_iqa=True,
-                 tvm='tv_chambolle', eps=2.e-4, use_graph=True):
-    """ADMM with the TV denoiser (``pnp_sci_algo.py:708-864``); returns x."""
+                 tvm='tv_chambolle', eps=2.e-4, use_graph=True, precision=None):
+    """ADMM with the TV denoiser (``pnp_sci_algo.py:708-864``) or FFDNet /
+    FastDVDnet (``:822-825``); returns ``(x, psnr_, ssim_, psnr_all)``."""
     _check_plugin(denoiser, tvm)
+    if str(denoiser).lower() in _CNN_DENOISERS:
+        x, psnr_all = _cnn_solve("admm", y, Phi_sum, A, At, iter_max, sigma, _lambda, gamma,
+                                 True, denoiser, model, x0, X_orig, show_iqa, precision)
+        psnr_, ssim_ = _metrics(x, X_orig, y)
+        return _dev.unplanar(x, y), psnr_, ssim_, psnr_all
     iters = _total_iters(iter_max, sigma)
     x, psnr_all = _solve("admm", y, Phi_sum, A, At, iters, _lambda, tv_weight, tv_iter_max,
                          eps, True, gamma, x0, X_orig, show_iqa, use_graph, tvm)

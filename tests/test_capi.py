@@ -88,8 +88,10 @@ def test_schedule_and_layout_helpers():
     from sci_algorithms_gb300.pnp_sci_algo import _total_iters, _check_plugin, _flip
     assert _total_iters(50, None) == 50
     assert _total_iters([10, 10, 5], [1, 2, 3]) == 25
+    _check_plugin("ffdnet")  # the CNN denoisers run with a model= network
+    _check_plugin("fastdvdnet")
     with pytest.raises(ValueError):
-        _check_plugin("ffdnet")
+        _check_plugin("wavelet")
     _check_plugin("tv", "ATV_ClipA")  # the MATLAB twin's TV names are accepted
     with pytest.raises(ValueError):
         _check_plugin("tv", "ATV_ClipC")

@@ -1,0 +1,200 @@
+"""GPU FFDNet / FastDVDnet denoisers (cnn.CnnEngine: folded batch norm,
+batched frames, the sci_cnn_* glue kernels, CUDA graphs) against the
+reference's own outputs for seeded weights (tests/golden/cnn_*.npz) and
+against the oracle restatement where the reference cannot run (odd sizes,
+padded multi-frame sequences); and the PnP / joint loops with real networks
+against the reference's drivers."""
+import json
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import cnn as ocnn
+import sci_algorithms_gb300 as sci
+from sci_algorithms_gb300 import cnn
+
+pytestmark = pytest.mark.gpu
+
+# relative error of the estimated noise (output - input) per precision
+NOISE_TOL = {"fp32": 1e-4, "tf32": 1e-2, "bf16": 5e-2}
+
+
+def rel(a, b):
+    a, b = np.asarray(a, np.float64), np.asarray(b, np.float64)
+    return np.linalg.norm(a - b) / np.linalg.norm(b)
+
+
+def ref_sd(g):
+    layout = list(zip([str(k) for k in g["keys"]], map(tuple, json.loads(str(g["shapes"])))))
+    sd = ocnn.seeded_state_dict(layout, int(g["seed"]))
+    return {k: torch.from_numpy(np.asarray(v)) for k, v in sd.items()}
+
+
+def ffdnet(golden):
+    return cnn.load_reference_state_dict(sci.FFDNet(1), ref_sd(golden("cnn_ffdnet"))).eval()
+
+
+def fastdvdnet(golden):
+    g = golden("cnn_fastdvdnet")
+    return cnn.load_reference_state_dict(sci.FastDVDnet(5, 1), ref_sd(g)).eval()
+
+
+def noise_rel(out, v, ref):
+    out, v, ref = (np.asarray(a, np.float64) for a in (out, v, ref))
+    return np.linalg.norm(out - ref) / np.linalg.norm(v - ref)
+
+
+@pytest.mark.parametrize("precision", ["fp32", "tf32", "bf16"])
+def test_ffdnet_vdenoiser(golden, precision):
+    g = golden("cnn_ffdnet")
+    x = sci.ffdnet_vdenoiser(g["v"], float(g["sigma"]), model=ffdnet(golden),
+                             precision=precision)
+    assert x.shape == g["v"].shape and x.dtype == np.float32
+    assert noise_rel(x, g["v"], g["x"]) < NOISE_TOL[precision]
+
+
+@pytest.mark.parametrize("case", ["cnn_fastdvdnet", "cnn_fastdvdnet_pad"])
+@pytest.mark.parametrize("precision", ["fp32", "tf32", "bf16"])
+def test_fastdvdnet_denoiser(golden, case, precision):
+    g = golden(case)
+    x = sci.fastdvdnet_denoiser(g["v"], float(g["sigma"]), model=fastdvdnet(golden), gray=True,
+                                precision=precision)
+    assert x.shape == g["v"].shape
+    assert noise_rel(x, g["v"], g["x"]) < NOISE_TOL[precision]
+
+
+@pytest.mark.parametrize("precision", ["fp32", "bf16"])
+def test_fastdvdnet_chunks_and_eager_agree(golden, precision):
+    """Frame chunks of 1, 2 and 3 centres and the eager (non-graph) run give
+    the graph's result."""
+    g = golden("cnn_fastdvdnet")
+    net = fastdvdnet(golden)
+    x = torch.from_numpy(np.moveaxis(g["v"], -1, 0).copy()).float().cuda()
+    full = cnn.CnnEngine(net, "fastdvdnet", precision)(x, 0.1)
+    for per in (1, 2, 3):
+        eng = cnn.CnnEngine(net, "fastdvdnet", precision, graphs=False)
+        eng.chunk_bytes = per * eng._bytes_per_frame(24, 32)
+        got = eng(x, 0.1)
+        assert torch.allclose(got, full, rtol=0, atol=2e-5 if precision == "fp32" else 2e-2)
+
+
+def test_graph_replay_takes_new_sigma_and_clip(golden):
+    g = golden("cnn_ffdnet")
+    net = ffdnet(golden)
+    x = torch.from_numpy(np.moveaxis(g["v"], -1, 0).copy()).float().cuda()
+    eng = cnn.CnnEngine(net, "ffdnet", "fp32")
+    eager = cnn.CnnEngine(net, "ffdnet", "fp32", graphs=False)
+    a = eng(x, 0.05)
+    b = eng(x, 0.2)
+    assert torch.allclose(a, eager(x, 0.05), atol=1e-6)
+    assert torch.allclose(b, eager(x, 0.2), atol=1e-6)
+    assert not torch.allclose(a, b)
+    c = eng(x, 0.2, clip=True)
+    assert torch.equal(c, b.clamp(0, 1))
+
+
+def test_parameter_change_refolds(golden):
+    net = ffdnet(golden).cuda()
+    g = golden("cnn_ffdnet")
+    x = torch.from_numpy(np.moveaxis(g["v"], -1, 0).copy()).float().cuda()
+    eng = cnn.CnnEngine(net, "ffdnet", "fp32")
+    a = eng(x, 0.1)
+    with torch.no_grad():
+        net.convs[-1].weight.mul_(2.0)
+    b = eng(x, 0.1)
+    assert not torch.allclose(a, b)
+    assert torch.allclose(x - b, 2 * (x - a), rtol=1e-4, atol=1e-5)
+
+
+def test_ffdnet_odd_sizes_against_oracle(golden):
+    """Odd frames repeat the last row / column (the reference fails on them)."""
+    g = golden("cnn_ffdnet")
+    v = g["v"][:-1, :-3]  # 23 x 29
+    x = sci.ffdnet_vdenoiser(v, 0.1, model=ffdnet(golden), precision="fp32")
+    vp = np.pad(v, ((0, 1), (0, 1), (0, 0)), mode="edge")
+    p = ocnn.as_float64(ocnn.seeded_state_dict(ocnn.ffdnet_layout(1), int(g["seed"])))
+    ref = ocnn.ffdnet_vdenoiser(vp, 0.1, p)[:-1, :-1]
+    assert noise_rel(x, v, ref) < 1e-4
+
+
+def test_fastdvdnet_padded_sequence_against_oracle(golden):
+    """Several frames of a size that needs padding (the reference re-pads
+    its noise map per frame and fails; the oracle pads each window)."""
+    g = golden("cnn_fastdvdnet")
+    v = np.asarray(g["v"][:22, :30, :5], np.float32).copy()
+    x = sci.fastdvdnet_denoiser(v, 0.1, model=fastdvdnet(golden), gray=True, precision="fp32")
+    p = ocnn.as_float64(ocnn.seeded_state_dict(ocnn.fastdvdnet_layout(1), int(g["seed"])))
+    ref = ocnn.fastdvdnet_denoiser(v, 0.1, p)
+    assert noise_rel(x, v, ref) < 1e-4
+
+
+def _tree(sd):
+    """A module tree with the given (dotted) parameter names, standing in for
+    a network built by the reference's own classes."""
+    root = torch.nn.Module()
+    for k, v in sd.items():
+        parts = k.split(".")
+        m = root
+        for p in parts[:-1]:
+            if not hasattr(m, p):
+                m.add_module(p, torch.nn.Module())
+            m = getattr(m, p)
+        m.register_buffer(parts[-1], v.clone())
+    return root
+
+
+def test_reference_built_model_is_converted(golden):
+    g = golden("cnn_ffdnet")
+    foreign = torch.nn.DataParallel(_tree(ref_sd(g)))
+    x = sci.ffdnet_vdenoiser(g["v"], float(g["sigma"]), model=foreign, precision="fp32")
+    assert noise_rel(x, g["v"], g["x"]) < 1e-4
+    with pytest.raises(ValueError):
+        sci.ffdnet_vdenoiser(g["v"], 0.1, model=None)
+
+
+def test_torch_inputs_stay_on_device(golden):
+    g = golden("cnn_fastdvdnet")
+    v = torch.from_numpy(g["v"]).cuda()
+    x = sci.fastdvdnet_denoiser(v, float(g["sigma"]), model=fastdvdnet(golden), gray=True,
+                                precision="fp32")
+    assert x.is_cuda and noise_rel(x.cpu().numpy(), g["v"], g["x"]) < 1e-4
+
+
+@pytest.mark.parametrize("projmeth", ["gap", "admm"])
+def test_joint_loops_with_networks(golden, projmeth):
+    g = golden("cnn_joint_" + projmeth)
+    net = ffdnet(golden) if projmeth == "gap" else fastdvdnet(golden)
+    A, At = sci.make_ops(g["mask"])
+    x_, _t, psnr_, ssim_, psnrall_ = sci.joint_admmdenoise_cacti(
+        g["meas"], g["mask"], A, At, projmeth=projmeth, orig=g["orig"],
+        denoiser=str(g["denoiser"]), model=net, precision="fp32",
+        **json.loads(str(g["args_json"])))
+    assert rel(x_, g["x"]) < 1e-4
+    assert np.max(np.abs(np.array(psnr_) - g["psnr"])) < 1e-2
+    assert np.max(np.abs(np.array(psnrall_) - g["psnrall"])) < 1e-2
+
+
+@pytest.mark.parametrize("projmeth", ["gap", "admm"])
+def test_pnp_cnn_loops(golden, projmeth):
+    g = golden("cnn_pnp_" + projmeth)
+    net = ffdnet(golden) if projmeth == "gap" else fastdvdnet(golden)
+    A, At = sci.make_ops(g["mask"])
+    x_, _t, psnr_, ssim_, psnrall_ = sci.admmdenoise_cacti(
+        g["meas"], g["mask"], A, At, projmeth=projmeth, orig=g["orig"],
+        denoiser=str(g["denoiser"]), model=net, precision="fp32",
+        **json.loads(str(g["args_json"])))
+    assert rel(x_, g["x"]) < 1e-4
+    assert np.max(np.abs(np.array(psnrall_) - g["psnrall"])) < 1e-2
+
+
+def test_bf16_joint_loop_close(golden):
+    """The bf16 network inside the joint ADMM loop stays near the float32
+    reference run (PSNR within 0.05 dB)."""
+    g = golden("cnn_joint_admm")
+    A, At = sci.make_ops(g["mask"])
+    out = sci.joint_admmdenoise_cacti(
+        g["meas"], g["mask"], A, At, projmeth="admm", orig=g["orig"],
+        denoiser=str(g["denoiser"]), model=fastdvdnet(golden), precision="bf16",
+        **json.loads(str(g["args_json"])))
+    assert np.max(np.abs(np.array(out[2]) - g["psnr"])) < 0.05
