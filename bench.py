@@ -352,6 +352,8 @@ def run_kernel(args):
     from sci_algorithms_gb300._lib import call
     if args.kernel == "unrolled":
         return run_unrolled(args)
+    if args.kernel == "cnn":
+        return run_cnn(args)
     dev = _dev.device()
     F = args.frames
     orig, mask, meas = sci.datasets.video_config(H, W, F, noise_rel=0.01)
@@ -390,6 +392,43 @@ def run_kernel(args):
     torch.cuda.synchronize()
     print(json.dumps({"kernel": args.kernel, "frames": F, "H": H, "W": W,
                       "ms_per_launch": e0.elapsed_time(e1) / args.launches}))
+
+
+def run_cnn(args):
+    """Profiling mode for the CNN denoisers: ``--launches`` eager calls of
+    one network (``--net``, ``--precision``) on a 2048 x 2048 x F stack."""
+    import torch
+    import sci_algorithms_gb300 as sci
+    from sci_algorithms_gb300 import _dev, cnn
+    from oracle import cnn as ocnn  # seeded weights only (test infrastructure)
+    dev = _dev.device()
+    F = args.frames
+    x = _dev.planar(sci.datasets.video_scene(H, W, F, seed=3), dev)
+    if args.net == "ffdnet":
+        net, layout = sci.FFDNet(1), ocnn.ffdnet_layout(1)
+    else:
+        net, layout = sci.FastDVDnet(5, 1), ocnn.fastdvdnet_layout(1)
+    sd = {k: torch.from_numpy(np.asarray(v)) for k, v in ocnn.seeded_state_dict(layout, 7).items()}
+    cnn.load_reference_state_dict(net, sd)
+    eng = cnn.CnnEngine(net.to(dev).eval(), args.net, args.precision, graphs=False)
+    out = torch.empty_like(x)
+    eng.sigma.fill_(0.05)
+    eng.run(x, out)
+    torch.cuda.synchronize()
+    s = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.nvtx.range_push("timed")  # ncu --nvtx-include "timed/" lists these launches
+    e0.record(s)
+    for _ in range(args.launches):
+        eng.run(x, out)
+    e1.record(s)
+    torch.cuda.nvtx.range_pop()
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.launches
+    flops = cnn.conv_flops(net, args.net, F, H, W)
+    print(json.dumps({"kernel": "cnn", "net": args.net, "precision": args.precision,
+                      "frames": F, "H": H, "W": W, "ms_per_call": ms,
+                      "tflops": flops / (ms * 1e-3) / 1e12}))
 
 
 def side_workloads(dev):
@@ -506,7 +545,67 @@ def side_workloads(dev):
     out["bayer"] = {"workload": "gap_tv_bayer_2048x2048x24", "iters": ITERS,
                     "value": ITERS * 1e3 / ms_bay, "unit": "iter/s",
                     "ms_per_call_incl_setup": ms_bay}
+    del yb, mb
+    out["cnn"] = cnn_workload(dev, ev_time)
     return out
+
+
+def cnn_workload(dev, ev_time):
+    """FFDNet / FastDVDnet denoiser calls on the 2048 x 2048 x 24 stack
+    (seeded weights; the trained ones are not in the reference tree), per
+    precision, against the reference's structure run eagerly on the same
+    GPU: one network call per frame (FFDNet) or per output frame with three
+    first-stage DenBlocks each (FastDVDnet), TF32 convolutions, unfolded
+    batch norm -- timed on 4 frames and scaled to 24."""
+    import torch
+    import sci_algorithms_gb300 as sci
+    from sci_algorithms_gb300 import _dev, cnn
+    from oracle import cnn as ocnn  # seeded weights only (test infrastructure)
+    Hs, Ws, Bs = STACK
+    peaks = load_peaks()
+    x = _dev.planar(sci.datasets.video_scene(Hs, Ws, Bs, seed=3), dev)
+    res = {}
+    nets = {"ffdnet": (sci.FFDNet(1), ocnn.ffdnet_layout(1)),
+            "fastdvdnet": (sci.FastDVDnet(5, 1), ocnn.fastdvdnet_layout(1))}
+    for kind, (net, layout) in nets.items():
+        sd = {k: torch.from_numpy(np.asarray(v))
+              for k, v in ocnn.seeded_state_dict(layout, 7).items()}
+        cnn.load_reference_state_dict(net, sd)
+        net = net.to(dev).eval()
+        flops = cnn.conv_flops(net, kind, Bs, Hs, Ws)
+        r = {"tflop_per_call": flops / 1e12}
+        for prec in ("tf32", "bf16"):
+            eng = cnn.CnnEngine(net, kind, prec)
+            ms = ev_time(lambda: eng(x, 0.05), 3, warm=2)
+            r[prec] = {"ms": ms, "tflops": flops / (ms * 1e-3) / 1e12}
+            if peaks.get("bf16_tflops") and prec == "bf16":
+                r[prec]["frac_of_measured_bf16"] = r[prec]["tflops"] / peaks["bf16_tflops"]
+            del eng
+        # the reference's structure: eager per-frame calls, TF32 cuDNN
+        nf = 4
+        sub = x[:nf]
+        with torch.no_grad(), cnn._Prec("tf32"):
+            if kind == "ffdnet":
+                def ref_style():
+                    for f in range(nf):
+                        fr = sub[f][None, None]
+                        fr - net(fr, torch.full((1,), 0.05, device=dev))
+            else:
+                nmap = torch.full((1, 1, Hs, Ws), 0.05, device=dev)
+
+                def ref_style():
+                    for f in range(nf):
+                        idx = torch.tensor([(f + k - 2) % nf for k in range(5)], device=dev)
+                        net(sub[idx][None], nmap)
+            ms_ref = ev_time(ref_style, 2, warm=1) * Bs / nf
+        r["reference_style_tf32_ms"] = ms_ref
+        r["speedup_bf16_vs_reference_style"] = ms_ref / r["bf16"]["ms"]
+        r["speedup_tf32_vs_reference_style"] = ms_ref / r["tf32"]["ms"]
+        res[kind] = r
+        del net
+    torch.cuda.empty_cache()
+    res["workload"] = "cnn_denoise_2048x2048x24"
+    return res
 
 
 def main():
@@ -519,9 +618,12 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the spectral and differentiable side workloads")
-    ap.add_argument("--kernel", choices=["tv", "proj", "proj_admm", "unrolled"], default=None,
+    ap.add_argument("--kernel", choices=["tv", "proj", "proj_admm", "unrolled", "cnn"],
+                    default=None,
                     help="profiling mode: time one kernel on a 2048x2048xFRAMES stack")
     ap.add_argument("--frames", type=int, default=8)
+    ap.add_argument("--net", choices=["ffdnet", "fastdvdnet"], default="ffdnet")
+    ap.add_argument("--precision", choices=["fp32", "tf32", "bf16"], default="bf16")
     ap.add_argument("--launches", type=int, default=3)
     args = ap.parse_args()
     if args.kernel:

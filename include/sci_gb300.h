@@ -381,6 +381,33 @@ int sci_cnn_center_sub(const float *src, int64_t nframes, int64_t Hs, int64_t Ws
                        int channels, int64_t Hp, int64_t Wp, int64_t Ho, int64_t Wo,
                        int clip, float *out, void *stream);
 
+/* FastDVDnet's upsampling and skip connection in one pass, bfloat16 NHWC:
+ * out[n, 2i+a, 2j+b, c] = a[n, 2i+a, 2j+b, c] + u[n, i, j, (2a+b)*C + c]
+ * (a nullable: the shuffle alone).  u is N x h x w x 4C with the
+ * upsampling convolution's output channels ordered sub-pixel-major (its
+ * channel c*4 + 2a + b moved to (2a+b)*C + c); a, out: N x 2h x 2w x C;
+ * C % 8 == 0; 16-byte aligned.  Replaces nn.PixelShuffle(2) of UpBlock
+ * and the additions x1 + x2, x0 + x1 of DenBlock.forward
+ * (packages/fastdvdnet/models.py:72-84, :202-203). */
+int sci_cnn_shuffle_add(const void *a, const void *u, void *out, int64_t N,
+                        int64_t h, int64_t w, int64_t C, void *stream);
+
+/* 3 x 3 convolution (zero padding 1, stride 1) of a thin input on the
+ * tensor cores (tcgen05.mma, float32 accumulation in tensor memory):
+ * out[p, n] = act(bias[n] + sum_{tap, c} in[p + tap offset, c] * w[n, tap*8 + c])
+ * for every pixel p of nframes x H x W.  in: NHWC8 bfloat16 (8 channels =
+ * 16 bytes per pixel, as written by sci_cnn_window / sci_cnn_ffdnet_pack);
+ * weights: N x 80 bfloat16 (k = tap*8 + c with tap = 3*dy + dx, k >= 72
+ * zero); bias: N float32; out: NHWC bfloat16 with N channels; act = ReLU
+ * when relu != 0.  N = 64 or 96.  16-byte aligned buffers.  A timed-out
+ * device-side wait sets bit 0 of the status word of sci_device_status.
+ * Replaces the first convolution of FastDVDnet's DenBlock (InputCvBlock,
+ * packages/fastdvdnet/models.py:29-43, 3 groups of 2 -> 30 channels as
+ * one dense 8 -> 96 filter) and of FFDNet (packages/ffdnet/models.py:37-42). */
+int sci_cnn_conv_thin(const void *in, const void *weights, const float *bias,
+                      void *out, int64_t nframes, int64_t H, int64_t W, int N,
+                      int relu, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

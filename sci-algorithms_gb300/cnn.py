@@ -35,6 +35,7 @@ reference's per-frame loops:
 The trained weights are not part of the reference tree (git-LFS pointers),
 so none ship here: pass ``model`` built from a checkpoint.
 """
+import os
 import weakref
 
 import torch
@@ -281,24 +282,35 @@ def _pad8(n):
 
 
 def _fold(conv, bn, dtype, cin_pad=None, cout_pad=None, cl=False):
-    """(weight, bias) of conv followed by inference batch norm."""
+    """(weight, bias) of conv followed by inference batch norm; bias None
+    for a convolution without batch norm (the networks' convolutions have
+    no bias of their own)."""
     w = conv.weight.detach().float()
     cout = w.shape[0]
+    b = None
     if bn is not None:
         s = bn.weight.detach().float() / torch.sqrt(bn.running_var.detach().float() + bn.eps)
         b = bn.bias.detach().float() - bn.running_mean.detach().float() * s
         w = w * s[:, None, None, None]
-    else:
-        b = torch.zeros(cout, device=w.device)
     if cin_pad is not None and cin_pad > w.shape[1]:
         w = F.pad(w, (0, 0, 0, 0, 0, cin_pad - w.shape[1]))
     if cout_pad is not None and cout_pad > cout:
         w = F.pad(w, (0, 0, 0, 0, 0, 0, 0, cout_pad - cout))
-        b = F.pad(b, (0, cout_pad - cout))
+        if b is not None:
+            b = F.pad(b, (0, cout_pad - cout))
     w = w.to(dtype)
     if cl:
         w = w.contiguous(memory_format=torch.channels_last)
-    return w, b.to(dtype)
+    return w, (None if b is None else b.to(dtype))
+
+
+def _subpixel_major(w):
+    """Output channels c*4 + k of an upsampling convolution (PixelShuffle(2)
+    order) reordered to k*C + c, so that each sub-pixel's C channels are one
+    contiguous vector for sci_cnn_shuffle_add."""
+    C = w.shape[0] // 4
+    perm = torch.tensor([c * 4 + k for k in range(4) for c in range(C)], device=w.device)
+    return w[perm]
 
 
 def _dense_groups(w, groups, cin_total):
@@ -311,11 +323,43 @@ def _dense_groups(w, groups, cin_total):
     return d
 
 
+def _pack_thin(w, b):
+    """(N, 8, 3, 3) weights -> the N x 80 bfloat16 rows of sci_cnn_conv_thin
+    (k = (3 dy + dx) * 8 + c, k >= 72 zero); bias as float32."""
+    N = w.shape[0]
+    wp = torch.zeros(N, 80, dtype=torch.bfloat16, device=w.device)
+    wp[:, :72] = w.float().permute(0, 2, 3, 1).reshape(N, 72).to(torch.bfloat16)
+    bias = b.float() if b is not None else torch.zeros(N, device=w.device)
+    return wp.contiguous(), bias.contiguous()
+
+
+def conv_thin(x, packed, relu=True):
+    """sci_cnn_conv_thin on a bfloat16 NHWC8 tensor given as its
+    channels-last (n, 8, H, W) view; returns the (n, N, H, W) channels-last
+    view of the NHWC output."""
+    wp, bias = packed
+    n, c8, H, W = x.shape
+    xn = x.permute(0, 2, 3, 1)
+    if c8 != 8 or x.dtype != torch.bfloat16 or not xn.is_contiguous():
+        raise ValueError("conv_thin takes a bfloat16 NHWC8 tensor")
+    N = wp.shape[0]
+    out = torch.empty((n, H, W, N), dtype=torch.bfloat16, device=x.device)
+    call("sci_cnn_conv_thin", xn.data_ptr(), wp.data_ptr(), bias.data_ptr(), out.data_ptr(), n,
+         H, W, N, int(relu), _dev.stream_handle())
+    return out.permute(0, 3, 1, 2)
+
+
 _fused_relu_ok = {}
 
 
-def _conv_act(h, w, b, stride=1, groups=1, relu=True):
-    """3 x 3 convolution + bias (+ ReLU, fused by cuDNN where it can)."""
+def _conv_act(h, w, b, stride=1, groups=1, relu=True, tf32=False):
+    """3 x 3 convolution + bias (+ ReLU) through cuDNN's fused
+    convolution-bias-activation op; without bias or ReLU, the plain cuDNN
+    convolution (aten's generic path picks slower kernels for bfloat16
+    NHWC)."""
+    if not relu and b is None:
+        return torch.cudnn_convolution(h, w, (1, 1), (stride, stride), (1, 1), groups, True,
+                                       False, tf32)
     key = (h.dtype, h.is_contiguous(memory_format=torch.channels_last), groups)
     if relu and _fused_relu_ok.get(key, True):
         try:
@@ -342,6 +386,9 @@ class CnnEngine:
         if self.precision not in PRECISIONS:
             raise ValueError("precision must be one of %s" % (PRECISIONS,))
         self.bf16 = self.precision == "bf16"
+        # first layer on the tensor cores by this library's tcgen05 kernel
+        # (bf16 only; SCI_CNN_TC=0 leaves it to cuDNN)
+        self.tc = self.bf16 and os.environ.get("SCI_CNN_TC", "1") != "0"
         self.graphs = graphs
         self.chunk_bytes = chunk_bytes
         self.dev = _dev.device()
@@ -369,6 +416,7 @@ class CnnEngine:
                 cout_pad = 8 if (self.bf16 and i == len(net.convs) - 1) else None
                 layers.append(_fold(conv, bn, dt, cin_pad, cout_pad, cl))
             self.layers = layers
+            self.first_tc = _pack_thin(*layers[0]) if self.tc else None
         else:
             self.blocks = []
             for blk in (net.temp1, net.temp2):
@@ -385,10 +433,16 @@ class CnnEngine:
                         b = F.pad(b, (0, 6))
                         p[name] = (w.to(dt).contiguous(memory_format=torch.channels_last),
                                    b.to(dt))
+                        if self.tc:
+                            p["in0_tc"] = _pack_thin(*p[name])
                     elif self.bf16 and name == "in1":
                         p[name] = _fold(conv, bn, dt, cin_pad=96, cl=True)
                     elif self.bf16 and name == "o1":
                         p[name] = _fold(conv, bn, dt, cout_pad=8, cl=True)
+                    elif self.bf16 and name in ("u2c", "u1c"):
+                        w, b = _fold(conv, bn, dt)
+                        p[name] = (_subpixel_major(w).contiguous(
+                            memory_format=torch.channels_last), b)
                     else:
                         p[name] = _fold(conv, bn, dt, cl=cl)
                 self.blocks.append(p)
@@ -410,8 +464,12 @@ class CnnEngine:
             call("sci_cnn_ffdnet_pack", x.data_ptr(), Fn, H, W, self.sigma.data_ptr(),
                  h.data_ptr(), NCHW_F32, s)
         L = self.layers
+        tf32 = self.precision == "tf32"
         for i, (w, b) in enumerate(L):
-            h = _conv_act(h, w, b, relu=i < len(L) - 1)
+            if i == 0 and self.tc:
+                h = conv_thin(h, self.first_tc)
+            else:
+                h = _conv_act(h, w, b, relu=i < len(L) - 1, tf32=tf32)
         if self.bf16:
             noise = h.permute(0, 2, 3, 1)
             if not noise.is_contiguous():
@@ -426,16 +484,39 @@ class CnnEngine:
     def _denblock(self, p, win):
         """DenBlock body on a prepared window tensor; returns the network
         output r (before `centre - r`)."""
-        g = 1 if self.bf16 else 3
-        x0 = _conv_act(win, *p["in0"], groups=g)
-        x0 = _conv_act(x0, *p["in1"])
-        x1 = _conv_act(_conv_act(_conv_act(x0, *p["d0a"], stride=2), *p["d0b"]), *p["d0c"])
-        x2 = _conv_act(_conv_act(_conv_act(x1, *p["d1a"], stride=2), *p["d1b"]), *p["d1c"])
-        x2 = F.pixel_shuffle(_conv_act(_conv_act(_conv_act(x2, *p["u2a"]), *p["u2b"]),
-                                       *p["u2c"], relu=False), 2)
-        x1 = F.pixel_shuffle(_conv_act(_conv_act(_conv_act(x1 + x2, *p["u1a"]), *p["u1b"]),
-                                       *p["u1c"], relu=False), 2)
-        return _conv_act(_conv_act(x0 + x1, *p["o0"]), *p["o1"], relu=False)
+        tf = self.precision == "tf32"
+
+        def c(x, name, stride=1, groups=1, relu=True):
+            w, b = p[name]
+            return _conv_act(x, w, b, stride, groups, relu, tf)
+
+        if self.tc:
+            x0 = c(conv_thin(win, p["in0_tc"]), "in1")
+        else:
+            x0 = c(c(win, "in0", groups=1 if self.bf16 else 3), "in1")
+        x1 = c(c(c(x0, "d0a", 2), "d0b"), "d0c")
+        x2 = c(c(c(x1, "d1a", 2), "d1b"), "d1c")
+        u2 = c(c(c(x2, "u2a"), "u2b"), "u2c", relu=False)
+        if not self.bf16:
+            x1 = x1 + F.pixel_shuffle(u2, 2)
+            u1 = c(c(c(x1, "u1a"), "u1b"), "u1c", relu=False)
+            return c(c(x0 + F.pixel_shuffle(u1, 2), "o0"), "o1", relu=False)
+        x1 = self._shuffle_add(x1, u2)
+        u1 = c(c(c(x1, "u1a"), "u1b"), "u1c", relu=False)
+        return c(c(self._shuffle_add(x0, u1), "o0"), "o1", relu=False)
+
+    def _shuffle_add(self, a, u):
+        """a + PixelShuffle(2)(u) on bfloat16 NHWC tensors (u's channels in
+        sub-pixel-major order), by sci_cnn_shuffle_add."""
+        N, C, H2, W2 = a.shape
+        an = a.permute(0, 2, 3, 1)
+        un = u.permute(0, 2, 3, 1)
+        an = an if an.is_contiguous() else an.contiguous()
+        un = un if un.is_contiguous() else un.contiguous()
+        out = torch.empty((N, H2, W2, C), dtype=a.dtype, device=a.device)
+        call("sci_cnn_shuffle_add", an.data_ptr(), un.data_ptr(), out.data_ptr(), N, H2 // 2,
+             W2 // 2, C, _dev.stream_handle())
+        return out.permute(0, 3, 1, 2)
 
     def _window(self, src, Hs, Ws, Hp, Wp, first, count):
         s = _dev.stream_handle()
@@ -551,6 +632,28 @@ def engine_for(model, kind, precision=None):
         e = CnnEngine(net, kind, prec)
         per[prec] = e
     return e
+
+
+def conv_flops(model, kind, nframes, H, W):
+    """Multiply-add FLOPs (2 per MAC) of one denoiser call on nframes H x W
+    frames, counted on the network's own layer shapes (grouped convolution
+    at its group size, no channel padding).  FastDVDnet counts the
+    2 * nframes DenBlock evaluations the engine runs (the reference's
+    per-frame loop runs 4 * nframes)."""
+    net = as_native(model, kind)
+
+    def conv(c, h, w):
+        k = c.weight.shape
+        return 2.0 * k[0] * k[1] * k[2] * k[3] * h * w
+
+    if kind == "ffdnet":
+        h, w = (H + 1) // 2, (W + 1) // 2
+        return nframes * sum(conv(c, h, w) for c in net.convs)
+    Hp, Wp = H + (-H) % 4, W + (-W) % 4
+    level = {"in0": 1, "in1": 1, "d0a": 2, "d0b": 2, "d0c": 2, "d1a": 4, "d1b": 4, "d1c": 4,
+             "u2a": 4, "u2b": 4, "u2c": 4, "u1a": 2, "u1b": 2, "u1c": 2, "o0": 1, "o1": 1}
+    per = sum(conv(net.temp1.conv[n], Hp // s, Wp // s) for n, s in level.items())
+    return 2 * nframes * per
 
 
 # ------------------------------------------------- the reference's wrappers

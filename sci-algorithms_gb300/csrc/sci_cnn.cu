@@ -171,6 +171,42 @@ __global__ void k_center_sub(const float *__restrict__ src, int64_t Hs, int64_t 
     }
 }
 
+// ------------------------------------- FastDVDnet upsampling + skip add
+// u: N x h x w x 4C bfloat16 whose channel k*C + c holds sub-pixel k = 2a + b
+// of output channel c (the upsampling convolution's outputs permuted so
+// that each sub-pixel is one contiguous vector); a, out: N x 2h x 2w x C.
+// out[n, 2i+a, 2j+b, c] = a[n, 2i+a, 2j+b, c] + u[n, i, j, (2a+b)*C + c],
+// summed in float32 and rounded to bfloat16.
+__device__ __forceinline__ uint4 add8(uint4 x, uint4 y) {
+    uint4 r;
+    const unsigned *px = reinterpret_cast<const unsigned *>(&x);
+    const unsigned *py = reinterpret_cast<const unsigned *>(&y);
+    unsigned *pr = reinterpret_cast<unsigned *>(&r);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const __nv_bfloat162 a = *reinterpret_cast<const __nv_bfloat162 *>(px + q);
+        const __nv_bfloat162 b = *reinterpret_cast<const __nv_bfloat162 *>(py + q);
+        const __nv_bfloat162 c = __floats2bfloat162_rn(__low2float(a) + __low2float(b),
+                                                       __high2float(a) + __high2float(b));
+        pr[q] = *reinterpret_cast<const unsigned *>(&c);
+    }
+    return r;
+}
+
+__global__ void k_shuffle_add(const uint4 *__restrict__ a, const uint4 *__restrict__ u,
+                              uint4 *__restrict__ out, int64_t N, int64_t h, int64_t w,
+                              int64_t V) {
+    const int64_t n = N * h * w * 4 * V;
+    for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < n;
+         t += int64_t(gridDim.x) * blockDim.x) {
+        const int64_t v = t % V, k = (t / V) % 4, pix = t / (4 * V);
+        const int64_t j = pix % w, i = (pix / w) % h, b = pix / (w * h);
+        const int64_t o = ((b * 2 * h + 2 * i + (k >> 1)) * 2 * w + 2 * j + (k & 1)) * V + v;
+        const uint4 uv = __ldg(u + t);
+        out[o] = a ? add8(__ldg(a + o), uv) : uv;
+    }
+}
+
 int grid_for(int64_t n) {
     int64_t b = (n + kThreads - 1) / kThreads;
     const int64_t cap = int64_t(kSMs) * 16;
@@ -275,6 +311,22 @@ int sci_cnn_center_sub(const float *src, int64_t nframes, int64_t Hs, int64_t Ws
         k_center_sub<false><<<grid_for(n), kThreads, 0, as_stream(stream)>>>(
             src, Hs, Ws, first, count, r, 1, Hp, Wp, Ho, Wo, clip, out);
     SCI_LAUNCHED("k_center_sub");
+    return SCI_OK;
+}
+
+int sci_cnn_shuffle_add(const void *a, const void *u, void *out, int64_t N, int64_t h,
+                        int64_t w, int64_t C, void *stream) {
+    SCI_CHECK_ARG(u && out, "sci_cnn_shuffle_add: null pointer");
+    SCI_CHECK_ARG(N >= 1 && h >= 1 && w >= 1 && C >= 8 && C % 8 == 0,
+                  "sci_cnn_shuffle_add: invalid sizes (C must be a multiple of 8)");
+    SCI_CHECK_ARG(aligned16(u) && aligned16(out) && (!a || aligned16(a)),
+                  "sci_cnn_shuffle_add: buffers must be 16-byte aligned");
+    SCI_CHECK_ARG(out != u, "sci_cnn_shuffle_add: out must not alias u");
+    const int64_t n = N * h * w * 4 * (C / 8);
+    k_shuffle_add<<<grid_for(n), kThreads, 0, as_stream(stream)>>>(
+        reinterpret_cast<const uint4 *>(a), reinterpret_cast<const uint4 *>(u),
+        reinterpret_cast<uint4 *>(out), N, h, w, C / 8);
+    SCI_LAUNCHED("k_shuffle_add");
     return SCI_OK;
 }
 

@@ -309,6 +309,9 @@ namespace sci {
 namespace batch {
 unsigned batch_device_status(bool clear);  // sci_batch.cu
 }
+namespace cnn {
+unsigned cnn_device_status(int clear);  // sci_cnn_tc.cu
+}
 namespace {
 
 // The error path of the bounded waits, on purpose: the barrier expects 16
@@ -345,7 +348,8 @@ extern "C" int sci_selftest_bounded_wait(unsigned int polls, void *stream) {
 
 extern "C" int sci_device_status(unsigned int *status, int clear) {
     SCI_CHECK_ARG(status, "sci_device_status: null pointer");
-    const unsigned int batch = sci::batch::batch_device_status(clear != 0);
+    const unsigned int batch = sci::batch::batch_device_status(clear != 0) |
+                               sci::cnn::cnn_device_status(clear);
     unsigned int v = 0;
     cudaError_t e = cudaMemcpyFromSymbol(&v, sci::g_device_status, sizeof(v));
     if (e != cudaSuccess) return sci::cuda_status(e, "cudaMemcpyFromSymbol");

@@ -4,6 +4,7 @@ reference's own outputs for seeded weights (tests/golden/cnn_*.npz) and
 against the oracle restatement where the reference cannot run (odd sizes,
 padded multi-frame sequences); and the PnP / joint loops with real networks
 against the reference's drivers."""
+import ctypes
 import json
 
 import numpy as np
@@ -13,6 +14,7 @@ import torch
 from oracle import cnn as ocnn
 import sci_algorithms_gb300 as sci
 from sci_algorithms_gb300 import cnn
+from sci_algorithms_gb300._lib import call
 
 pytestmark = pytest.mark.gpu
 
@@ -198,3 +200,42 @@ def test_bf16_joint_loop_close(golden):
         denoiser=str(g["denoiser"]), model=fastdvdnet(golden), precision="bf16",
         **json.loads(str(g["args_json"])))
     assert np.max(np.abs(np.array(out[2]) - g["psnr"])) < 0.05
+
+
+@pytest.mark.parametrize("N,shape", [(96, (2, 37, 53)), (64, (1, 8, 16)), (96, (3, 200, 300)),
+                                     (64, (2, 130, 71))])
+def test_tcgen05_thin_conv_matches_cudnn(N, shape):
+    """sci_cnn_conv_thin (tcgen05, TMEM accumulator) against cuDNN's
+    convolution of the same bfloat16 operands: both accumulate in float32
+    and round to bfloat16, so they agree to a bfloat16 rounding step."""
+    torch.manual_seed(N + shape[1])
+    n, H, W = shape
+    x = torch.randn(n, 8, H, W, device="cuda").to(torch.bfloat16)
+    x = x.contiguous(memory_format=torch.channels_last)
+    w = (torch.randn(N, 8, 3, 3, device="cuda") * 0.2).to(torch.bfloat16)
+    b = torch.randn(N, device="cuda").to(torch.bfloat16)
+    ref = torch.relu(torch.nn.functional.conv2d(x.float(), w.float(), b.float(), padding=1))
+    got = cnn.conv_thin(x, cnn._pack_thin(w, b)).float()
+    assert got.shape == ref.shape
+    err = (got - ref).abs()
+    assert float(err.max()) <= 2 ** -7 * float(ref.abs().max()) + 1e-3
+    assert float(err.mean()) < 4e-3 * float(ref.abs().mean()) + 1e-4
+    got_lin = cnn.conv_thin(x, cnn._pack_thin(w, b), relu=False).float()
+    lin = torch.nn.functional.conv2d(x.float(), w.float(), b.float(), padding=1)
+    assert float((got_lin - lin).abs().max()) <= 2 ** -7 * float(lin.abs().max()) + 1e-3
+    v = ctypes.c_uint(0)
+    call("sci_device_status", ctypes.byref(v), 1)
+    assert v.value == 0
+
+
+def test_tc_and_cudnn_first_layers_agree(golden, monkeypatch):
+    g = golden("cnn_fastdvdnet")
+    net = fastdvdnet(golden)
+    x = torch.from_numpy(np.moveaxis(g["v"], -1, 0).copy()).float().cuda()
+    a = cnn.CnnEngine(net, "fastdvdnet", "bf16", graphs=False)
+    assert a.tc
+    monkeypatch.setenv("SCI_CNN_TC", "0")
+    b = cnn.CnnEngine(net, "fastdvdnet", "bf16", graphs=False)
+    assert not b.tc
+    ra, rb = a(x, 0.1), b(x, 0.1)
+    assert float((ra - rb).abs().max()) < 2e-2
