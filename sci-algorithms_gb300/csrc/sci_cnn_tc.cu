@@ -27,6 +27,8 @@
 // flight, frees its tensor memory and returns.
 #include <cuda_bf16.h>
 
+#include <cstdlib>
+
 #include "sci_bulk.cuh"
 #include "sci_common.cuh"
 
@@ -42,11 +44,14 @@ constexpr int kCore = 128;               // bytes of one core matrix (8 rows x 1
 constexpr int kSBO = kKC * kCore;        // bytes between 8-row groups
 constexpr int kATile = (kM / 8) * kSBO;  // 20 KiB
 constexpr int kTmemCols = 128;
-constexpr int kSmemBytes = 64 * 1024;    // requested per block: at most 3 blocks per SM
+// shared memory requested per block: 64 KiB with one A buffer (3 blocks per
+// SM), 100 KiB with two (2 blocks per SM)
+template <int NBUF>
+__host__ __device__ constexpr int smem_bytes() { return NBUF == 1 ? 64 * 1024 : 100 * 1024; }
 
-template <int N>
+template <int N, int NBUF>
 struct alignas(1024) TcSmem {
-    uint8_t a[kATile];
+    uint8_t a[NBUF][kATile];
     uint8_t b[(N / 8) * kSBO];
     uint8_t stage[kM * N * 2];  // the tile's output, pixel-major (NHWC)
     float bias[N];
@@ -125,18 +130,37 @@ __device__ __forceinline__ void cp_async16(void *dst, const void *src) {
                  : "memory");
 }
 
-template <int N>
-__global__ void __launch_bounds__(kThr, 3)
+// One im2col row (this thread's pixel p, 9 taps) of a tile into an A buffer:
+// cp.async for taps inside the frame, zeros outside.
+__device__ __forceinline__ void gather_row(const uint4 *__restrict__ in, uint8_t *arow,
+                                           int64_t p, int64_t P, int64_t H, int64_t W) {
+    if (p >= P) return;  // rows past the end keep stale data; their results are not stored
+    const int64_t x = p % W, y = (p / W) % H, f = p / (W * H);
+#pragma unroll
+    for (int tap = 0; tap < 9; ++tap) {
+        const int64_t yy = y + tap / 3 - 1, xx = x + tap % 3 - 1;
+        uint8_t *dst = arow + tap * kCore;
+        if (yy >= 0 && yy < H && xx >= 0 && xx < W)
+            cp_async16(dst, in + (f * H + yy) * W + xx);
+        else
+            *reinterpret_cast<uint4 *>(dst) = make_uint4(0u, 0u, 0u, 0u);
+    }
+}
+
+// NBUF = 2: the gather of the block's next tile is issued before the
+// current tile's MMAs and epilogue, so its latency overlaps them.
+template <int N, int NBUF>
+__global__ void __launch_bounds__(kThr, NBUF == 1 ? 3 : 2)
     k_conv_thin_tc(const uint4 *__restrict__ in, const uint4 *__restrict__ wts,
                    const float *__restrict__ bias, uint4 *__restrict__ out, int64_t F,
                    int64_t H, int64_t W, int relu) {
     static_assert(N % 32 == 0 && N >= 32 && N <= 256, "N: multiple of 32 up to 256");
-    static_assert(sizeof(TcSmem<N>) + 1024 <= kSmemBytes, "shared memory layout too large");
+    static_assert(sizeof(TcSmem<N, NBUF>) + 1024 <= smem_bytes<NBUF>(),
+                  "shared memory layout too large");
     extern __shared__ uint8_t smem_raw[];
-    TcSmem<N> &s = *reinterpret_cast<TcSmem<N> *>(
+    TcSmem<N, NBUF> &s = *reinterpret_cast<TcSmem<N, NBUF> *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const int tid = threadIdx.x, warp = tid >> 5;
-    const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
 
     // weights into the core-matrix layout; the zero K chunk of A
     for (int i = tid; i < N * kKC; i += kThr) {
@@ -144,7 +168,10 @@ __global__ void __launch_bounds__(kThr, 3)
         *reinterpret_cast<uint4 *>(s.b + (n >> 3) * kSBO + kc * kCore + (n & 7) * 16) = wts[i];
     }
     for (int i = tid; i < N; i += kThr) s.bias[i] = bias[i];
-    *reinterpret_cast<uint4 *>(s.a + (tid >> 3) * kSBO + 9 * kCore + (tid & 7) * 16) = zero;
+    const int row_off = (tid >> 3) * kSBO + (tid & 7) * 16;
+#pragma unroll
+    for (int b = 0; b < NBUF; ++b)
+        *reinterpret_cast<uint4 *>(s.a[b] + row_off + 9 * kCore) = make_uint4(0u, 0u, 0u, 0u);
     if (tid == 0) {
         mbar_init(&s.bar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -161,32 +188,33 @@ __global__ void __launch_bounds__(kThr, 3)
     __syncthreads();
     tc_fence_after();
     const uint32_t tmem = s.tmem;
-    const uint32_t a_addr = smem_u32(s.a), b_addr = smem_u32(s.b);
+    const uint32_t b_addr = smem_u32(s.b);
     const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
-    uint8_t *arow = s.a + (tid >> 3) * kSBO + (tid & 7) * 16;
 
     const int64_t P = F * H * W, ntiles = (P + kM - 1) / kM;
     unsigned phase = 0;
-    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+    if (NBUF == 2) {
+        gather_row(in, s.a[0] + row_off, blockIdx.x * kM + tid, P, H, W);
+        asm volatile("cp.async.commit_group;" ::: "memory");
+    }
+    int buf = 0;
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, buf ^= (NBUF - 1)) {
         const int64_t p = tile * kM + tid;
-        if (p < P) {
-            const int64_t x = p % W, y = (p / W) % H, f = p / (W * H);
-#pragma unroll
-            for (int tap = 0; tap < 9; ++tap) {
-                const int64_t yy = y + tap / 3 - 1, xx = x + tap % 3 - 1;
-                uint8_t *dst = arow + tap * kCore;
-                if (yy >= 0 && yy < H && xx >= 0 && xx < W)
-                    cp_async16(dst, in + (f * H + yy) * W + xx);
-                else
-                    *reinterpret_cast<uint4 *>(dst) = zero;
-            }
-        }  // rows past the end keep stale data; their results are not stored
-        asm volatile("cp.async.wait_all;" ::: "memory");
+        if (NBUF == 2) {
+            const int64_t nxt = tile + gridDim.x;
+            if (nxt < ntiles) gather_row(in, s.a[buf ^ 1] + row_off, nxt * kM + tid, P, H, W);
+            asm volatile("cp.async.commit_group;" ::: "memory");
+            asm volatile("cp.async.wait_group 1;" ::: "memory");  // this tile's copies
+        } else {
+            gather_row(in, s.a[0] + row_off, p, P, H, W);
+            asm volatile("cp.async.wait_all;" ::: "memory");
+        }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         tc_fence_before();  // the previous tile's tcgen05.ld before the barrier
         __syncthreads();
         tc_fence_after();
         if (tid == 0) {
+            const uint32_t a_addr = smem_u32(s.a[buf]);
 #pragma unroll
             for (int kk = 0; kk < kKC / 2; ++kk)
                 tc_mma(tmem, smem_desc(a_addr + kk * 2 * kCore), smem_desc(b_addr + kk * 2 * kCore),
@@ -208,25 +236,23 @@ __global__ void __launch_bounds__(kThr, 3)
         for (int c0 = 0; c0 < N; c0 += 32) {
             uint32_t r[32];
             tc_ld32(lane_base + (uint32_t)c0, r);
-            {
-                uint4 *o = srow + c0 / 8;
+            uint4 *o = srow + c0 / 8;
 #pragma unroll
-                for (int q = 0; q < 4; ++q) {
-                    uint32_t w4[4];
+            for (int q = 0; q < 4; ++q) {
+                uint32_t w4[4];
 #pragma unroll
-                    for (int e = 0; e < 4; ++e) {
-                        const int j = q * 8 + e * 2;
-                        float v0 = __uint_as_float(r[j]) + s.bias[c0 + j];
-                        float v1 = __uint_as_float(r[j + 1]) + s.bias[c0 + j + 1];
-                        if (relu) {
-                            v0 = fmaxf(v0, 0.f);
-                            v1 = fmaxf(v1, 0.f);
-                        }
-                        const __nv_bfloat162 h = __floats2bfloat162_rn(v0, v1);
-                        w4[e] = *reinterpret_cast<const uint32_t *>(&h);
+                for (int e = 0; e < 4; ++e) {
+                    const int j = q * 8 + e * 2;
+                    float v0 = __uint_as_float(r[j]) + s.bias[c0 + j];
+                    float v1 = __uint_as_float(r[j + 1]) + s.bias[c0 + j + 1];
+                    if (relu) {
+                        v0 = fmaxf(v0, 0.f);
+                        v1 = fmaxf(v1, 0.f);
                     }
-                    o[q] = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+                    const __nv_bfloat162 h = __floats2bfloat162_rn(v0, v1);
+                    w4[e] = *reinterpret_cast<const uint32_t *>(&h);
                 }
+                o[q] = make_uint4(w4[0], w4[1], w4[2], w4[3]);
             }
         }
         // the staged tile -> global memory in one bulk copy
@@ -237,6 +263,7 @@ __global__ void __launch_bounds__(kThr, 3)
             bulk_s2g(out + tile * kM * (N / 8), s.stage, (unsigned)(rows * N * 2));
         }
     }
+    asm volatile("cp.async.wait_all;" ::: "memory");  // no copy may land after the block ends
     if (tid == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
     tc_fence_before();
     __syncthreads();
@@ -246,19 +273,34 @@ __global__ void __launch_bounds__(kThr, 3)
                      : "memory");
 }
 
-template <int N>
+template <int N, int NBUF>
 int launch_thin(const void *in, const void *wts, const float *bias, void *out, int64_t F,
                 int64_t H, int64_t W, int relu, cudaStream_t st) {
     const int64_t ntiles = (F * H * W + kM - 1) / kM;
-    const int64_t cap = int64_t(kSMs) * 3;
+    const int64_t cap = int64_t(kSMs) * (NBUF == 1 ? 3 : 2);
     const int grid = int(ntiles < cap ? ntiles : cap);
-    SCI_CUDA(cudaFuncSetAttribute(k_conv_thin_tc<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  kSmemBytes));
-    k_conv_thin_tc<N><<<grid, kThr, kSmemBytes, st>>>(
+    SCI_CUDA(cudaFuncSetAttribute(k_conv_thin_tc<N, NBUF>,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  smem_bytes<NBUF>()));
+    k_conv_thin_tc<N, NBUF><<<grid, kThr, smem_bytes<NBUF>(), st>>>(
         reinterpret_cast<const uint4 *>(in), reinterpret_cast<const uint4 *>(wts), bias,
         reinterpret_cast<uint4 *>(out), F, H, W, relu);
     SCI_LAUNCHED("k_conv_thin_tc");
     return SCI_OK;
+}
+
+template <int N>
+int launch_thin_n(const void *in, const void *wts, const float *bias, void *out, int64_t F,
+                  int64_t H, int64_t W, int relu, cudaStream_t st) {
+    // one A buffer and 3 blocks per SM: 1.99 ms for 8 x 2048 x 2048 -> 96
+    // channels; two buffers (next gather overlapping) and 2 blocks per SM:
+    // 2.37 ms (SCI_THIN_NBUF=2)
+    static const int nbuf = [] {
+        const char *e = getenv("SCI_THIN_NBUF");
+        return (e && e[0] == '2') ? 2 : 1;
+    }();
+    if (nbuf == 1) return launch_thin<N, 1>(in, wts, bias, out, F, H, W, relu, st);
+    return launch_thin<N, 2>(in, wts, bias, out, F, H, W, relu, st);
 }
 
 }  // namespace
@@ -288,8 +330,8 @@ extern "C" int sci_cnn_conv_thin(const void *in, const void *weights, const floa
                   "sci_cnn_conv_thin: in, weights and out must be 16-byte aligned");
     const cudaStream_t st = as_stream(stream);
     switch (N) {
-        case 64: return launch_thin<64>(in, weights, bias, out, nframes, H, W, relu, st);
-        case 96: return launch_thin<96>(in, weights, bias, out, nframes, H, W, relu, st);
+        case 64: return launch_thin_n<64>(in, weights, bias, out, nframes, H, W, relu, st);
+        case 96: return launch_thin_n<96>(in, weights, bias, out, nframes, H, W, relu, st);
         default:
             set_error("sci_cnn_conv_thin: N = %d (64 or 96)", N);
             return SCI_ERR_UNSUPPORTED;
