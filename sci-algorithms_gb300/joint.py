@@ -20,7 +20,6 @@ scikit-image Chambolle.
 """
 import time
 
-import numpy as np
 import torch
 
 from . import _dev
@@ -289,7 +288,9 @@ def joint_admmdenoise_cacti(meas, mask, A, At, projmeth='admm', v0=None, orig=No
         mask_sum = msk.sum(dim=0)
         mask_sum = torch.where(mask_sum == 0, torch.ones_like(mask_sum), mask_sum)
     fn = admm_joint_denoise if projmeth.lower() == 'admm' else gap_joint_denoise
-    outs, psnr_, ssim_, psnrall_ = [], [], [], []
+    torch_in = _dev.is_torch(meas)
+    psnr_, ssim_, psnrall_ = [], [], []
+    x_dev = None  # the H x W x (B nframe) result, assembled on the device
     begin = time.time()
     t_ = 0.0
     for kf in range(nframe):
@@ -297,6 +298,8 @@ def joint_admmdenoise_cacti(meas, mask, A, At, projmeth='admm', v0=None, orig=No
         flip = (maskdirection.lower() == 'updown' and k % 2 == 1) or \
                (maskdirection.lower() == 'downup' and k % 2 == 0)
         meas_k = meas[..., k] / MAXB
+        if not torch_in:
+            meas_k = _dev.plane(meas_k)  # block results stay on the device
         orig_k = None if orig is None else orig[..., k * nmask:(k + 1) * nmask] / MAXB
         v0_k = None
         if v0 is not None:
@@ -308,15 +311,21 @@ def joint_admmdenoise_cacti(meas, mask, A, At, projmeth='admm', v0=None, orig=No
                                             iter_max2=iter_max2, sigma1=sigma1, sigma2=sigma2,
                                             **dict(args))
         if flip:
-            x_k = x_k.flip(-1) if _dev.is_torch(x_k) else x_k[..., ::-1]
+            x_k = x_k.flip(-1)
             psnr_k, ssim_k, psnrall_k = psnr_k[::-1], ssim_k[::-1], psnrall_k[::-1]
+        if x_dev is None:
+            x_dev = torch.empty((*x_k.shape[:-1], nmask * nframe), dtype=torch.float32,
+                                device=x_k.device)
+        x_dev[..., kf * nmask:(kf + 1) * nmask] = x_k
+        torch.cuda.synchronize()
         t_ = time.time() - begin
-        outs.append(x_k)
         psnr_.extend(psnr_k)
         ssim_.extend(ssim_k)
         psnrall_.append(psnrall_k)
-    if _dev.is_torch(meas):
-        x_ = torch.cat([o if _dev.is_torch(o) else torch.from_numpy(o) for o in outs], dim=-1)
+    if torch_in:
+        x_ = x_dev
     else:
-        x_ = np.concatenate([np.asarray(o, np.float32) for o in outs], axis=-1)
+        x_host = torch.empty(x_dev.shape, dtype=torch.float32, pin_memory=True)
+        x_host.copy_(x_dev)
+        x_ = x_host.numpy()
     return x_, t_, psnr_, ssim_, psnrall_

@@ -27,7 +27,6 @@ with gapdenoise's parameters and iteration counts); and for ``denoiser``
 Outputs follow the measurement's kind: numpy in -> numpy float32 out; torch
 in -> CUDA tensors out.
 """
-import math
 import time
 
 import numpy as np
@@ -225,13 +224,15 @@ def admmdenoise_cacti(meas, mask, A, At, projmeth='admm', v0=None, orig=None, if
         msk = _dev.planar(mask)
         mask_sum = msk.sum(dim=0)
         mask_sum = torch.where(mask_sum == 0, torch.ones_like(mask_sum), mask_sum)
-    outs = []
     psnr_, ssim_, psnrall_ = [], [], []
+    x_dev = None  # the H x W x (B nframe) result, assembled on the device
     begin = time.time()
     t_ = 0.0
     for kf in range(nframe):
         k = kf + iframe
         meas_k = meas[..., k] / MAXB
+        if not torch_in:
+            meas_k = _dev.plane(meas_k)  # block results stay on the device
         orig_k = None if orig is None else orig[..., k * nmask:(k + 1) * nmask] / MAXB
         v0_k = None
         if v0 is not None:
@@ -242,18 +243,23 @@ def admmdenoise_cacti(meas, mask, A, At, projmeth='admm', v0=None, orig=None, if
         x_k, psnr_k, ssim_k, psnrall_k = fn(meas_k, mask_sum, A, At, x0=v0_k, X_orig=orig_k,
                                             **args)
         if _flip(maskdirection, k):
-            x_k = x_k.flip(-1) if _dev.is_torch(x_k) else x_k[..., ::-1]
+            x_k = x_k.flip(-1)
             psnr_k, ssim_k, psnrall_k = psnr_k[::-1], ssim_k[::-1], psnrall_k[::-1]
+        if x_dev is None:
+            x_dev = torch.empty((*x_k.shape[:-1], nmask * nframe), dtype=torch.float32,
+                                device=x_k.device)
+        x_dev[..., kf * nmask:(kf + 1) * nmask] = x_k
+        torch.cuda.synchronize()
         t_ = time.time() - begin
-        outs.append(x_k)
         psnr_.extend(psnr_k)
         ssim_.extend(ssim_k)
         psnrall_.append(psnrall_k)
     if torch_in:
-        x_ = torch.cat([o.to(torch.float32) for o in outs], dim=-1)
-    else:
-        x_ = np.concatenate([np.asarray(o, dtype=np.float32) for o in outs], axis=-1)
-    return x_, t_, psnr_, ssim_, psnrall_
+        return x_dev, t_, psnr_, ssim_, psnrall_
+    # one copy of the whole result into page-locked host memory
+    x_host = torch.empty(x_dev.shape, dtype=torch.float32, pin_memory=True)
+    x_host.copy_(x_dev)
+    return x_host.numpy(), t_, psnr_, ssim_, psnrall_
 
 
 # ------------------------------------------------------------- legacy loops

@@ -5,7 +5,8 @@ and calls ``sci_gap_tv`` / ``sci_admm_tv``, which enqueue (and, by default,
 replay as one cached CUDA graph) every iteration of
 ``gap_denoise`` / ``admm_denoise`` (``PnP_SCI/python/pnp_sci_algo.py:536-864``).
 ``Solver.run_host`` is the end-to-end entry: pinned host inputs in, host
-result out.
+result out; ``Solver.run_host_many`` pipelines a sequence of measurements
+(the copy-out of one overlaps the solve of the next).
 """
 import ctypes
 import math
@@ -104,6 +105,44 @@ class Solver:
             mse = s / n
             out.append(100 if mse == 0 else 20 * math.log10(1.0 / math.sqrt(mse)))
         return out
+
+    def run_host_many(self, y_hosts, x_hosts):
+        """End to end over a sequence of measurements (the frame-block loop of
+        ``admmdenoise_cacti``): each pinned host measurement (H, W) is copied
+        in and solved on the current stream while the previous result is
+        copied back into its pinned ``x_hosts[k]`` (B, H, W) on a second
+        stream.  Two device result slots alternate; a slot is reused only
+        after its copy-out has finished.  Returns when every result is on
+        the host."""
+        if len(y_hosts) != len(x_hosts):
+            raise ValueError("one host result buffer per measurement")
+        dev = self.op.dev
+        if getattr(self, "_slots", None) is None:
+            self._slots = [torch.empty((self.B, self.H, self.W), dtype=torch.float32, device=dev)
+                           for _ in range(2)]
+            self._y_slots = [torch.empty((self.H, self.W), dtype=torch.float32, device=dev)
+                             for _ in range(2)]
+            self._copy_stream = torch.cuda.Stream(device=dev)
+        main = torch.cuda.current_stream()
+        copy = self._copy_stream
+        freed = [None, None]  # events: copy-out of each slot finished
+        for k, (yh, xh) in enumerate(zip(y_hosts, x_hosts)):
+            s = k % 2
+            if freed[s] is not None:
+                main.wait_event(freed[s])
+            y = self._y_slots[s]
+            y.copy_(yh, non_blocking=True)
+            x = self.run(y, out=self._slots[s])
+            solved = torch.cuda.Event()
+            solved.record(main)
+            copy.wait_event(solved)
+            with torch.cuda.stream(copy):
+                xh.copy_(x, non_blocking=True)
+            freed[s] = torch.cuda.Event()
+            freed[s].record(copy)
+        copy.synchronize()
+        main.synchronize()
+        return x_hosts
 
     def run_host(self, y_host, x_host=None):
         """End to end: copy a pinned host measurement (H, W) in, solve, copy
