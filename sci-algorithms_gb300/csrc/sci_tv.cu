@@ -119,6 +119,7 @@ static int choose_cpl(int64_t W) {
 struct RuleArgs {
     int rule = tv::RULE_SKIMAGE;
     float tau = 0.f, tw = 0.f, c1 = 0.f, c2 = 0.f;
+    float *tape_p = nullptr, *tape_u = nullptr;  // single-pass tape (sci_tv_tape.cu)
 };
 
 static int tv_launch_core(const float *f, float *u, float *resid, int64_t nf, int64_t H,
@@ -126,9 +127,13 @@ static int tv_launch_core(const float *f, float *u, float *resid, int64_t nf, in
                           double *energy_out, void *workspace, size_t ws_bytes, cudaStream_t s,
                           int force_R, int flags, const uint32_t *proj_bits, const float *proj_c,
                           float proj_lam, const RuleArgs &ra) {
-    const bool no_stop = (flags & 1) != 0 || ra.rule != tv::RULE_SKIMAGE;
+    const bool tape = ra.tape_p != nullptr;
+    const bool no_stop = (flags & 1) != 0 || ra.rule != tv::RULE_SKIMAGE || tape;
     const bool proj = proj_bits != nullptr;
     using namespace tv;
+    SCI_CHECK_ARG(!tape || (ra.tape_u && K >= 2 && K - 1 <= SMAX && !proj && !resid &&
+                            ra.rule == RULE_SKIMAGE),
+                  "tv: a tape needs one pass (2 <= K <= 5), no projection, no resid");
     SCI_CHECK_ARG(f && u && nf >= 1 && H >= 1 && W >= 1, "tv: bad arguments");
     SCI_CHECK_ARG(K >= 1, "tv: n_iter_max must be >= 1");
     SCI_CHECK_ARG(weight > 0.f, "tv: weight must be > 0 (got %g)", (double)weight);
@@ -162,7 +167,7 @@ static int tv_launch_core(const float *f, float *u, float *resid, int64_t nf, in
 
     // the on-load projection and the MATLAB rules are built for 4 columns
     const int cpl = (proj || ra.rule != RULE_SKIMAGE) ? 4 : choose_cpl(W);
-    const int lag = (proj || ra.rule != RULE_SKIMAGE) ? 1 : choose_lag();
+    const int lag = (proj || tape || ra.rule != RULE_SKIMAGE) ? 1 : choose_lag();
     const bool vec = (W % cpl == 0) && (fs % cpl == 0) &&
                      ((reinterpret_cast<uintptr_t>(f) | reinterpret_cast<uintptr_t>(u) |
                        reinterpret_cast<uintptr_t>(resid)) % (4 * cpl) == 0);
@@ -213,9 +218,13 @@ static int tv_launch_core(const float *f, float *u, float *resid, int64_t nf, in
         P.nchunks = (int)((H + P.R - 1) / P.R);
         P.S = SG;
         P.vec = vec ? 1 : 0;
+        P.tape_p = ra.tape_p;
+        P.tape_u = ra.tape_u;
         const int per_frame_blocks = (P.nbands * P.nchunks + WPB - 1) / WPB;
         P.gpf = std::max(1, std::min(per_frame_blocks, 16));
-        if (ra.rule == RULE_CHAM_ITV) {
+        if (tape) {
+            launch_tape(P, SG, s);
+        } else if (ra.rule == RULE_CHAM_ITV) {
             launch_rule1(P, SG, PIN, FINAL, s);
         } else if (ra.rule == RULE_CHAM_ATV) {
             launch_rule2(P, SG, PIN, FINAL, s);
@@ -255,6 +264,20 @@ int tv_launch_impl(const float *f, float *u, float *resid, int64_t nf, int64_t H
 
 // A MATLAB-rule run of `updates` dual updates (rule, tau, tw, c1, c2 as in
 // sci_tv.cuh); the workspace is tv_workspace_bytes(nf, H, W, updates + 1).
+// TV of nf frames (K Chambolle steps, 2 <= K <= 5, no stop test) that also
+// writes its tape: p_1..p_{K-1} to tape_p [K-1][nf][2][H][W] and
+// u_1..u_{K-2} to tape_u [K-2][nf][H][W].
+int tv_launch_tape(const float *f, float *u, int64_t nf, int64_t H, int64_t W, float weight,
+                   int K, float *tape_p, float *tape_u, void *workspace, size_t ws_bytes,
+                   cudaStream_t s) {
+    SCI_CHECK_ARG(tape_p && tape_u, "tv: null tape");
+    RuleArgs ra;
+    ra.tape_p = tape_p;
+    ra.tape_u = tape_u;
+    return tv_launch_core(f, u, nullptr, nf, H, W, H * W, weight, 0.f, K, nullptr, nullptr,
+                          workspace, ws_bytes, s, 0, 1, nullptr, nullptr, 0.f, ra);
+}
+
 int tv_launch_rule(int rule, const float *f, float *u, float *resid, int64_t nf, int64_t H,
                    int64_t W, int updates, float tau, float tw, float c1, float c2, int *steps,
                    void *workspace, size_t ws_bytes, cudaStream_t s) {

@@ -82,9 +82,13 @@ struct Pass {
     float lam;
     int frame_fast;       // work-item order: 1 = frames of one tile adjacent
     // MATLAB-twin update rules (RULE != 0; no stop test): c1 is lambda of
-    // the anisotropic Chambolle projection (RULE_CHAM_ATV) or the clip
+    // the anisotropic Chambolle projection (RULE_CHAM_ITV) or the clip
     // bound (RULE_CLIP); c2 scales div p in u = f - c2 div p (RULE_CLIP)
     float c1, c2;
+    // Tape of a single-pass run (kernels with TAPE = true): every stage k
+    // writes its p_k to tape_p [S][nf][2][H][W] and, for k < S, its u_k to
+    // tape_u [S-1][nf][H][W] (the reverse pass of the unrolled solver).
+    float *tape_p, *tape_u;
 };
 
 // Dual update rules of the pipeline (the dual p is held as p / lambda for
@@ -249,7 +253,7 @@ __device__ __forceinline__ Row<CPL> divergence(const Row<CPL> &prn, const Row<CP
 // One pipeline step: input row r enters, stage k handles row r-k.
 // GEN: rows may be outside [r0, r1) or touch the frame's first/last row.
 template <int S, int CPL, bool PIN, bool OUT_U, bool ENERGY, int MODE, bool GEN, int PROJ,
-          int RULE = RULE_SKIMAGE>
+          int RULE = RULE_SKIMAGE, bool TAPE = false>
 __device__ __forceinline__ void step(const Pass &P, const St<S, CPL> &in, St<S, CPL> &out,
                                      int r, int rs, int r0, int r1, const Lane<CPL> &L,
                                      const float *fb, const float *pinb, float *ob, float *rb,
@@ -383,6 +387,16 @@ __device__ __forceinline__ void step(const Pass &P, const St<S, CPL> &in, St<S, 
                 }
             }
         }
+        if (TAPE && (!GEN || (i >= r0 && i < r1))) {
+            const int64_t ro = (int64_t)i * W;
+            float *tp = P.tape_p + ((int64_t)(k - 1) * P.nf + frame) * 2 * hw;
+            store_row<CPL, MODE>(tp + ro, L.col, prn, L.lane_own, L.mk, vec);
+            store_row<CPL, MODE>(tp + hw + ro, L.col, pcn, L.lane_own, L.mk, vec);
+            if (k < S) {
+                float *tu = P.tape_u + ((int64_t)(k - 1) * P.nf + frame) * hw;
+                store_row<CPL, MODE>(tu + ro, L.col, uk, L.lane_own, L.mk, vec);
+            }
+        }
         if (k == S) {
             if (!GEN || (i >= r0 && i < r1)) {
                 const int64_t ro = (int64_t)i * W;
@@ -407,7 +421,7 @@ __device__ __forceinline__ void step(const Pass &P, const St<S, CPL> &in, St<S, 
 }
 
 template <int S, int CPL, bool PIN, bool OUT_U, bool ENERGY, int MODE, int PROJ,
-          int RULE = RULE_SKIMAGE>
+          int RULE = RULE_SKIMAGE, bool TAPE = false>
 __device__ __forceinline__ void run(const Pass &P, int frame, int chunk, int band, int lane) {
     const int H = P.H, W = P.W;
     Lane<CPL> L;
@@ -454,16 +468,17 @@ __device__ __forceinline__ void run(const Pass &P, int frame, int chunk, int ban
     while (r <= rlast) {
         if (r == rfb && r + 1 <= rfe) {
             for (; r + 1 <= rfe; r += 2) {
-                step<S, CPL, PIN, OUT_U, ENERGY, MODE, false, PROJ, RULE>(
+                step<S, CPL, PIN, OUT_U, ENERGY, MODE, false, PROJ, RULE, TAPE>(
                     P, A, B, r, rs, r0, r1, L, fb, pinb, ob, rb, ek, frame);
-                step<S, CPL, PIN, OUT_U, ENERGY, MODE, false, PROJ, RULE>(
+                step<S, CPL, PIN, OUT_U, ENERGY, MODE, false, PROJ, RULE, TAPE>(
                     P, B, A, r + 1, rs, r0, r1, L, fb, pinb, ob, rb, ek, frame);
             }
             continue;
         }
         // prologue (halo rows, first S steps) and epilogue (chunk tail, last row)
-        step<S, CPL, PIN, OUT_U, ENERGY, MODE, true, PROJ, RULE>(P, A, B, r, rs, r0, r1, L, fb,
-                                                                  pinb, ob, rb, ek, frame);
+        step<S, CPL, PIN, OUT_U, ENERGY, MODE, true, PROJ, RULE, TAPE>(P, A, B, r, rs, r0, r1, L,
+                                                                        fb, pinb, ob, rb, ek,
+                                                                        frame);
         A = B;
         ++r;
     }
@@ -714,18 +729,20 @@ __device__ __forceinline__ void run2(const Pass &P, int frame, int chunk, int ba
 }
 
 template <int S, int CPL, bool PIN, bool OUT_U, bool ENERGY, int LAG = 1, int PROJ = 0,
-          int RULE = RULE_SKIMAGE>
+          int RULE = RULE_SKIMAGE, bool TAPE = false>
 __device__ __forceinline__ void run_mode(const Pass &P, int frame, int chunk, int band, int lane) {
     const int c0 = band * P.own - P.hl;
     const bool interior = P.vec && c0 >= 0 && c0 + 32 * CPL - 1 <= P.W - 1;
+    static_assert(!(TAPE && LAG == 2), "the tape is written by the lag-1 pipeline");
     if (LAG == 2) {
         if (interior) run2<S, CPL, PIN, OUT_U, ENERGY, INTERIOR>(P, frame, chunk, band, lane);
         else run2<S, CPL, PIN, OUT_U, ENERGY, EDGE>(P, frame, chunk, band, lane);
     } else {
         if (interior)
-            run<S, CPL, PIN, OUT_U, ENERGY, INTERIOR, PROJ, RULE>(P, frame, chunk, band, lane);
+            run<S, CPL, PIN, OUT_U, ENERGY, INTERIOR, PROJ, RULE, TAPE>(P, frame, chunk, band,
+                                                                         lane);
         else
-            run<S, CPL, PIN, OUT_U, ENERGY, EDGE, PROJ, RULE>(P, frame, chunk, band, lane);
+            run<S, CPL, PIN, OUT_U, ENERGY, EDGE, PROJ, RULE, TAPE>(P, frame, chunk, band, lane);
     }
 }
 
@@ -777,14 +794,14 @@ constexpr int min_blocks() { return CPL == 2 ? 4 : 3; }
 
 // Main launch of one pass: every frame not yet stopped runs all SG updates.
 template <int SG, bool PIN, bool FINAL, int CPL, int LAG = 1, int PROJ = 0,
-          int RULE = RULE_SKIMAGE>
+          int RULE = RULE_SKIMAGE, bool TAPE = false>
 __global__ void __launch_bounds__(WPB * 32, min_blocks<CPL>()) k_tv_main(Pass P) {
     int frame, chunk, band;
     if (!decode_item(P, frame, chunk, band)) return;
     if (PIN && P.done[frame] >= 0) return;  // stopped in an earlier pass
-    // the MATLAB rules have no stop test and need no energies
-    run_mode<SG, CPL, PIN, FINAL, RULE == RULE_SKIMAGE, LAG, PROJ, RULE>(P, frame, chunk, band,
-                                                                         threadIdx.x & 31);
+    // the MATLAB rules and the taped runs have no stop test and need no energies
+    run_mode<SG, CPL, PIN, FINAL, RULE == RULE_SKIMAGE && !TAPE, LAG, PROJ, RULE, TAPE>(
+        P, frame, chunk, band, threadIdx.x & 31);
 }
 
 // Stop-test launch of one pass over the same work items as the main launch:
@@ -826,6 +843,7 @@ void launch_main4_lag2(const Pass &P, bool pin, bool final_pass, cudaStream_t s)
 void launch_main_proj(const Pass &P, int SG, cudaStream_t s);
 void launch_fixup_proj(const Pass &P, cudaStream_t s);
 void launch_main123(const Pass &P, int SG, bool pin, cudaStream_t s);
+void launch_tape(const Pass &P, int SG, cudaStream_t s);  // sci_tv_tape.cu
 void launch_rule1(const Pass &P, int SG, bool pin, bool final_pass, cudaStream_t s);
 void launch_rule2(const Pass &P, int SG, bool pin, bool final_pass, cudaStream_t s);
 void launch_rule3(const Pass &P, int SG, bool pin, bool final_pass, cudaStream_t s);

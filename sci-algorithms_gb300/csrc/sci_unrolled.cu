@@ -9,14 +9,17 @@
 //     v^k = x^k + lambda_k At(q);   x^{k+1} = TV(v^k)   (fixed T Chambolle
 //     steps, no stop test: the stop rule is not differentiable)
 //   loss = mean (x^K - x_true)^2.
-// The forward keeps x^k and y1^k; the reverse pass recomputes each TV call
-// from v^k with a step-by-step tape (u_k, p_{k+1}) and runs its adjoint:
+// The forward keeps x^k and y1^k and, when they fit (up to 48 GiB), v^k and
+// the tape (u_k, p_{k+1}) its TV pipeline writes as it runs; otherwise the
+// reverse pass recomputes each TV call from v^k step by step.  The reverse
+// pass runs the adjoint of every TV step:
 //   p_{k+1} = (p_k - tau g_k) r_k,  r_k = 1 / (1 + (tau/w) n_k),  n_k = |g_k|,
 //   gbar_k = -tau r_k pbar_{k+1} - (tau/w) r_k (g_k / n_k) <pbar_{k+1}, p_{k+1}>
 //            (0 for the second term where n_k = 0: the safe-norm convention),
 //   ubar_k = -div gbar_k,  fbar += ubar_k,  pbar_k = r_k pbar_{k+1} + grad ubar_k.
 // then the adjoint of the projection (including d/dPhi through A, At and
 // Phi_sum, and d/dlambda_k), and finally of the measurement and x^0.
+#include <cstdlib>
 #include <list>
 #include <mutex>
 #include <string>
@@ -28,6 +31,9 @@ namespace sci {
 int tv_launch_flags(const float *f, float *u, float *resid, int64_t nf, int64_t H, int64_t W,
                     int64_t fs, float weight, float eps, int K, int *steps, double *energy_out,
                     void *workspace, size_t ws_bytes, cudaStream_t s, int force_R, int flags);
+int tv_launch_tape(const float *f, float *u, int64_t nf, int64_t H, int64_t W, float weight,
+                   int K, float *tape_p, float *tape_u, void *workspace, size_t ws_bytes,
+                   cudaStream_t s);
 size_t tv_workspace_bytes(int64_t nf, int64_t H, int64_t W, int K);
 
 namespace unr {
@@ -448,15 +454,30 @@ __global__ void k_init_bwd(const float *__restrict__ x0b, const float *__restric
 struct Ws {
     float *phi, *ps, *y, *X, *Y1, *V;          // forward
     float *tu, *tp;                            // tape: u_1..u_{T-1}, p_1..p_{T-1}
+    // stored tapes (when they fit): per outer iteration k, v^k and the
+    // forward TV's tape, so that the reverse pass recomputes neither
+    bool stored;
+    float *Vall, *tpall, *tuall;               // [K][nbhw], [K][U][2 nbhw], [K][U-1][nbhw]
     float *pb0, *pb1, *fb, *xb, *y1c, *ybar, *phib, *psb;  // reverse
     double *loss;
     void *tv;
     size_t tv_bytes;
 };
 
+// Whether the forward keeps v^k and the TV tape of every outer iteration
+// (3 (T-1) planes per iteration) for the reverse pass: up to 48 GiB, unless
+// SCI_UNROLLED_TAPE=0 (then the reverse pass recomputes them).
+bool stored_tape(int64_t N, int64_t B, int64_t H, int64_t W, int K, int T) {
+    const char *e = getenv("SCI_UNROLLED_TAPE");
+    if (e && e[0] == '0') return false;
+    const double bytes = 4.0 * (double)(N * B * H * W) * 3.0 * (T - 1) * K;
+    return bytes <= 48.0 * (1ull << 30);
+}
+
 size_t layout(int64_t N, int64_t B, int64_t H, int64_t W, int K, int T, Ws *w, char *base) {
     const size_t hw = (size_t)(H * W), nbhw = (size_t)(N * B) * hw, nhw = (size_t)N * hw;
     const int U = T - 1;
+    const bool st = stored_tape(N, B, H, W, K, T);
     size_t off = 0;
     auto take = [&](size_t floats) {
         size_t o = off;
@@ -469,6 +490,12 @@ size_t layout(int64_t N, int64_t B, int64_t H, int64_t W, int K, int T, Ws *w, c
     const size_t o_pb0 = take(2 * nbhw), o_pb1 = take(2 * nbhw);
     const size_t o_fb = take(nbhw), o_xb = take(nbhw), o_y1c = take(nhw), o_ybar = take(nhw);
     const size_t o_phib = take(B * hw), o_psb = take(hw), o_loss = take(4);
+    size_t o_Vall = 0, o_tpall = 0, o_tuall = 0;
+    if (st) {
+        o_Vall = take((size_t)K * nbhw);
+        o_tpall = take((size_t)K * U * 2 * nbhw);
+        o_tuall = take((size_t)K * (U > 1 ? U - 1 : 1) * nbhw);
+    }
     const size_t tvb = tv_workspace_bytes(N * B, H, W, T);
     const size_t o_tv = off;
     off += (tvb + 255) & ~size_t(255);
@@ -479,6 +506,10 @@ size_t layout(int64_t N, int64_t B, int64_t H, int64_t W, int K, int T, Ws *w, c
         w->fb = F(o_fb); w->xb = F(o_xb); w->y1c = F(o_y1c);
         w->ybar = F(o_ybar); w->phib = F(o_phib); w->psb = F(o_psb);
         w->loss = reinterpret_cast<double *>(base + o_loss);
+        w->stored = st;
+        w->Vall = st ? F(o_Vall) : nullptr;
+        w->tpall = st ? F(o_tpall) : nullptr;
+        w->tuall = st ? F(o_tuall) : nullptr;
         w->tv = base + o_tv;
         w->tv_bytes = tvb;
     }
@@ -501,13 +532,20 @@ int forward(const float *logits, const float *lambdas, const float *xt, int64_t 
     k_mask<<<grid1(hw, 256), 256, 0, s>>>(logits, w.phi, w.ps, (int)B, hw);
     k_meas_x0<<<g, 256, 0, s>>>(xt, w.phi, w.ps, w.y, w.X, (int)N, (int)B, hw);
     SCI_LAUNCHED("k_meas_x0");
+    const int U = T - 1;
     for (int k = 0; k < K; ++k) {
+        float *V = w.stored ? w.Vall + k * nbhw : w.V;
         k_proj_fwd<<<g, 256, 0, s>>>(w.X + k * nbhw, w.phi, w.ps, w.y,
                                      k ? w.Y1 + (k - 1) * N * hw : nullptr, w.Y1 + k * N * hw,
-                                     w.V, lambdas, k, (int)N, (int)B, hw);
+                                     V, lambdas, k, (int)N, (int)B, hw);
         SCI_LAUNCHED("k_proj_fwd");
-        int e = tv_launch_flags(w.V, w.X + (k + 1) * nbhw, nullptr, N * B, H, W, hw, weight,
-                                0.f, T, nullptr, nullptr, w.tv, w.tv_bytes, s, 0, kNoStop);
+        int e = w.stored
+                    ? tv_launch_tape(V, w.X + (k + 1) * nbhw, N * B, H, W, weight, T,
+                                     w.tpall + (int64_t)k * U * 2 * nbhw,
+                                     w.tuall + (int64_t)k * (U > 1 ? U - 1 : 1) * nbhw, w.tv,
+                                     w.tv_bytes, s)
+                    : tv_launch_flags(V, w.X + (k + 1) * nbhw, nullptr, N * B, H, W, hw, weight,
+                                      0.f, T, nullptr, nullptr, w.tv, w.tv_bytes, s, 0, kNoStop);
         if (e) return e;
     }
     SCI_CUDA(cudaMemsetAsync(w.loss, 0, sizeof(double), s));
@@ -614,7 +652,7 @@ int sci_unrolled_fwd(const float *logits, const float *lambdas, const float *x_t
         return SCI_OK;
     };
     const std::string key = make_key(1, logits, lambdas, x_true, N, B, H, W, K, tv_iters,
-                                     tv_weight, loss, x_out, workspace);
+                                     tv_weight, loss, x_out, workspace, (int)w.stored);
     return run_graph(key, as_stream(stream), body);
 }
 
@@ -632,7 +670,8 @@ int sci_unrolled_bwd(const float *logits, const float *lambdas, const float *x_t
     Ws w;
     layout(N, B, H, W, K, tv_iters, &w, static_cast<char *>(workspace));
     const std::string key = make_key(2, logits, lambdas, x_true, N, B, H, W, K, tv_iters,
-                                     tv_weight, grad_loss, grad_logits, grad_lambdas, workspace);
+                                     tv_weight, grad_loss, grad_logits, grad_lambdas, workspace,
+                                     (int)w.stored);
     return run_graph(key, as_stream(stream), [&](cudaStream_t s) -> int {
     // The checkpoints of the preceding sci_unrolled_fwd call on this
     // workspace (same arguments) are used as they are.
@@ -650,36 +689,41 @@ int sci_unrolled_bwd(const float *logits, const float *lambdas, const float *x_t
     SCI_CUDA(cudaMemsetAsync(w.psb, 0, 4 * hw, s));
     SCI_CUDA(cudaMemsetAsync(grad_lambdas, 0, sizeof(double) * K, s));
     for (int k = K - 1; k >= 0; --k) {
-        // recompute v^k and the TV tape
-        k_proj_fwd<<<grid1(nhw, 256), 256, 0, s>>>(
-            w.X + k * nbhw, w.phi, w.ps, w.y, k ? w.Y1 + (k - 1) * nhw : nullptr,
-            w.Y1 + k * nhw, w.V, lambdas, k, (int)N, (int)B, hw);
-        const float *u_prev = w.V;  // u_0 = f = v^k
-        for (int j = 0; j < U; ++j) {
-            float *pj = w.tp + (int64_t)j * 2 * nbhw;  // p_{j+1}
-            const float *pprev = j ? w.tp + (int64_t)(j - 1) * 2 * nbhw : nullptr;
-            float *uj = w.tu + (int64_t)j * nbhw;      // u_{j+1}
-            const bool p0 = j == 0, lastp = j + 1 == U;
-            if (p0 && lastp)
-                k_tape_step<true, true><<<g3, kBlk3, 0, s>>>(u_prev, pprev, w.V, pj, uj, (int)H,
-                                                             (int)W, tau, tw);
-            else if (p0)
-                k_tape_step<true, false><<<g3, kBlk3, 0, s>>>(u_prev, pprev, w.V, pj, uj, (int)H,
-                                                              (int)W, tau, tw);
-            else if (lastp)
-                k_tape_step<false, true><<<g3, kBlk3, 0, s>>>(u_prev, pprev, w.V, pj, uj, (int)H,
-                                                              (int)W, tau, tw);
-            else
-                k_tape_step<false, false><<<g3, kBlk3, 0, s>>>(u_prev, pprev, w.V, pj, uj,
-                                                               (int)H, (int)W, tau, tw);
-            u_prev = uj;
+        // v^k and the TV tape: kept by the forward, or recomputed
+        const float *V = w.stored ? w.Vall + k * nbhw : w.V;
+        const float *tp = w.stored ? w.tpall + (int64_t)k * U * 2 * nbhw : w.tp;
+        const float *tu = w.stored ? w.tuall + (int64_t)k * (U > 1 ? U - 1 : 1) * nbhw : w.tu;
+        if (!w.stored) {
+            k_proj_fwd<<<grid1(nhw, 256), 256, 0, s>>>(
+                w.X + k * nbhw, w.phi, w.ps, w.y, k ? w.Y1 + (k - 1) * nhw : nullptr,
+                w.Y1 + k * nhw, w.V, lambdas, k, (int)N, (int)B, hw);
+            const float *u_prev = w.V;  // u_0 = f = v^k
+            for (int j = 0; j < U; ++j) {
+                float *pj = w.tp + (int64_t)j * 2 * nbhw;  // p_{j+1}
+                const float *pprev = j ? w.tp + (int64_t)(j - 1) * 2 * nbhw : nullptr;
+                float *uj = w.tu + (int64_t)j * nbhw;      // u_{j+1}
+                const bool p0 = j == 0, lastp = j + 1 == U;
+                if (p0 && lastp)
+                    k_tape_step<true, true><<<g3, kBlk3, 0, s>>>(u_prev, pprev, w.V, pj, uj, (int)H,
+                                                                 (int)W, tau, tw);
+                else if (p0)
+                    k_tape_step<true, false><<<g3, kBlk3, 0, s>>>(u_prev, pprev, w.V, pj, uj, (int)H,
+                                                                  (int)W, tau, tw);
+                else if (lastp)
+                    k_tape_step<false, true><<<g3, kBlk3, 0, s>>>(u_prev, pprev, w.V, pj, uj, (int)H,
+                                                                  (int)W, tau, tw);
+                else
+                    k_tape_step<false, false><<<g3, kBlk3, 0, s>>>(u_prev, pprev, w.V, pj, uj,
+                                                                   (int)H, (int)W, tau, tw);
+                u_prev = uj;
+            }
+            SCI_LAUNCHED("tv tape");
         }
-        SCI_LAUNCHED("tv tape");
         // TV adjoint: fbar = d/dv^k, one fused step per dual update
         float *pb_in = w.pb0, *pb_out = w.pb1;
         for (int j = U - 1; j >= 0; --j) {
-            const float *uj = j == 0 ? w.V : w.tu + (int64_t)(j - 1) * nbhw;  // u_j
-            const float *pn = w.tp + (int64_t)j * 2 * nbhw;                   // p_{j+1}
+            const float *uj = j == 0 ? V : tu + (int64_t)(j - 1) * nbhw;  // u_j
+            const float *pn = tp + (int64_t)j * 2 * nbhw;                 // p_{j+1}
             const bool first = j == U - 1, last = j == 0;
             if (first && last)
                 k_tvb_step<true, true><<<g3, kBlk3, 0, s>>>(uj, pn, pb_in, w.xb, pb_out, w.fb,

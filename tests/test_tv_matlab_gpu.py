@@ -57,6 +57,18 @@ def test_projection_active_and_iteration_counts(tvm, lam, iters):
     assert np.max(np.abs(_dev.unplanar(u, f) - ref)) < (2e-4 if "FGP" in tvm else ATOL)
 
 
+@pytest.mark.parametrize("B", [5, 7, 22, 31, 32])
+@pytest.mark.parametrize("H,W", [(33, 70), (17, 9)])
+def test_itv3d_frame_counts(B, H, W):
+    """ITV3D Chambolle with frame counts that leave frame lanes idle (the
+    norm over frames is reduced across lanes) and strips narrower than a
+    warp's 8 columns."""
+    f = frames(H, W, B, seed=B + H)
+    ref = tm.tv_by_name(f, "ITV3D_cham", 0.1)
+    out = sci.denoise_tv_matlab(f, "ITV3D_cham", 0.1)
+    assert np.max(np.abs(out - ref)) < ATOL
+
+
 def test_one_frame_takes_matlabs_2d_branch():
     f = frames(40, 52, 1, seed=5)
     a = sci.denoise_tv_matlab(f, "ATV_ClipB", 0.1)
