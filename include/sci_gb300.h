@@ -410,6 +410,18 @@ int sci_cnn_conv_thin(const void *in, const void *weights, const float *bias,
                       void *out, int64_t nframes, int64_t H, int64_t W, int N,
                       int relu, void *stream);
 
+/* Per-frame image-quality sums of x against orig (planar nframes x H x W,
+ * H, W >= 7): sqerr[f] = sum (orig - x)^2 over frame f, and ssim_sum[f] =
+ * the sum of the SSIM map (7 x 7 uniform windows, sample covariance, K1 =
+ * 0.01, K2 = 0.03, dynamic range data_range) over the frame cropped by 3
+ * pixels, i.e. SSIM = ssim_sum / ((H - 6)(W - 6)) and PSNR =
+ * 10 log10(data_range^2 / (sqerr / (H W))).  Device doubles, overwritten.
+ * Replaces compare_psnr / compare_ssim(..., data_range=1.) per frame
+ * (PnP_SCI/python/pnp_sci_algo.py:702-705, scikit-image 0.16). */
+int sci_frame_metrics(const float *orig, const float *x, int64_t nframes,
+                      int64_t H, int64_t W, double data_range, double *sqerr,
+                      double *ssim_sum, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

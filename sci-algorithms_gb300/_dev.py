@@ -63,6 +63,20 @@ def plane(a, dev=None):
     return torch.from_numpy(np.ascontiguousarray(a, dtype=np.float32)).to(dev)
 
 
+def stack(a, dev=None):
+    """An H x W x F array (numpy or torch) as a float32 tensor on the GPU,
+    in its own layout: numpy input crosses to the device once in its own
+    dtype and is converted there (a host-side float64 -> float32 pass over
+    a multi-GB ground truth costs more than the larger copy)."""
+    dev = dev or device()
+    if is_torch(a):
+        return a.to(device=dev, dtype=torch.float32)
+    a = np.asarray(a)
+    if a.dtype not in (np.float32, np.float64):
+        a = a.astype(np.float32)
+    return torch.from_numpy(np.ascontiguousarray(a)).to(dev).to(torch.float32)
+
+
 def unplanar(p, like):
     """B x H x W device tensor -> H x W x B in the kind of ``like``.
 

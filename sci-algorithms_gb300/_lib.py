@@ -76,6 +76,7 @@ _SIGS = {
     "sci_tv_matlab": [ctypes.c_int, c_vp, c_vp, c_i64, c_i64, c_i64, c_f, ctypes.c_int, c_vp,
                       c_sz, c_vp],
     "sci_sqerr_accum": [c_vp, c_vp, c_i64, c_vp, c_vp],
+    "sci_frame_metrics": [c_vp, c_vp, c_i64, c_i64, c_i64, ctypes.c_double, c_vp, c_vp, c_vp],
     "sci_solver_workspace_bytes": [c_i64, c_i64, c_i64, ctypes.POINTER(SolveOpts),
                                    ctypes.POINTER(c_sz)],
     "sci_gap_tv": [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_i64, c_i64,

@@ -19,7 +19,7 @@ import math
 import torch
 
 from . import _dev
-from .metrics import frame_psnr, frame_ssim
+from .metrics import frame_psnr_ssim
 from .solver import Solver
 from .utils import MaskOperator
 
@@ -90,7 +90,7 @@ def gap_denoise_bayer(y_bayer, Phi_bayer, _lambda=1, accelerate=True, denoiser='
     psnr_, ssim_ = [], []
     if X_orig is not None:
         o = _dev.planar(X_orig)
-        psnr_, ssim_ = frame_psnr(o, x), frame_ssim(o, x)
+        psnr_, ssim_ = frame_psnr_ssim(o, x)
     return _dev.unplanar(x, y_bayer), psnr_, ssim_, psnr_all
 
 

@@ -24,7 +24,7 @@ import torch
 
 from . import _dev
 from ._lib import call
-from .metrics import frame_psnr, frame_ssim
+from .metrics import frame_psnr_ssim
 from .pnp_sci_algo import gap_denoise
 from .tv import tv_frames, tv_workspace
 from .utils import MaskOperator, operator_of, psnr_from_mse, sum_sq_err
@@ -96,7 +96,7 @@ def _metrics(x, X_orig):
     if X_orig is None:
         return [], []
     o = _dev.planar(X_orig)
-    return frame_psnr(o, x), frame_ssim(o, x)
+    return frame_psnr_ssim(o, x)
 
 
 def cnn_step(denoiser, model, precision=None):
@@ -291,16 +291,19 @@ def joint_admmdenoise_cacti(meas, mask, A, At, projmeth='admm', v0=None, orig=No
     torch_in = _dev.is_torch(meas)
     psnr_, ssim_, psnrall_ = [], [], []
     x_dev = None  # the H x W x (B nframe) result, assembled on the device
+    # the measurements and the ground truth go to the device once; the
+    # blocks are sliced there (host-side strided slices of H x W x F arrays
+    # cost more than the copies)
+    meas_d = _dev.stack(meas)
+    orig_d = None if orig is None else _dev.stack(orig)
     begin = time.time()
     t_ = 0.0
     for kf in range(nframe):
         k = kf + iframe
         flip = (maskdirection.lower() == 'updown' and k % 2 == 1) or \
                (maskdirection.lower() == 'downup' and k % 2 == 0)
-        meas_k = meas[..., k] / MAXB
-        if not torch_in:
-            meas_k = _dev.plane(meas_k)  # block results stay on the device
-        orig_k = None if orig is None else orig[..., k * nmask:(k + 1) * nmask] / MAXB
+        meas_k = meas_d[..., k] / MAXB  # block results stay on the device
+        orig_k = None if orig_d is None else orig_d[..., k * nmask:(k + 1) * nmask] / MAXB
         v0_k = None
         if v0 is not None:
             v0_k = v0[:, :, kf * nmask:(kf + 1) * nmask]

@@ -33,7 +33,7 @@ import numpy as np
 import torch
 
 from . import _dev
-from .metrics import frame_psnr, frame_ssim
+from .metrics import frame_psnr_ssim
 from .solver import Solver
 from .tv import TVM, tv_frames, tv_matlab_frames, tv_matlab_workspace, tv_workspace, tvm_kind
 from .cassi import CassiOperator, CassiSolver
@@ -72,7 +72,7 @@ def _metrics(x_planar, X_orig, like):
     if X_orig is None:
         return [], []
     o = _dev.planar(X_orig)
-    return frame_psnr(o, x_planar), frame_ssim(o, x_planar)
+    return frame_psnr_ssim(o, x_planar)
 
 
 def _solve(projmeth, y, Phi_sum, A, At, iters, _lambda, tv_weight, tv_iter_max, eps,
@@ -226,14 +226,17 @@ def admmdenoise_cacti(meas, mask, A, At, projmeth='admm', v0=None, orig=None, if
         mask_sum = torch.where(mask_sum == 0, torch.ones_like(mask_sum), mask_sum)
     psnr_, ssim_, psnrall_ = [], [], []
     x_dev = None  # the H x W x (B nframe) result, assembled on the device
+    # the measurements and the ground truth go to the device once; the
+    # blocks are sliced there (host-side strided slices of H x W x F arrays
+    # cost more than the copies)
+    meas_d = _dev.stack(meas)
+    orig_d = None if orig is None else _dev.stack(orig)
     begin = time.time()
     t_ = 0.0
     for kf in range(nframe):
         k = kf + iframe
-        meas_k = meas[..., k] / MAXB
-        if not torch_in:
-            meas_k = _dev.plane(meas_k)  # block results stay on the device
-        orig_k = None if orig is None else orig[..., k * nmask:(k + 1) * nmask] / MAXB
+        meas_k = meas_d[..., k] / MAXB  # block results stay on the device
+        orig_k = None if orig_d is None else orig_d[..., k * nmask:(k + 1) * nmask] / MAXB
         v0_k = None
         if v0 is not None:
             v0_k = v0[:, :, kf * nmask:(kf + 1) * nmask]
