@@ -27,7 +27,6 @@
 // dual update of the FGP loop does not reach the returned value and is not
 // computed.
 #include <cmath>
-#include <cstdlib>
 #include <utility>
 
 #include "sci_common.cuh"
@@ -136,33 +135,53 @@ __global__ void __launch_bounds__(32 * FL) k_cham_update_coupled(
         const bool lastrow = i + 1 >= g.H;
         float z1[FMAX], z2[FMAX], zn[FMAX], p1n[FMAX], p2n[FMAX], zrn[FMAX], p2rn[FMAX];
         float s = 0.f;
+        // every load of row i + 1 first, by all lanes alike (lanes that are
+        // not at the strip's edge load their own column for the halo
+        // values, an L1 hit), so that one memory latency covers the row
+        const int jl = (lane == 0 && x0 > 0) ? x0 - 1 : jc;  // left p1
+        const int jh = (lane == 31) ? jr : jc;               // right halo column
+        float la[FMAX], lb[FMAX], lf[FMAX], ll[FMAX], ra[FMAX], rb[FMAX], rf[FMAX];
+#pragma unroll
+        for (int t = 0; t < FMAX; ++t) {
+            const int b = threadIdx.y + t * FL;
+            la[t] = lb[t] = lf[t] = ll[t] = ra[t] = rb[t] = rf[t] = 0.f;
+            if (b >= nf || lastrow) continue;
+            const int64_t o = (int64_t)b * g.hw + (int64_t)(i + 1) * g.W;
+            lf[t] = f[o + jc];
+            rf[t] = f[o + jh];
+            if (!first) {
+                la[t] = p1[o + jc];
+                lb[t] = p2[o + jc];
+                ll[t] = p1[o + jl];
+                ra[t] = p1[o + jh];
+                rb[t] = p2[o + jh];
+            }
+        }
 #pragma unroll
         for (int t = 0; t < FMAX; ++t) {
             const int b = threadIdx.y + t * FL;
             // right neighbour of z in this row (all lanes shuffle)
             float zright = __shfl_down_sync(0xffffffffu, zc[t], 1);
             if (lane == 31) zright = zr[t];
+            const float a = la[t];
+            float al = __shfl_up_sync(0xffffffffu, a, 1);
             zn[t] = p1n[t] = p2n[t] = zrn[t] = p2rn[t] = 0.f;
             z1[t] = z2[t] = 0.f;
             if (b >= nf) continue;
-            const int64_t fo = (int64_t)b * g.hw;
             if (!lastrow) {  // row i + 1
-                const int64_t o = fo + (int64_t)(i + 1) * g.W;
                 if (first) {
-                    zn[t] = -f[o + jc] * lam;
-                    if (lane == 31 && right) zrn[t] = -f[o + jr] * lam;
+                    zn[t] = -lf[t] * lam;
+                    if (lane == 31 && right) zrn[t] = -rf[t] * lam;
                 } else {
-                    const float a = p1[o + jc], bb = p2[o + jc];
-                    float al = __shfl_up_sync(0xffffffffu, a, 1);
-                    if (lane == 0) al = (x0 > 0) ? p1[o + x0 - 1] : a;
+                    const float bb = lb[t];
+                    if (lane == 0) al = (x0 > 0) ? ll[t] : a;
                     if (jc == 0) al = a;  // MATLAB: no p1 at the first column
-                    zn[t] = zval(a, al, bb, p2c[t], f[o + jc]);
+                    zn[t] = zval(a, al, bb, p2c[t], lf[t]);
                     p1n[t] = a;
                     p2n[t] = bb;
                     if (lane == 31 && right) {
-                        const float ar = p1[o + jr], br = p2[o + jr];
-                        zrn[t] = zval(ar, a, br, p2r[t], f[o + jr]);
-                        p2rn[t] = br;
+                        zrn[t] = zval(ra[t], a, rb[t], p2r[t], rf[t]);
+                        p2rn[t] = rb[t];
                     }
                 }
             }
@@ -180,123 +199,6 @@ __global__ void __launch_bounds__(32 * FL) k_cham_update_coupled(
 #pragma unroll
         for (int t = 0; t < FMAX; ++t) {
             const int b = threadIdx.y + t * FL;
-            if (b < nf && in) {
-                const int64_t q = (int64_t)b * g.hw + (int64_t)i * g.W + j;
-                q1[q] = (p1c[t] + dt * z1[t]) / denom;
-                q2[q] = (p2c[t] + dt * z2[t]) / denom;
-            }
-            zc[t] = zn[t];
-            p1c[t] = p1n[t];
-            p2c[t] = p2n[t];
-            zr[t] = zrn[t];
-            p2r[t] = p2rn[t];
-        }
-    }
-}
-
-// ITV3D, warp form: a warp owns a strip of 8 columns (lane & 7) and RB rows
-// with 4 frame lanes (lane >> 3), lane l handling frames l >> 3, +4, +8, ...
-// (at most FW per lane).  The norm over the frames is two xor shuffles, so
-// no block barrier sits in the row loop; neighbours along the row come by
-// shuffles within the 8-lane group (column 0 loads the strip's left p1,
-// column 7 carries the right halo column's z).  The same arithmetic as
-// k_cham_update_coupled except the order of the float32 frame sum.
-constexpr int FW = 8;  // frames per lane (nf <= 32)
-
-__global__ void __launch_bounds__(128) k_cham_itv3d_warp(
-    const float *__restrict__ f, const float *__restrict__ p1, const float *__restrict__ p2,
-    float *__restrict__ q1, float *__restrict__ q2, Geo g, int nf, float lam, float dt,
-    int first) {
-    const int lane = threadIdx.x & 31, col = lane & 7, fl = lane >> 3;
-    const int x0 = (blockIdx.x * 4 + (threadIdx.x >> 5)) * 8;
-    if (x0 >= g.W) return;  // whole warp outside the frame (no shuffle partner waits)
-    const int j = x0 + col;
-    const int i0 = blockIdx.y * RB, i1 = min(i0 + RB, g.H);
-    const bool in = j < g.W;
-    const int jc = in ? j : g.W - 1;
-    const bool right = x0 + 8 < g.W;
-    const int jr = right ? x0 + 8 : jc;
-    auto zval = [&](float a, float al, float b, float bu, float fv) {
-        return (((a - al) + b) - bu) - fv * lam;
-    };
-    float zc[FW], zr[FW], p1c[FW], p2c[FW], p2r[FW];
-#pragma unroll
-    for (int t = 0; t < FW; ++t) {  // row i0
-        const int b = fl + 4 * t;
-        zc[t] = zr[t] = p1c[t] = p2c[t] = p2r[t] = 0.f;
-        if (b >= nf) continue;
-        const int64_t o = (int64_t)b * g.hw + (int64_t)i0 * g.W;
-        if (first) {
-            zc[t] = -f[o + jc] * lam;
-            if (col == 7 && right) zr[t] = -f[o + jr] * lam;
-            continue;
-        }
-        const float a = p1[o + jc], bb = p2[o + jc];
-        const float al = (jc > 0) ? p1[o + jc - 1] : a;
-        const float bu = (i0 > 0) ? p2[o - g.W + jc] : bb;
-        zc[t] = zval(a, al, bb, bu, f[o + jc]);
-        p1c[t] = a;
-        p2c[t] = bb;
-        if (col == 7 && right) {
-            const float ar = p1[o + jr], br = p2[o + jr];
-            const float bur = (i0 > 0) ? p2[o - g.W + jr] : br;
-            zr[t] = zval(ar, a, br, bur, f[o + jr]);
-            p2r[t] = br;
-        }
-    }
-    for (int i = i0; i < i1; ++i) {
-        const bool lastrow = i + 1 >= g.H;
-        const int64_t rowo = (int64_t)(lastrow ? i : i + 1) * g.W;  // row i + 1 (clamped)
-        float z1[FW], z2[FW], zn[FW], p1n[FW], p2n[FW], zrn[FW], p2rn[FW];
-        float s = 0.f;
-#pragma unroll
-        for (int t = 0; t < FW; ++t) {
-            const int b = fl + 4 * t;
-            const bool live = b < nf;
-            const int64_t o = (int64_t)(live ? b : 0) * g.hw + rowo;
-            float a = 0.f, bb = 0.f, fv = 0.f;
-            if (live && !lastrow) {
-                fv = f[o + jc];
-                if (!first) {
-                    a = p1[o + jc];
-                    bb = p2[o + jc];
-                }
-            }
-            // all 32 lanes take part in both shuffles, live frame or not
-            const float zsh = __shfl_down_sync(0xffffffffu, zc[t], 1, 8);
-            float al = __shfl_up_sync(0xffffffffu, a, 1, 8);
-            zn[t] = p1n[t] = p2n[t] = zrn[t] = p2rn[t] = 0.f;
-            z1[t] = z2[t] = 0.f;
-            if (!live) continue;
-            const float zright = (col == 7) ? zr[t] : zsh;
-            z1[t] = (j < g.W - 1) ? zright - zc[t] : 0.f;
-            if (!lastrow) {
-                if (first) {
-                    zn[t] = -fv * lam;
-                    if (col == 7 && right) zrn[t] = -f[o + jr] * lam;
-                } else {
-                    if (col == 0) al = (x0 > 0) ? p1[o + x0 - 1] : a;
-                    if (jc == 0) al = a;  // MATLAB: no p1 at the first column
-                    zn[t] = zval(a, al, bb, p2c[t], fv);
-                    p1n[t] = a;
-                    p2n[t] = bb;
-                    if (col == 7 && right) {
-                        const float ar = p1[o + jr], br = p2[o + jr];
-                        zrn[t] = zval(ar, a, br, p2r[t], f[o + jr]);
-                        p2rn[t] = br;
-                    }
-                }
-                z2[t] = zn[t] - zc[t];
-            }
-            s += z1[t] * z1[t] + z2[t] * z2[t];
-        }
-        // the sum over the 4 frame lanes of this column (lanes col, +8, +16, +24)
-        const float tot = s + __shfl_xor_sync(0xffffffffu, s, 8);
-        const float all = tot + __shfl_xor_sync(0xffffffffu, tot, 16);
-        const float denom = 1.f + dt * sqrtf(all);
-#pragma unroll
-        for (int t = 0; t < FW; ++t) {
-            const int b = fl + 4 * t;
             if (b < nf && in) {
                 const int64_t q = (int64_t)b * g.hw + (int64_t)i * g.W + j;
                 q1[q] = (p1c[t] + dt * z1[t]) / denom;
@@ -504,18 +406,9 @@ int tvx_launch(int kind, const float *f, float *u, float *resid, int64_t nf, int
             // tvdenoise_cham_ITV3D.m:74-91
             const float dt = 0.25f;
             float *p1 = a1, *p2 = a2, *q1 = b1, *q2 = b2;
-            static const bool warp_form = [] {
-                const char *e = getenv("SCI_ITV3D_WARP");
-                return !(e && e[0] == '0');
-            }();
-            const dim3 grdw((unsigned)((W + 31) / 32), (unsigned)((H + RB - 1) / RB), 1);
             for (int it = 0; it < iters; ++it) {
-                if (warp_form)
-                    k_cham_itv3d_warp<<<grdw, 128, 0, s>>>(f, p1, p2, q1, q2, g, (int)nf, lam,
-                                                           dt, it == 0);
-                else
-                    k_cham_update_coupled<<<grds, blkc, 0, s>>>(f, p1, p2, q1, q2, g, (int)nf,
-                                                                lam, dt, it == 0);
+                k_cham_update_coupled<<<grds, blkc, 0, s>>>(f, p1, p2, q1, q2, g, (int)nf, lam,
+                                                            dt, it == 0);
                 SCI_LAUNCHED("k_cham_update_coupled");
                 std::swap(p1, q1);
                 std::swap(p2, q2);
