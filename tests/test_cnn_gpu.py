@@ -239,3 +239,26 @@ def test_tc_and_cudnn_first_layers_agree(golden, monkeypatch):
     assert not b.tc
     ra, rb = a(x, 0.1), b(x, 0.1)
     assert float((ra - rb).abs().max()) < 2e-2
+
+
+@pytest.mark.parametrize("kind", ["ffdnet", "fastdvdnet"])
+def test_bf16_tensor_core_path_on_odd_sizes(golden, kind):
+    """bf16 engine (tcgen05 first layer, NHWC8 glue kernels, shuffle-add) on
+    sizes that need padding (FastDVDnet: reflect to multiples of 4; FFDNet:
+    odd sizes repeat the last row / column) against the float64 oracle."""
+    g = golden("cnn_ffdnet" if kind == "ffdnet" else "cnn_fastdvdnet")
+    v = np.asarray(g["v"], np.float32)
+    if kind == "ffdnet":
+        v = v[:-1, :-3]  # 23 x 29 x 3
+        x = sci.ffdnet_vdenoiser(v, 0.1, model=ffdnet(golden), precision="bf16")
+        vp = np.pad(v, ((0, 1), (0, 1), (0, 0)), mode="edge")
+        p = ocnn.as_float64(ocnn.seeded_state_dict(ocnn.ffdnet_layout(1), int(g["seed"])))
+        ref = ocnn.ffdnet_vdenoiser(vp, 0.1, p)[:-1, :-1]
+    else:
+        v = v[:22, :30, :5].copy()
+        x = sci.fastdvdnet_denoiser(v, 0.1, model=fastdvdnet(golden), gray=True,
+                                    precision="bf16")
+        p = ocnn.as_float64(ocnn.seeded_state_dict(ocnn.fastdvdnet_layout(1), int(g["seed"])))
+        ref = ocnn.fastdvdnet_denoiser(v, 0.1, p)
+    assert x.shape == v.shape
+    assert noise_rel(x, v, ref) < NOISE_TOL["bf16"]
