@@ -57,12 +57,22 @@ def _solve(projmeth, y_bayer, Phi_bayer, iters, _lambda, tv_weight, tv_iter_max,
            accelerate, gamma, x0_bayer, X_orig, want_iqa, use_graph, tvm):
     chans, (B, H, W), dev = _channels(y_bayer, Phi_bayer, x0_bayer, X_orig if want_iqa else None)
     x_bayer = torch.empty((B, H, W), dtype=torch.float32, device=dev)
+    # the four sub-lattice problems are independent: one stream each, so
+    # that their kernels fill each other's tails
+    main = torch.cuda.current_stream()
+    streams = [torch.cuda.Stream(device=dev) for _ in BAYER]
+    solvers = []
+    for st, ((b0, b1), (yc, op, x0c, oc)) in zip(streams, zip(BAYER, chans)):
+        st.wait_stream(main)
+        with torch.cuda.stream(st):
+            s = Solver(op, projmeth, iters, _lambda, tv_weight, tv_iter_max, eps, accelerate,
+                       gamma, use_graph=use_graph, tvm=tvm)
+            xc = s.run(yc, x0=x0c, orig=oc)
+            x_bayer[:, b0::2, b1::2] = xc
+        solvers.append((s, oc))
     sq = None
-    for (b0, b1), (yc, op, x0c, oc) in zip(BAYER, chans):
-        s = Solver(op, projmeth, iters, _lambda, tv_weight, tv_iter_max, eps, accelerate, gamma,
-                   use_graph=use_graph, tvm=tvm)
-        xc = s.run(yc, x0=x0c, orig=oc)
-        x_bayer[:, b0::2, b1::2] = xc
+    for st, (s, oc) in zip(streams, solvers):
+        main.wait_stream(st)
         if oc is not None:
             sq = s.sqerr.clone() if sq is None else sq + s.sqerr
     mse = [] if sq is None else [v / float(B * H * W) for v in sq.tolist()]

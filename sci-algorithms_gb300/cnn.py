@@ -241,9 +241,12 @@ def as_native(model, kind):
     if not isinstance(model, nn.Module):
         raise TypeError("model must be an FFDNet / FastDVDnet network, got %s"
                         % type(model).__name__)
+    # the converted copy follows later changes of the foreign network's
+    # parameters (their version counters)
+    versions = tuple(t._version for t in list(model.parameters()) + list(model.buffers()))
     hit = _converted.get(model)
-    if hit is not None:
-        return hit
+    if hit is not None and hit[1] == versions:
+        return hit[0]
     sd = _strip(model.state_dict())
     if kind == "ffdnet":
         w = sd.get("intermediate_dncnn.itermediate_dncnn.0.weight")
@@ -255,9 +258,11 @@ def as_native(model, kind):
         if w is None:
             raise TypeError("model is not a FastDVDnet")
         net = FastDVDnet(5, w.shape[1] - 1)
+    if hit is not None:  # reload into the same copy, so that its engines refold
+        net = hit[0]
     load_reference_state_dict(net, sd)
     net.eval()
-    _converted[model] = net
+    _converted[model] = (net, versions)
     return net
 
 

@@ -151,6 +151,11 @@ def test_reference_built_model_is_converted(golden):
     foreign = torch.nn.DataParallel(_tree(ref_sd(g)))
     x = sci.ffdnet_vdenoiser(g["v"], float(g["sigma"]), model=foreign, precision="fp32")
     assert noise_rel(x, g["v"], g["x"]) < 1e-4
+    # a later change of the foreign network's weights reaches the converted copy
+    last = foreign.module.intermediate_dncnn.itermediate_dncnn
+    getattr(last, str(2 + 3 * 13)).weight.mul_(2.0)
+    x2 = sci.ffdnet_vdenoiser(g["v"], float(g["sigma"]), model=foreign, precision="fp32")
+    assert np.allclose(g["v"] - x2, 2 * (g["v"] - x), rtol=1e-3, atol=1e-5)
     with pytest.raises(ValueError):
         sci.ffdnet_vdenoiser(g["v"], 0.1, model=None)
 
