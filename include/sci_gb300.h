@@ -337,11 +337,13 @@ int sci_unrolled_bwd(const float *logits, const float *lambdas,
  * that all frames of a stack go through one batched network call.  The
  * convolutions themselves run in the caller's framework.  Layouts:
  * SCI_CNN_NCHW_F32 planar float32; SCI_CNN_NHWC8_BF16 one 16-byte vector
- * of 8 bfloat16 channels per pixel (unused channels 0).  sigma is a device
+ * of 8 bfloat16 channels per pixel; SCI_CNN_NHWC8_F32 8 float32 channels
+ * per pixel (unused channels 0).  sigma is a device
  * float (the noise level), read at run time so that a captured CUDA graph
  * replays with a new level. */
 #define SCI_CNN_NCHW_F32 0
 #define SCI_CNN_NHWC8_BF16 1
+#define SCI_CNN_NHWC8_F32 2
 
 /* FFDNet input: channel 0 = sigma, channel 1 + 2i + j = pixel (i, j) of
  * each 2 x 2 cell; out is nframes x 5 x ceil(H/2) x ceil(W/2) (NCHW) or
@@ -354,7 +356,7 @@ int sci_cnn_ffdnet_pack(const float *x, int64_t nframes, int64_t H, int64_t W,
 
 /* out = x - depth_to_space(noise), cropped to H x W, clipped to [0, 1] when
  * clip != 0.  noise: nframes x 4 x ceil(H/2) x ceil(W/2) float32 (NCHW) or
- * bfloat16 NHWC with `channels` (4 or 8) channels per pixel.  Replaces
+ * bfloat16 / float32 NHWC with `channels` (4 or 8) channels per pixel.  Replaces
  * upsamplefeatures (packages/ffdnet/functions.py:60-93) and the
  * subtraction of test_ffdnet_ipol.py:174. */
 int sci_cnn_ffdnet_unpack_sub(const float *x, const void *noise, int64_t nframes,
@@ -375,7 +377,7 @@ int sci_cnn_window(const float *src, int64_t nframes, int64_t Hs, int64_t Ws,
 
 /* out[k] = src[first + k] (reflect-padded as in sci_cnn_window) - r[k],
  * k < count, cropped to Ho x Wo, clipped to [0, 1] when clip != 0.  r:
- * count x 1 x Hp x Wp float32 (NCHW) or bfloat16 NHWC with `channels`
+ * count x 1 x Hp x Wp float32 (NCHW) or bfloat16 / float32 NHWC with `channels`
  * channels (channel 0 used).  Replaces DenBlock's `in1 - x` (packages/fastdvdnet/models.py:205)
  * and the crop of fastdvdnet.py:136-140. */
 int sci_cnn_center_sub(const float *src, int64_t nframes, int64_t Hs, int64_t Ws,
@@ -393,6 +395,10 @@ int sci_cnn_center_sub(const float *src, int64_t nframes, int64_t Hs, int64_t Ws
  * (packages/fastdvdnet/models.py:72-84, :202-203). */
 int sci_cnn_shuffle_add(const void *a, const void *u, void *out, int64_t N,
                         int64_t h, int64_t w, int64_t C, void *stream);
+
+/* The same on float32 NHWC tensors (C % 4 == 0). */
+int sci_cnn_shuffle_add_f32(const float *a, const float *u, float *out, int64_t N,
+                            int64_t h, int64_t w, int64_t C, void *stream);
 
 /* 3 x 3 convolution (zero padding 1, stride 1) of a thin input on the
  * tensor cores (tcgen05.mma, float32 accumulation in tensor memory):

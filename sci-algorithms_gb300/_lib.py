@@ -104,6 +104,7 @@ _SIGS = {
     "sci_cnn_center_sub": [c_vp, c_i64, c_i64, c_i64, c_i64, c_i64, c_vp, ctypes.c_int,
                            ctypes.c_int, c_i64, c_i64, c_i64, c_i64, ctypes.c_int, c_vp, c_vp],
     "sci_cnn_shuffle_add": [c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_i64, c_vp],
+    "sci_cnn_shuffle_add_f32": [c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_i64, c_vp],
     "sci_cnn_conv_thin": [c_vp, c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, ctypes.c_int,
                           ctypes.c_int, c_vp],
     "sci_unrolled_workspace_bytes": [c_i64, c_i64, c_i64, c_i64, ctypes.c_int, ctypes.c_int,

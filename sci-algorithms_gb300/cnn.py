@@ -26,10 +26,12 @@ reference's per-frame loops:
   (``sci_cnn_*``: 2 x 2 space-to-depth with the noise map, the circular
   frame window with reflect padding, and the final subtraction / crop /
   [0, 1] clip) straight from the planar frame stack;
-* ``precision``: 'fp32' (IEEE convolutions), 'tf32' (cuDNN's default, what
-  the reference's GPU run computes in) or 'bf16' (bfloat16 NHWC tensor-core
-  convolutions, channels padded to multiples of 8, float32 frames in and
-  out);
+* activations are channels-last (NHWC) with channel counts padded to
+  multiples of 8 (cuDNN's NHWC kernels run TF32 about 5x faster than NCHW
+  on GB300); ``precision``: 'fp32' (IEEE convolutions), 'tf32' (cuDNN's
+  default, what the reference's GPU run computes in) or 'bf16' (bfloat16
+  tensor-core convolutions, the first layer by this library's tcgen05
+  kernel); frames are float32 in and out;
 * each (frames, H, W) shape is captured once as a CUDA graph and replayed.
 
 The trained weights are not part of the reference tree (git-LFS pointers),
@@ -47,6 +49,7 @@ from ._lib import call
 
 NCHW_F32 = 0  # SCI_CNN_NCHW_F32
 NHWC8_BF16 = 1  # SCI_CNN_NHWC8_BF16
+NHWC8_F32 = 2  # SCI_CNN_NHWC8_F32
 PRECISIONS = ("fp32", "tf32", "bf16")
 _default_precision = "tf32"
 
@@ -391,6 +394,10 @@ class CnnEngine:
         if self.precision not in PRECISIONS:
             raise ValueError("precision must be one of %s" % (PRECISIONS,))
         self.bf16 = self.precision == "bf16"
+        # channels-last everywhere (cuDNN's NHWC kernels: TF32 about 5x its
+        # NCHW rate on GB300); NHWC8 frames in / out of the glue kernels
+        self.dtype = torch.bfloat16 if self.bf16 else torch.float32
+        self.layout = NHWC8_BF16 if self.bf16 else NHWC8_F32
         # first layer on the tensor cores by this library's tcgen05 kernel
         # (bf16 only; SCI_CNN_TC=0 leaves it to cuDNN)
         self.tc = self.bf16 and os.environ.get("SCI_CNN_TC", "1") != "0"
@@ -407,67 +414,74 @@ class CnnEngine:
         return tuple(t._version for t in list(self.net.parameters()) + list(self.net.buffers()))
 
     def _fold(self):
+        """Folded, channel-padded weights in the execution dtype, NHWC."""
         net = self.net.to(self.dev).eval()
-        dt = torch.bfloat16 if self.bf16 else torch.float32
-        cl = self.bf16
+        dt = self.dtype
         if self.kind == "ffdnet":
-            C = net.num_input_channels
-            if self.bf16 and C != 1:
-                raise ValueError("bf16 FFDNet runs the grayscale network")
+            if net.num_input_channels != 1:
+                raise ValueError("the frame-stack engine runs the grayscale FFDNet")
             layers = []
             for i, conv in enumerate(net.convs):
                 bn = net.norms[i - 1] if 0 < i < len(net.convs) - 1 else None
-                cin_pad = 8 if (self.bf16 and i == 0) else None
-                cout_pad = 8 if (self.bf16 and i == len(net.convs) - 1) else None
-                layers.append(_fold(conv, bn, dt, cin_pad, cout_pad, cl))
+                cin_pad = 8 if i == 0 else None                    # NHWC8 input
+                cout_pad = 8 if i == len(net.convs) - 1 else None  # 4 -> 8 outputs
+                layers.append(_fold(conv, bn, dt, cin_pad, cout_pad, cl=True))
             self.layers = layers
             self.first_tc = _pack_thin(*layers[0]) if self.tc else None
         else:
+            if net.num_color_channels != 1:
+                raise ValueError("the frame-stack engine runs the grayscale FastDVDnet")
             self.blocks = []
             for blk in (net.temp1, net.temp2):
                 p = {}
                 for name, _, bpath in _DEN_LAYERS:
                     conv = blk.conv[name]
                     bn = blk.bn[name] if bpath is not None else None
-                    if self.bf16 and name == "in0":
-                        if net.num_color_channels != 1:
-                            raise ValueError("bf16 FastDVDnet runs the grayscale network")
+                    if name == "in0":
+                        # the 3-group input convolution as one dense 8 -> 96
+                        # filter on the NHWC8 window (channels 6, 7 and
+                        # outputs 90..95 zero)
                         w, b = _fold(conv, bn, torch.float32)
                         w = F.pad(_dense_groups(w, 3, 6), (0, 0, 0, 0, 0, 2))
-                        w = F.pad(w, (0, 0, 0, 0, 0, 0, 0, 6))  # 90 -> 96 outputs
+                        w = F.pad(w, (0, 0, 0, 0, 0, 0, 0, 6))
                         b = F.pad(b, (0, 6))
                         p[name] = (w.to(dt).contiguous(memory_format=torch.channels_last),
                                    b.to(dt))
                         if self.tc:
                             p["in0_tc"] = _pack_thin(*p[name])
-                    elif self.bf16 and name == "in1":
+                    elif name == "in1":
                         p[name] = _fold(conv, bn, dt, cin_pad=96, cl=True)
-                    elif self.bf16 and name == "o1":
+                    elif name == "o1":
                         p[name] = _fold(conv, bn, dt, cout_pad=8, cl=True)
-                    elif self.bf16 and name in ("u2c", "u1c"):
+                    elif name in ("u2c", "u1c"):
                         w, b = _fold(conv, bn, dt)
                         p[name] = (_subpixel_major(w).contiguous(
                             memory_format=torch.channels_last), b)
                     else:
-                        p[name] = _fold(conv, bn, dt, cl=cl)
+                        p[name] = _fold(conv, bn, dt, cl=True)
                 self.blocks.append(p)
         self._versions = self._param_versions()
         self._graphs.clear()
+
+    def _nhwc(self, n, H, W, C, dev):
+        """An NHWC tensor (n, H, W, C) of the execution dtype."""
+        return torch.empty((n, H, W, C), dtype=self.dtype, device=dev)
+
+    @staticmethod
+    def _dense(t):
+        """The NHWC storage of a channels-last (n, C, H, W) view."""
+        n = t.permute(0, 2, 3, 1)
+        return n if n.is_contiguous() else n.contiguous()
 
     # -- FFDNet ------------------------------------------------------------
     def _ffdnet(self, x, out, clip):
         Fn, H, W = x.shape
         H2, W2 = (H + 1) // 2, (W + 1) // 2
         s = _dev.stream_handle()
-        if self.bf16:
-            h = torch.empty((Fn, H2, W2, 8), dtype=torch.bfloat16, device=x.device)
-            call("sci_cnn_ffdnet_pack", x.data_ptr(), Fn, H, W, self.sigma.data_ptr(),
-                 h.data_ptr(), NHWC8_BF16, s)
-            h = h.permute(0, 3, 1, 2)  # channels-last view
-        else:
-            h = torch.empty((Fn, 5 * self.net.num_input_channels, H2, W2), device=x.device)
-            call("sci_cnn_ffdnet_pack", x.data_ptr(), Fn, H, W, self.sigma.data_ptr(),
-                 h.data_ptr(), NCHW_F32, s)
+        h = self._nhwc(Fn, H2, W2, 8, x.device)
+        call("sci_cnn_ffdnet_pack", x.data_ptr(), Fn, H, W, self.sigma.data_ptr(), h.data_ptr(),
+             self.layout, s)
+        h = h.permute(0, 3, 1, 2)  # channels-last view
         L = self.layers
         tf32 = self.precision == "tf32"
         for i, (w, b) in enumerate(L):
@@ -475,15 +489,9 @@ class CnnEngine:
                 h = conv_thin(h, self.first_tc)
             else:
                 h = _conv_act(h, w, b, relu=i < len(L) - 1, tf32=tf32)
-        if self.bf16:
-            noise = h.permute(0, 2, 3, 1)
-            if not noise.is_contiguous():
-                noise = noise.contiguous()
-            call("sci_cnn_ffdnet_unpack_sub", x.data_ptr(), noise.data_ptr(), Fn, H, W,
-                 NHWC8_BF16, noise.shape[-1], int(clip), out.data_ptr(), s)
-        else:
-            call("sci_cnn_ffdnet_unpack_sub", x.data_ptr(), h.contiguous().data_ptr(), Fn, H, W,
-                 NCHW_F32, 4, int(clip), out.data_ptr(), s)
+        noise = self._dense(h)
+        call("sci_cnn_ffdnet_unpack_sub", x.data_ptr(), noise.data_ptr(), Fn, H, W, self.layout,
+             noise.shape[-1], int(clip), out.data_ptr(), s)
 
     # -- FastDVDnet ----------------------------------------------------------
     def _denblock(self, p, win):
@@ -491,64 +499,40 @@ class CnnEngine:
         output r (before `centre - r`)."""
         tf = self.precision == "tf32"
 
-        def c(x, name, stride=1, groups=1, relu=True):
+        def c(x, name, stride=1, relu=True):
             w, b = p[name]
-            return _conv_act(x, w, b, stride, groups, relu, tf)
+            return _conv_act(x, w, b, stride, 1, relu, tf)
 
-        if self.tc:
-            x0 = c(conv_thin(win, p["in0_tc"]), "in1")
-        else:
-            x0 = c(c(win, "in0", groups=1 if self.bf16 else 3), "in1")
+        x0 = c(conv_thin(win, p["in0_tc"]) if self.tc else c(win, "in0"), "in1")
         x1 = c(c(c(x0, "d0a", 2), "d0b"), "d0c")
         x2 = c(c(c(x1, "d1a", 2), "d1b"), "d1c")
         u2 = c(c(c(x2, "u2a"), "u2b"), "u2c", relu=False)
-        if not self.bf16:
-            x1 = x1 + F.pixel_shuffle(u2, 2)
-            u1 = c(c(c(x1, "u1a"), "u1b"), "u1c", relu=False)
-            return c(c(x0 + F.pixel_shuffle(u1, 2), "o0"), "o1", relu=False)
         x1 = self._shuffle_add(x1, u2)
         u1 = c(c(c(x1, "u1a"), "u1b"), "u1c", relu=False)
         return c(c(self._shuffle_add(x0, u1), "o0"), "o1", relu=False)
 
     def _shuffle_add(self, a, u):
-        """a + PixelShuffle(2)(u) on bfloat16 NHWC tensors (u's channels in
-        sub-pixel-major order), by sci_cnn_shuffle_add."""
+        """a + PixelShuffle(2)(u) on NHWC tensors (u's channels in
+        sub-pixel-major order), by sci_cnn_shuffle_add(_f32)."""
         N, C, H2, W2 = a.shape
-        an = a.permute(0, 2, 3, 1)
-        un = u.permute(0, 2, 3, 1)
-        an = an if an.is_contiguous() else an.contiguous()
-        un = un if un.is_contiguous() else un.contiguous()
-        out = torch.empty((N, H2, W2, C), dtype=a.dtype, device=a.device)
-        call("sci_cnn_shuffle_add", an.data_ptr(), un.data_ptr(), out.data_ptr(), N, H2 // 2,
-             W2 // 2, C, _dev.stream_handle())
+        an, un = self._dense(a), self._dense(u)
+        out = self._nhwc(N, H2, W2, C, a.device)
+        fn = "sci_cnn_shuffle_add" if self.bf16 else "sci_cnn_shuffle_add_f32"
+        call(fn, an.data_ptr(), un.data_ptr(), out.data_ptr(), N, H2 // 2, W2 // 2, C,
+             _dev.stream_handle())
         return out.permute(0, 3, 1, 2)
 
     def _window(self, src, Hs, Ws, Hp, Wp, first, count):
-        s = _dev.stream_handle()
-        Fn = src.shape[0]
-        if self.bf16:
-            w = torch.empty((count, Hp, Wp, 8), dtype=torch.bfloat16, device=src.device)
-            call("sci_cnn_window", src.data_ptr(), Fn, Hs, Ws, Hp, Wp, first, count,
-                 self.sigma.data_ptr(), w.data_ptr(), NHWC8_BF16, s)
-            return w.permute(0, 3, 1, 2)  # channels-last view
-        w = torch.empty((count, 6, Hp, Wp), device=src.device)
-        call("sci_cnn_window", src.data_ptr(), Fn, Hs, Ws, Hp, Wp, first, count,
-             self.sigma.data_ptr(), w.data_ptr(), NCHW_F32, s)
-        return w
+        w = self._nhwc(count, Hp, Wp, 8, src.device)
+        call("sci_cnn_window", src.data_ptr(), src.shape[0], Hs, Ws, Hp, Wp, first, count,
+             self.sigma.data_ptr(), w.data_ptr(), self.layout, _dev.stream_handle())
+        return w.permute(0, 3, 1, 2)  # channels-last view
 
     def _center_sub(self, src, Hs, Ws, first, count, r, Hp, Wp, Ho, Wo, clip, out):
-        s = _dev.stream_handle()
-        Fn = src.shape[0]
-        if self.bf16:
-            rr = r.permute(0, 2, 3, 1)
-            if not rr.is_contiguous():
-                rr = rr.contiguous()
-            call("sci_cnn_center_sub", src.data_ptr(), Fn, Hs, Ws, first, count, rr.data_ptr(),
-                 NHWC8_BF16, rr.shape[-1], Hp, Wp, Ho, Wo, int(clip), out.data_ptr(), s)
-        else:
-            call("sci_cnn_center_sub", src.data_ptr(), Fn, Hs, Ws, first, count,
-                 r.contiguous().data_ptr(), NCHW_F32, 1, Hp, Wp, Ho, Wo, int(clip),
-                 out.data_ptr(), s)
+        rr = self._dense(r)
+        call("sci_cnn_center_sub", src.data_ptr(), src.shape[0], Hs, Ws, first, count,
+             rr.data_ptr(), self.layout, rr.shape[-1], Hp, Wp, Ho, Wo, int(clip),
+             out.data_ptr(), _dev.stream_handle())
 
     def _fastdvdnet(self, x, out, clip):
         if self.net.num_color_channels != 1:
@@ -575,7 +559,7 @@ class CnnEngine:
     def _bytes_per_frame(self, Hp, Wp):
         # live activations of one DenBlock call at full resolution (~4
         # tensors of 96 channels) plus the half / quarter levels
-        e = 2 if self.bf16 else 4
+        e = 2 if self.bf16 else 4  # activations of the execution dtype
         return int(Hp * Wp * e * (4 * 96 + 2 * 64 + 2 * 32)) + 1
 
     # -- call ---------------------------------------------------------------

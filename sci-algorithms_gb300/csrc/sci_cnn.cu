@@ -16,9 +16,10 @@
 //   FastDVDnet output (models.py:205): centre frame - network output,
 //     cropped to Ho x Wo.
 //
-// Layouts: SCI_CNN_NCHW_F32 (planar float32) or SCI_CNN_NHWC8_BF16 (one
-// 16-byte vector of 8 bfloat16 channels per pixel, unused channels 0) for
-// the tensor-core convolutions.  The noise level is read from device memory
+// Layouts: SCI_CNN_NCHW_F32 (planar float32), SCI_CNN_NHWC8_BF16 (one
+// 16-byte vector of 8 bfloat16 channels per pixel, unused channels 0) and
+// SCI_CNN_NHWC8_F32 (8 float32 channels per pixel) for the channels-last
+// tensor-core convolutions.  The noise level is read from device memory
 // so that a captured CUDA graph replays with a new level.
 #include <cuda_bf16.h>
 
@@ -49,8 +50,29 @@ __device__ __forceinline__ uint4 pack8(float a0, float a1, float a2, float a3, f
     return r;
 }
 
+// 8 channels of one NHWC8 pixel: 8 bfloat16 (16 bytes) or 8 float32 (32 bytes)
+template <int LAYOUT>
+__device__ __forceinline__ void store8(void *out, int64_t t, float a0, float a1, float a2,
+                                       float a3, float a4, float a5, float a6, float a7) {
+    if (LAYOUT == SCI_CNN_NHWC8_BF16) {
+        reinterpret_cast<uint4 *>(out)[t] = pack8(a0, a1, a2, a3, a4, a5, a6, a7);
+    } else {
+        float4 *o = reinterpret_cast<float4 *>(out) + 2 * t;
+        o[0] = make_float4(a0, a1, a2, a3);
+        o[1] = make_float4(a4, a5, a6, a7);
+    }
+}
+
+// channel c of pixel p of an NHWC tensor with nch channels (bf16 or f32)
+template <int LAYOUT>
+__device__ __forceinline__ float load_ch(const void *r, int64_t p, int nch, int c) {
+    if (LAYOUT == SCI_CNN_NHWC8_BF16)
+        return __bfloat162float(reinterpret_cast<const __nv_bfloat16 *>(r)[p * nch + c]);
+    return __ldg(reinterpret_cast<const float *>(r) + p * nch + c);
+}
+
 // ------------------------------------------------------------ FFDNet pack
-template <bool BF16>
+template <int LAYOUT>
 __global__ void k_ffdnet_pack(const float *__restrict__ x, int64_t F, int64_t H, int64_t W,
                               const float *__restrict__ sigma, void *__restrict__ out) {
     const int64_t H2 = (H + 1) / 2, W2 = (W + 1) / 2, n = F * H2 * W2;
@@ -63,8 +85,8 @@ __global__ void k_ffdnet_pack(const float *__restrict__ x, int64_t F, int64_t H,
         const int64_t c0 = 2 * c, c1 = min(2 * c + 1, W - 1);
         const float d0 = __ldg(xf + r0 * W + c0), d1 = __ldg(xf + r0 * W + c1);
         const float d2 = __ldg(xf + r1 * W + c0), d3 = __ldg(xf + r1 * W + c1);
-        if (BF16) {
-            reinterpret_cast<uint4 *>(out)[t] = pack8(s, d0, d1, d2, d3, 0.f, 0.f, 0.f);
+        if (LAYOUT != SCI_CNN_NCHW_F32) {
+            store8<LAYOUT>(out, t, s, d0, d1, d2, d3, 0.f, 0.f, 0.f);
         } else {
             float *o = reinterpret_cast<float *>(out) + f * 5 * H2 * W2 + r * W2 + c;
             const int64_t pl = H2 * W2;
@@ -78,7 +100,7 @@ __global__ void k_ffdnet_pack(const float *__restrict__ x, int64_t F, int64_t H,
 }
 
 // -------------------------------------------------- FFDNet unpack + subtract
-template <bool BF16>
+template <int LAYOUT>
 __global__ void k_ffdnet_unpack_sub(const float *__restrict__ x, const void *__restrict__ noise,
                                     int64_t F, int64_t H, int64_t W, int nch, int clip,
                                     float *__restrict__ out) {
@@ -87,7 +109,14 @@ __global__ void k_ffdnet_unpack_sub(const float *__restrict__ x, const void *__r
          t += int64_t(gridDim.x) * blockDim.x) {
         const int64_t c = t % W2, r = (t / W2) % H2, f = t / (W2 * H2);
         float e[4];
-        if (BF16) {
+        if (LAYOUT == SCI_CNN_NHWC8_F32) {
+            const float4 v = __ldg(reinterpret_cast<const float4 *>(
+                reinterpret_cast<const float *>(noise) + t * nch));
+            e[0] = v.x;
+            e[1] = v.y;
+            e[2] = v.z;
+            e[3] = v.w;
+        } else if (LAYOUT == SCI_CNN_NHWC8_BF16) {
             const __nv_bfloat16 *q = reinterpret_cast<const __nv_bfloat16 *>(noise) + t * nch;
             const uint2 v = *reinterpret_cast<const uint2 *>(q);
             const __nv_bfloat162 a = *reinterpret_cast<const __nv_bfloat162 *>(&v.x);
@@ -119,7 +148,7 @@ __global__ void k_ffdnet_unpack_sub(const float *__restrict__ x, const void *__r
 }
 
 // ------------------------------------------------------ FastDVDnet window
-template <bool BF16>
+template <int LAYOUT>
 __global__ void k_window(const float *__restrict__ src, int64_t F, int64_t Hs, int64_t Ws,
                          int64_t Hp, int64_t Wp, int64_t first, int64_t count,
                          const float *__restrict__ sigma, void *__restrict__ out) {
@@ -133,8 +162,8 @@ __global__ void k_window(const float *__restrict__ src, int64_t F, int64_t Hs, i
         const float a = __ldg(src + gm * Hs * Ws + off);
         const float b = __ldg(src + g * Hs * Ws + off);
         const float c = __ldg(src + gp * Hs * Ws + off);
-        if (BF16) {
-            reinterpret_cast<uint4 *>(out)[t] = pack8(a, s, b, s, c, s, 0.f, 0.f);
+        if (LAYOUT != SCI_CNN_NCHW_F32) {
+            store8<LAYOUT>(out, t, a, s, b, s, c, s, 0.f, 0.f);
         } else {
             const int64_t pl = Hp * Wp;
             float *o = reinterpret_cast<float *>(out) + gl * 6 * pl + i * Wp + j;
@@ -149,7 +178,7 @@ __global__ void k_window(const float *__restrict__ src, int64_t F, int64_t Hs, i
 }
 
 // ---------------------------------------------- FastDVDnet centre - output
-template <bool BF16>
+template <int LAYOUT>
 __global__ void k_center_sub(const float *__restrict__ src, int64_t Hs, int64_t Ws,
                              int64_t first, int64_t count, const void *__restrict__ r, int nch,
                              int64_t Hp, int64_t Wp, int64_t Ho, int64_t Wo, int clip,
@@ -160,11 +189,8 @@ __global__ void k_center_sub(const float *__restrict__ src, int64_t Hs, int64_t 
         const int64_t j = t % Wo, i = (t / Wo) % Ho, gl = t / (Wo * Ho), g = first + gl;
         const float cen = __ldg(src + g * Hs * Ws + reflect_hi(i, Hs) * Ws + reflect_hi(j, Ws));
         const int64_t p = (gl * Hp + i) * Wp + j;
-        float e;
-        if (BF16)
-            e = __bfloat162float(reinterpret_cast<const __nv_bfloat16 *>(r)[p * nch]);
-        else
-            e = __ldg(reinterpret_cast<const float *>(r) + p);
+        const float e = (LAYOUT == SCI_CNN_NCHW_F32) ? __ldg(reinterpret_cast<const float *>(r) + p)
+                                                     : load_ch<LAYOUT>(r, p, nch, 0);
         float v = cen - e;
         if (clip) v = fminf(fmaxf(v, 0.f), 1.f);
         out[t] = v;
@@ -207,6 +233,26 @@ __global__ void k_shuffle_add(const uint4 *__restrict__ a, const uint4 *__restri
     }
 }
 
+// the same on float32 NHWC (4 channels per 16-byte vector, V = C / 4)
+__global__ void k_shuffle_add_f32(const float4 *__restrict__ a, const float4 *__restrict__ u,
+                                  float4 *__restrict__ out, int64_t N, int64_t h, int64_t w,
+                                  int64_t V) {
+    const int64_t n = N * h * w * 4 * V;
+    for (int64_t t = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; t < n;
+         t += int64_t(gridDim.x) * blockDim.x) {
+        const int64_t v = t % V, k = (t / V) % 4, pix = t / (4 * V);
+        const int64_t j = pix % w, i = (pix / w) % h, b = pix / (w * h);
+        const int64_t o = ((b * 2 * h + 2 * i + (k >> 1)) * 2 * w + 2 * j + (k & 1)) * V + v;
+        const float4 uv = __ldg(u + t);
+        if (a) {
+            const float4 av = __ldg(a + o);
+            out[o] = make_float4(av.x + uv.x, av.y + uv.y, av.z + uv.z, av.w + uv.w);
+        } else {
+            out[o] = uv;
+        }
+    }
+}
+
 int grid_for(int64_t n) {
     int64_t b = (n + kThreads - 1) / kThreads;
     const int64_t cap = int64_t(kSMs) * 16;
@@ -224,17 +270,21 @@ int sci_cnn_ffdnet_pack(const float *x, int64_t nframes, int64_t H, int64_t W,
                         const float *sigma, void *out, int layout, void *stream) {
     SCI_CHECK_ARG(x && sigma && out, "sci_cnn_ffdnet_pack: null pointer");
     SCI_CHECK_ARG(nframes >= 1 && H >= 1 && W >= 1, "sci_cnn_ffdnet_pack: invalid sizes");
-    SCI_CHECK_ARG(layout == SCI_CNN_NCHW_F32 || layout == SCI_CNN_NHWC8_BF16,
+    SCI_CHECK_ARG(layout >= SCI_CNN_NCHW_F32 && layout <= SCI_CNN_NHWC8_F32,
                   "sci_cnn_ffdnet_pack: unknown layout %d", layout);
-    SCI_CHECK_ARG(layout != SCI_CNN_NHWC8_BF16 || aligned16(out),
+    SCI_CHECK_ARG(layout == SCI_CNN_NCHW_F32 || aligned16(out),
                   "sci_cnn_ffdnet_pack: NHWC8 output must be 16-byte aligned");
     const int64_t n = nframes * ((H + 1) / 2) * ((W + 1) / 2);
+    const cudaStream_t st = as_stream(stream);
     if (layout == SCI_CNN_NHWC8_BF16)
-        k_ffdnet_pack<true><<<grid_for(n), kThreads, 0, as_stream(stream)>>>(x, nframes, H, W,
-                                                                            sigma, out);
+        k_ffdnet_pack<SCI_CNN_NHWC8_BF16><<<grid_for(n), kThreads, 0, st>>>(x, nframes, H, W,
+                                                                           sigma, out);
+    else if (layout == SCI_CNN_NHWC8_F32)
+        k_ffdnet_pack<SCI_CNN_NHWC8_F32><<<grid_for(n), kThreads, 0, st>>>(x, nframes, H, W,
+                                                                          sigma, out);
     else
-        k_ffdnet_pack<false><<<grid_for(n), kThreads, 0, as_stream(stream)>>>(x, nframes, H, W,
-                                                                             sigma, out);
+        k_ffdnet_pack<SCI_CNN_NCHW_F32><<<grid_for(n), kThreads, 0, st>>>(x, nframes, H, W,
+                                                                         sigma, out);
     SCI_LAUNCHED("k_ffdnet_pack");
     return SCI_OK;
 }
@@ -244,18 +294,22 @@ int sci_cnn_ffdnet_unpack_sub(const float *x, const void *noise, int64_t nframes
                               void *stream) {
     SCI_CHECK_ARG(x && noise && out, "sci_cnn_ffdnet_unpack_sub: null pointer");
     SCI_CHECK_ARG(nframes >= 1 && H >= 1 && W >= 1, "sci_cnn_ffdnet_unpack_sub: invalid sizes");
-    SCI_CHECK_ARG(layout == SCI_CNN_NCHW_F32 || layout == SCI_CNN_NHWC8_BF16,
+    SCI_CHECK_ARG(layout >= SCI_CNN_NCHW_F32 && layout <= SCI_CNN_NHWC8_F32,
                   "sci_cnn_ffdnet_unpack_sub: unknown layout %d", layout);
-    SCI_CHECK_ARG(layout != SCI_CNN_NHWC8_BF16 ||
+    SCI_CHECK_ARG(layout == SCI_CNN_NCHW_F32 ||
                       ((channels == 4 || channels == 8) &&
-                       (reinterpret_cast<uintptr_t>(noise) & 7u) == 0),
-                  "sci_cnn_ffdnet_unpack_sub: bf16 noise needs 4 or 8 channels, 8-byte aligned");
+                       (reinterpret_cast<uintptr_t>(noise) & 15u) == 0),
+                  "sci_cnn_ffdnet_unpack_sub: NHWC noise needs 4 or 8 channels, 16-byte aligned");
     const int64_t n = nframes * ((H + 1) / 2) * ((W + 1) / 2);
+    const cudaStream_t st = as_stream(stream);
     if (layout == SCI_CNN_NHWC8_BF16)
-        k_ffdnet_unpack_sub<true><<<grid_for(n), kThreads, 0, as_stream(stream)>>>(
+        k_ffdnet_unpack_sub<SCI_CNN_NHWC8_BF16><<<grid_for(n), kThreads, 0, st>>>(
+            x, noise, nframes, H, W, channels, clip, out);
+    else if (layout == SCI_CNN_NHWC8_F32)
+        k_ffdnet_unpack_sub<SCI_CNN_NHWC8_F32><<<grid_for(n), kThreads, 0, st>>>(
             x, noise, nframes, H, W, channels, clip, out);
     else
-        k_ffdnet_unpack_sub<false><<<grid_for(n), kThreads, 0, as_stream(stream)>>>(
+        k_ffdnet_unpack_sub<SCI_CNN_NCHW_F32><<<grid_for(n), kThreads, 0, st>>>(
             x, noise, nframes, H, W, 4, clip, out);
     SCI_LAUNCHED("k_ffdnet_unpack_sub");
     return SCI_OK;
@@ -272,16 +326,20 @@ int sci_cnn_window(const float *src, int64_t nframes, int64_t Hs, int64_t Ws, in
                   (long long)first, (long long)(first + count), (long long)nframes);
     SCI_CHECK_ARG((Hp == Hs || Hp - Hs < Hs) && (Wp == Ws || Wp - Ws < Ws),
                   "sci_cnn_window: reflect padding must be shorter than the frame");
-    SCI_CHECK_ARG(layout == SCI_CNN_NCHW_F32 || layout == SCI_CNN_NHWC8_BF16,
+    SCI_CHECK_ARG(layout >= SCI_CNN_NCHW_F32 && layout <= SCI_CNN_NHWC8_F32,
                   "sci_cnn_window: unknown layout %d", layout);
-    SCI_CHECK_ARG(layout != SCI_CNN_NHWC8_BF16 || aligned16(out),
+    SCI_CHECK_ARG(layout == SCI_CNN_NCHW_F32 || aligned16(out),
                   "sci_cnn_window: NHWC8 output must be 16-byte aligned");
     const int64_t n = count * Hp * Wp;
+    const cudaStream_t st = as_stream(stream);
     if (layout == SCI_CNN_NHWC8_BF16)
-        k_window<true><<<grid_for(n), kThreads, 0, as_stream(stream)>>>(
+        k_window<SCI_CNN_NHWC8_BF16><<<grid_for(n), kThreads, 0, st>>>(
+            src, nframes, Hs, Ws, Hp, Wp, first, count, sigma, out);
+    else if (layout == SCI_CNN_NHWC8_F32)
+        k_window<SCI_CNN_NHWC8_F32><<<grid_for(n), kThreads, 0, st>>>(
             src, nframes, Hs, Ws, Hp, Wp, first, count, sigma, out);
     else
-        k_window<false><<<grid_for(n), kThreads, 0, as_stream(stream)>>>(
+        k_window<SCI_CNN_NCHW_F32><<<grid_for(n), kThreads, 0, st>>>(
             src, nframes, Hs, Ws, Hp, Wp, first, count, sigma, out);
     SCI_LAUNCHED("k_window");
     return SCI_OK;
@@ -299,16 +357,20 @@ int sci_cnn_center_sub(const float *src, int64_t nframes, int64_t Hs, int64_t Ws
                   "sci_cnn_center_sub: centre frames outside the stack");
     SCI_CHECK_ARG((Hp == Hs || Hp - Hs < Hs) && (Wp == Ws || Wp - Ws < Ws),
                   "sci_cnn_center_sub: reflect padding must be shorter than the frame");
-    SCI_CHECK_ARG(layout == SCI_CNN_NCHW_F32 || layout == SCI_CNN_NHWC8_BF16,
+    SCI_CHECK_ARG(layout >= SCI_CNN_NCHW_F32 && layout <= SCI_CNN_NHWC8_F32,
                   "sci_cnn_center_sub: unknown layout %d", layout);
-    SCI_CHECK_ARG(layout != SCI_CNN_NHWC8_BF16 || channels >= 1,
-                  "sci_cnn_center_sub: bf16 output needs its channel count");
+    SCI_CHECK_ARG(layout == SCI_CNN_NCHW_F32 || channels >= 1,
+                  "sci_cnn_center_sub: an NHWC output needs its channel count");
     const int64_t n = count * Ho * Wo;
+    const cudaStream_t st = as_stream(stream);
     if (layout == SCI_CNN_NHWC8_BF16)
-        k_center_sub<true><<<grid_for(n), kThreads, 0, as_stream(stream)>>>(
+        k_center_sub<SCI_CNN_NHWC8_BF16><<<grid_for(n), kThreads, 0, st>>>(
+            src, Hs, Ws, first, count, r, channels, Hp, Wp, Ho, Wo, clip, out);
+    else if (layout == SCI_CNN_NHWC8_F32)
+        k_center_sub<SCI_CNN_NHWC8_F32><<<grid_for(n), kThreads, 0, st>>>(
             src, Hs, Ws, first, count, r, channels, Hp, Wp, Ho, Wo, clip, out);
     else
-        k_center_sub<false><<<grid_for(n), kThreads, 0, as_stream(stream)>>>(
+        k_center_sub<SCI_CNN_NCHW_F32><<<grid_for(n), kThreads, 0, st>>>(
             src, Hs, Ws, first, count, r, 1, Hp, Wp, Ho, Wo, clip, out);
     SCI_LAUNCHED("k_center_sub");
     return SCI_OK;
@@ -327,6 +389,22 @@ int sci_cnn_shuffle_add(const void *a, const void *u, void *out, int64_t N, int6
         reinterpret_cast<const uint4 *>(a), reinterpret_cast<const uint4 *>(u),
         reinterpret_cast<uint4 *>(out), N, h, w, C / 8);
     SCI_LAUNCHED("k_shuffle_add");
+    return SCI_OK;
+}
+
+int sci_cnn_shuffle_add_f32(const float *a, const float *u, float *out, int64_t N, int64_t h,
+                            int64_t w, int64_t C, void *stream) {
+    SCI_CHECK_ARG(u && out, "sci_cnn_shuffle_add_f32: null pointer");
+    SCI_CHECK_ARG(N >= 1 && h >= 1 && w >= 1 && C >= 4 && C % 4 == 0,
+                  "sci_cnn_shuffle_add_f32: invalid sizes (C must be a multiple of 4)");
+    SCI_CHECK_ARG(aligned16(u) && aligned16(out) && (!a || aligned16(a)),
+                  "sci_cnn_shuffle_add_f32: buffers must be 16-byte aligned");
+    SCI_CHECK_ARG(out != u, "sci_cnn_shuffle_add_f32: out must not alias u");
+    const int64_t n = N * h * w * 4 * (C / 4);
+    k_shuffle_add_f32<<<grid_for(n), kThreads, 0, as_stream(stream)>>>(
+        reinterpret_cast<const float4 *>(a), reinterpret_cast<const float4 *>(u),
+        reinterpret_cast<float4 *>(out), N, h, w, C / 4);
+    SCI_LAUNCHED("k_shuffle_add_f32");
     return SCI_OK;
 }
 
