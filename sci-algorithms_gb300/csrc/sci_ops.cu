@@ -37,7 +37,7 @@ int launch_proj_gap_tma(const float *x, const uint32_t *bits, const float *y, fl
                         cudaStream_t s);
 int launch_proj_admm_tma(const float *th, const float *bb, const uint32_t *bits, const float *y,
                          const float *phisum, float *v, float *xo, float lam, float gamma, int B,
-                         int64_t hw, cudaStream_t s);
+                         int64_t hw, cudaStream_t s, bool b_from_v = false);
 
 // Grid for a grid-stride loop over `n` work units of one thread each.
 static inline dim3 grid_for(int64_t n, int threads) {

@@ -154,7 +154,9 @@ __device__ __forceinline__ void issue_theta(float *xs, uint64_t *bars, int buf, 
     for (int b = 0; b < B; ++b) bulk_g2s(dst + b * TP, th + b * hw + p0, n * 4u, bars + buf);
 }
 
-template <int TP, bool WANT_X>
+// BFV: the multiplier comes as the previous TV input, b = theta - bb (the
+// TV's residual u - f, formed here instead of stored by the TV pass).
+template <int TP, bool WANT_X, bool BFV = false>
 __global__ void __launch_bounds__(TP / 4) k_proj_admm_tma(
     const float *__restrict__ th, const float *__restrict__ bb, const uint32_t *__restrict__ bits,
     const float *__restrict__ y, const float *__restrict__ phisum, float *__restrict__ v,
@@ -194,7 +196,12 @@ __global__ void __launch_bounds__(TP / 4) k_proj_admm_tma(
         if (p0 + q < hw) {
             const int64_t p = p0 + q;
             const float *tb = xs + (int64_t)buf * B * TP + q;
-            auto bload = [&](int b) { return ldg4(bb + b * hw + p); };
+            auto bload = [&](int b) {
+                if (!BFV) return ldg4(bb + b * hw + p);
+                const float4 a = *reinterpret_cast<const float4 *>(tb + b * TP);
+                const float4 f = ldg4(bb + b * hw + p);
+                return make_float4(a.x - f.x, a.y - f.y, a.z - f.z, a.w - f.w);
+            };
             const uint4 w = __ldg(reinterpret_cast<const uint4 *>(bits + p));
             float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll 4
@@ -273,10 +280,11 @@ int launch_proj_gap_tma(const float *x, const uint32_t *bits, const float *y, fl
 
 // ADMM projection with a packed mask (B <= 32, 16-byte aligned planes,
 // hw % 4 == 0); SCI_ERR_UNSUPPORTED otherwise.  Tiles of TP pixels x B
-// rows, double-buffered (24 KB at 24 frames and TP = 128).
+// rows, double-buffered (24 KB at 24 frames and TP = 128).  b_from_v: bb
+// is the previous TV input v and b = theta - v (bitwise the TV's residual).
 int launch_proj_admm_tma(const float *th, const float *bb, const uint32_t *bits, const float *y,
                          const float *phisum, float *v, float *xo, float lam, float gamma, int B,
-                         int64_t hw, cudaStream_t s) {
+                         int64_t hw, cudaStream_t s, bool b_from_v) {
     const uintptr_t a = reinterpret_cast<uintptr_t>(th) | reinterpret_cast<uintptr_t>(bb) |
                         reinterpret_cast<uintptr_t>(bits) | reinterpret_cast<uintptr_t>(y) |
                         reinterpret_cast<uintptr_t>(phisum) | reinterpret_cast<uintptr_t>(v) |
@@ -291,7 +299,10 @@ int launch_proj_admm_tma(const float *th, const float *bb, const uint32_t *bits,
         const int64_t per_sm =
             std::max<int64_t>(1, std::min<int64_t>(16, (227 * 1024) / (int64_t)(smem + 1024)));
         const unsigned g = (unsigned)std::min<int64_t>(ntiles, per_sm * kSMs);
-        auto kern = xo ? k_proj_admm_tma<TP, true> : k_proj_admm_tma<TP, false>;
+        auto kern = b_from_v ? (xo ? k_proj_admm_tma<TP, true, true>
+                                   : k_proj_admm_tma<TP, false, true>)
+                             : (xo ? k_proj_admm_tma<TP, true, false>
+                                   : k_proj_admm_tma<TP, false, false>);
         SCI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
         kern<<<g, TP / 4, smem, s>>>(th, bb, bits, y, phisum, v, xo, lam, gamma, B, hw);

@@ -27,6 +27,9 @@ int tvx_launch(int kind, const float *f, float *u, float *resid, int64_t nf, int
                int64_t W, float lam, int iters, int *steps, void *ws, size_t ws_bytes,
                cudaStream_t s);
 size_t tvx_workspace_bytes(int kind, int64_t nf, int64_t H, int64_t W, int iters);
+int launch_proj_admm_tma(const float *th, const float *bb, const uint32_t *bits, const float *y,
+                         const float *phisum, float *v, float *xo, float lam, float gamma, int B,
+                         int64_t hw, cudaStream_t s, bool b_from_v);
 
 namespace {
 
@@ -221,6 +224,32 @@ int enqueue(const Args &a, cudaStream_t s) {
     }
     // admm_denoise: theta = x0, b = 0  (pnp_sci_algo.py:800-802)
     SCI_CUDA(cudaMemcpyAsync(w.theta, a.x0, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+    const char *bv = getenv("SCI_ADMM_B_FROM_V");
+    if (a.bits && aligned && hw % 4 == 0 && B <= 32 && !(bv && bv[0] == '0')) {
+        // b = b - (x - theta) = theta - v (pnp_sci_algo.py:836) is the TV's
+        // residual: the next projection forms it from theta and the TV input
+        // v, so the TV pass writes no residual (20N instead of 24N bytes per
+        // iteration, the same values bit for bit).  v ping-pongs between b0
+        // and b1; v_{-1} = theta_0 gives b_0 = 0.
+        SCI_CUDA(cudaMemcpyAsync(w.b1, a.x0, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+        float *vprev = w.b1, *vcur = w.b0;
+        for (int it = 0; it < o.iters; ++it) {
+            const bool want_x = (it == o.iters - 1) || (o.orig && o.sqerr);
+            const float gamma = o.gammas ? o.gammas[it] : o.gamma;
+            int e = launch_proj_admm_tma(w.theta, vprev, a.bits, a.y, a.phisum, vcur,
+                                         want_x ? a.x_out : nullptr, o.lambdas[it], gamma,
+                                         (int)B, hw, s, true);
+            if (e) return e;
+            e = denoise(vcur, w.theta, nullptr, it);
+            if (e) return e;
+            if (o.orig && o.sqerr) {
+                e = sci_sqerr_accum(o.orig, a.x_out, n, o.sqerr + it, s);
+                if (e) return e;
+            }
+            std::swap(vprev, vcur);
+        }
+        return SCI_OK;
+    }
     SCI_CUDA(cudaMemsetAsync(w.b0, 0, sizeof(float) * n, s));
     float *bcur = w.b0, *bnext = w.b1;
     for (int it = 0; it < o.iters; ++it) {

@@ -164,6 +164,26 @@ def test_run_host_end_to_end():
     assert torch.equal(x_host, ref)
 
 
+@pytest.mark.parametrize("tvm", ["tv_chambolle", "ATV_ClipA", "ITV3D_cham"])
+@pytest.mark.parametrize("with_orig", [False, True])
+def test_admm_multiplier_from_tv_input_is_bitwise_equal(monkeypatch, tvm, with_orig):
+    """ADMM forming b = theta - v in the projection (no residual written by
+    the TV) against the stored-residual loop (SCI_ADMM_B_FROM_V=0)."""
+    orig, mask, meas = sci.datasets.video_config(64, 96, 8, noise_rel=0.01)
+    op = sci.MaskOperator(mask)
+    y = _dev.plane(meas)
+    o = _dev.planar(orig) if with_orig else None
+    gam = np.linspace(0.01, 0.02, 7).astype(np.float32)
+    a = sci.Solver(op, "admm", 7, 1.0, 0.1, 5, gammas=gam, tvm=tvm)
+    xa = a.run(y, orig=o).clone()
+    monkeypatch.setenv("SCI_ADMM_B_FROM_V", "0")
+    b = sci.Solver(op, "admm", 7, 1.0, 0.1, 5, gammas=gam, tvm=tvm)
+    xb = b.run(y, orig=o).clone()
+    assert torch.equal(xa, xb)
+    if with_orig:  # the float64 atomic sums of the squared error may differ in order
+        assert np.allclose(a.psnr_all(), b.psnr_all(), rtol=0, atol=1e-9)
+
+
 def test_run_host_many_pipelined():
     """Several measurements through the pipelined host API: each result
     equals its own device solve (the alternating slots and the copy stream
