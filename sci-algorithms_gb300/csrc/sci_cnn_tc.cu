@@ -20,8 +20,14 @@
 // tile's pixels are contiguous in the NHWC output), which drains while the
 // block gathers its next tile.
 //
-// Persistent blocks of 128 threads; 64 KiB of shared memory per block caps
-// residency at 3 blocks per SM (3 x 128 of the SM's 512 TMEM columns).
+// Two tilings: k_conv_thin_rows (the default) takes 128-pixel segments of a
+// frame row, stages the three input row segments a tile needs in shared
+// memory by bulk copies two tiles ahead, and builds the im2col rows from
+// them; k_conv_thin_tc takes any 128 consecutive pixels and gathers each
+// row's nine taps from global memory by cp.async.
+//
+// Persistent blocks of 128 threads; 64 / 74 KiB of shared memory per block
+// caps residency at 3 blocks per SM (3 x 128 of the SM's 512 TMEM columns).
 // The wait for each tile's MMAs is bounded: on timeout the block sets bit 0
 // of the CNN status word, waits once more (bounded) for the MMAs in
 // flight, frees its tensor memory and returns.
@@ -44,14 +50,11 @@ constexpr int kCore = 128;               // bytes of one core matrix (8 rows x 1
 constexpr int kSBO = kKC * kCore;        // bytes between 8-row groups
 constexpr int kATile = (kM / 8) * kSBO;  // 20 KiB
 constexpr int kTmemCols = 128;
-// shared memory requested per block: 64 KiB with one A buffer (3 blocks per
-// SM), 100 KiB with two (2 blocks per SM)
-template <int NBUF>
-__host__ __device__ constexpr int smem_bytes() { return NBUF == 1 ? 64 * 1024 : 100 * 1024; }
+constexpr int kSmemBytes = 64 * 1024;  // requested per block: at most 3 blocks per SM
 
-template <int N, int NBUF>
+template <int N>
 struct alignas(1024) TcSmem {
-    uint8_t a[NBUF][kATile];
+    uint8_t a[kATile];
     uint8_t b[(N / 8) * kSBO];
     uint8_t stage[kM * N * 2];  // the tile's output, pixel-major (NHWC)
     float bias[N];
@@ -147,18 +150,15 @@ __device__ __forceinline__ void gather_row(const uint4 *__restrict__ in, uint8_t
     }
 }
 
-// NBUF = 2: the gather of the block's next tile is issued before the
-// current tile's MMAs and epilogue, so its latency overlaps them.
-template <int N, int NBUF>
-__global__ void __launch_bounds__(kThr, NBUF == 1 ? 3 : 2)
+template <int N>
+__global__ void __launch_bounds__(kThr, 3)
     k_conv_thin_tc(const uint4 *__restrict__ in, const uint4 *__restrict__ wts,
                    const float *__restrict__ bias, uint4 *__restrict__ out, int64_t F,
                    int64_t H, int64_t W, int relu) {
     static_assert(N % 32 == 0 && N >= 32 && N <= 256, "N: multiple of 32 up to 256");
-    static_assert(sizeof(TcSmem<N, NBUF>) + 1024 <= smem_bytes<NBUF>(),
-                  "shared memory layout too large");
+    static_assert(sizeof(TcSmem<N>) + 1024 <= kSmemBytes, "shared memory layout too large");
     extern __shared__ uint8_t smem_raw[];
-    TcSmem<N, NBUF> &s = *reinterpret_cast<TcSmem<N, NBUF> *>(
+    TcSmem<N> &s = *reinterpret_cast<TcSmem<N> *>(
         (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
     const int tid = threadIdx.x, warp = tid >> 5;
 
@@ -169,9 +169,7 @@ __global__ void __launch_bounds__(kThr, NBUF == 1 ? 3 : 2)
     }
     for (int i = tid; i < N; i += kThr) s.bias[i] = bias[i];
     const int row_off = (tid >> 3) * kSBO + (tid & 7) * 16;
-#pragma unroll
-    for (int b = 0; b < NBUF; ++b)
-        *reinterpret_cast<uint4 *>(s.a[b] + row_off + 9 * kCore) = make_uint4(0u, 0u, 0u, 0u);
+    *reinterpret_cast<uint4 *>(s.a + row_off + 9 * kCore) = make_uint4(0u, 0u, 0u, 0u);
     if (tid == 0) {
         mbar_init(&s.bar, 1);
         asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
@@ -193,28 +191,16 @@ __global__ void __launch_bounds__(kThr, NBUF == 1 ? 3 : 2)
 
     const int64_t P = F * H * W, ntiles = (P + kM - 1) / kM;
     unsigned phase = 0;
-    if (NBUF == 2) {
-        gather_row(in, s.a[0] + row_off, blockIdx.x * kM + tid, P, H, W);
-        asm volatile("cp.async.commit_group;" ::: "memory");
-    }
-    int buf = 0;
-    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x, buf ^= (NBUF - 1)) {
+    for (int64_t tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
         const int64_t p = tile * kM + tid;
-        if (NBUF == 2) {
-            const int64_t nxt = tile + gridDim.x;
-            if (nxt < ntiles) gather_row(in, s.a[buf ^ 1] + row_off, nxt * kM + tid, P, H, W);
-            asm volatile("cp.async.commit_group;" ::: "memory");
-            asm volatile("cp.async.wait_group 1;" ::: "memory");  // this tile's copies
-        } else {
-            gather_row(in, s.a[0] + row_off, p, P, H, W);
-            asm volatile("cp.async.wait_all;" ::: "memory");
-        }
+        gather_row(in, s.a + row_off, p, P, H, W);
+        asm volatile("cp.async.wait_all;" ::: "memory");
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         tc_fence_before();  // the previous tile's tcgen05.ld before the barrier
         __syncthreads();
         tc_fence_after();
         if (tid == 0) {
-            const uint32_t a_addr = smem_u32(s.a[buf]);
+            const uint32_t a_addr = smem_u32(s.a);
 #pragma unroll
             for (int kk = 0; kk < kKC / 2; ++kk)
                 tc_mma(tmem, smem_desc(a_addr + kk * 2 * kCore), smem_desc(b_addr + kk * 2 * kCore),
@@ -273,34 +259,241 @@ __global__ void __launch_bounds__(kThr, NBUF == 1 ? 3 : 2)
                      : "memory");
 }
 
-template <int N, int NBUF>
+// Row-segment tiles: a tile is kM = 128 consecutive pixels of one frame row
+// (x0 = 128 k; the last segment of a row may be shorter).  One thread
+// copies the tile's three input row segments (columns x0 - 1 .. x0 + 128,
+// clipped to the frame) into shared memory with bulk copies, two tiles
+// ahead (double-buffered, mbarrier-completed); the block then builds the
+// im2col rows from shared memory (zeros outside the frame) instead of nine
+// gathers per pixel from L2.
+constexpr int kRowPx = kM + 2;                 // staged pixels per input row
+constexpr int kRowBuf = 3 * kRowPx * 16;       // bytes of one tile's three rows
+constexpr int kSmemRows = 74 * 1024;           // 3 blocks per SM
+
+template <int N>
+struct alignas(1024) RowSmem {
+    uint8_t a[kATile];
+    uint8_t b[(N / 8) * kSBO];
+    uint8_t stage[kM * N * 2];
+    uint8_t rows[2][kRowBuf];
+    float bias[N];
+    uint64_t rbar[2];  // row copies of buffer 0 / 1
+    uint64_t bar;      // MMA completion
+    uint32_t tmem;
+};
+
+struct RowTile {
+    int64_t f, y, x0;
+    int nv;  // valid pixels
+};
+
+__device__ __forceinline__ RowTile row_tile(int64_t t, int64_t H, int64_t W, int64_t nseg) {
+    RowTile r;
+    const int64_t sg = t % nseg, fy = t / nseg;
+    r.y = fy % H;
+    r.f = fy / H;
+    r.x0 = sg * kM;
+    r.nv = (int)((W - r.x0) < kM ? (W - r.x0) : kM);
+    return r;
+}
+
+// thread 0: bulk copies of tile t's input rows into rows buffer `buf`
+__device__ __forceinline__ void issue_rows(const uint4 *in, uint8_t *rows, uint64_t *bar,
+                                          int64_t t, int64_t H, int64_t W, int64_t nseg) {
+    const RowTile r = row_tile(t, H, W, nseg);
+    const int64_t c0 = r.x0 - 1 < 0 ? 0 : r.x0 - 1;
+    const int64_t c1 = (r.x0 + kM + 1) < W ? (r.x0 + kM + 1) : W;  // exclusive
+    unsigned bytes = 0;
+    for (int dy = 0; dy < 3; ++dy) {
+        const int64_t yy = r.y + dy - 1;
+        if (yy >= 0 && yy < H) bytes += (unsigned)((c1 - c0) * 16);
+    }
+    mbar_expect_tx(bar, bytes);
+    for (int dy = 0; dy < 3; ++dy) {
+        const int64_t yy = r.y + dy - 1;
+        if (yy < 0 || yy >= H) continue;
+        uint8_t *dst = rows + dy * kRowPx * 16 + (c0 - (r.x0 - 1)) * 16;
+        bulk_g2s(dst, in + (r.f * H + yy) * W + c0, (unsigned)((c1 - c0) * 16), bar);
+    }
+}
+
+template <int N>
+__global__ void __launch_bounds__(kThr, 3)
+    k_conv_thin_rows(const uint4 *__restrict__ in, const uint4 *__restrict__ wts,
+                     const float *__restrict__ bias, uint4 *__restrict__ out, int64_t F,
+                     int64_t H, int64_t W, int relu) {
+    static_assert(N % 32 == 0 && N >= 32 && N <= 256, "N: multiple of 32 up to 256");
+    static_assert(sizeof(RowSmem<N>) + 1024 <= kSmemRows, "shared memory layout too large");
+    extern __shared__ uint8_t smem_raw[];
+    RowSmem<N> &s = *reinterpret_cast<RowSmem<N> *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
+    for (int i = tid; i < N * kKC; i += kThr) {
+        const int n = i / kKC, kc = i % kKC;
+        *reinterpret_cast<uint4 *>(s.b + (n >> 3) * kSBO + kc * kCore + (n & 7) * 16) = wts[i];
+    }
+    for (int i = tid; i < N; i += kThr) s.bias[i] = bias[i];
+    uint8_t *arow = s.a + (tid >> 3) * kSBO + (tid & 7) * 16;
+    *reinterpret_cast<uint4 *>(arow + 9 * kCore) = zero;
+    const int64_t nseg = (W + kM - 1) / kM, ntiles = F * H * nseg;
+    const int64_t G = gridDim.x;
+    if (tid == 0) {
+        mbar_init(&s.bar, 1);
+        mbar_init(s.rbar + 0, 1);
+        mbar_init(s.rbar + 1, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        const int64_t t0 = blockIdx.x;
+        if (t0 < ntiles) issue_rows(in, s.rows[0], s.rbar + 0, t0, H, W, nseg);
+        if (t0 + G < ntiles) issue_rows(in, s.rows[1], s.rbar + 1, t0 + G, H, W, nseg);
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(&s.tmem)),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = s.tmem;
+    const uint32_t a_addr = smem_u32(s.a), b_addr = smem_u32(s.b);
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    unsigned phase = 0;
+    int i = 0;
+    for (int64_t t = blockIdx.x; t < ntiles; t += G, ++i) {
+        const int buf = i & 1;
+        const RowTile r = row_tile(t, H, W, nseg);
+        const bool rows_ok = mbar_wait(s.rbar + buf, (unsigned)(i >> 1) & 1u);
+        if (__syncthreads_or(!rows_ok)) {
+            if (tid == 0) {
+                atomicOr(&g_cnn_status, 1u);
+                mbar_wait(s.rbar + buf, (unsigned)(i >> 1) & 1u);
+                if (t + G < ntiles) mbar_wait(s.rbar + (buf ^ 1), (unsigned)((i + 1) >> 1) & 1u);
+            }
+            break;
+        }
+        // im2col row of pixel x0 + tid from the staged rows
+        const uint4 *rw = reinterpret_cast<const uint4 *>(s.rows[buf]);
+#pragma unroll
+        for (int tap = 0; tap < 9; ++tap) {
+            const int dy = tap / 3, dx = tap % 3;
+            const int64_t yy = r.y + dy - 1, xx = r.x0 - 1 + tid + dx;
+            const bool ok = yy >= 0 && yy < H && xx >= 0 && xx < W;
+            *reinterpret_cast<uint4 *>(arow + tap * kCore) = ok ? rw[dy * kRowPx + tid + dx] : zero;
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        tc_fence_before();  // the previous tile's tcgen05.ld before the barrier
+        __syncthreads();
+        tc_fence_after();
+        if (tid == 0) {
+            // the rows of this buffer are consumed: refill it two tiles ahead
+            if (t + 2 * G < ntiles) issue_rows(in, s.rows[buf], s.rbar + buf, t + 2 * G, H, W, nseg);
+#pragma unroll
+            for (int kk = 0; kk < kKC / 2; ++kk)
+                tc_mma(tmem, smem_desc(a_addr + kk * 2 * kCore), smem_desc(b_addr + kk * 2 * kCore),
+                       instr_desc<N>(), kk > 0 ? 1u : 0u);
+            tc_commit(&s.bar);
+        }
+        const bool ok = mbar_wait(&s.bar, phase);
+        if (tid == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) {
+                atomicOr(&g_cnn_status, 1u);
+                mbar_wait(&s.bar, phase);
+                if (t + G < ntiles) mbar_wait(s.rbar + (buf ^ 1), (unsigned)((i + 1) >> 1) & 1u);
+                if (t + 2 * G < ntiles) mbar_wait(s.rbar + buf, (unsigned)((i + 2) >> 1) & 1u);
+            }
+            break;
+        }
+        phase ^= 1u;
+        tc_fence_after();
+        uint4 *srow = reinterpret_cast<uint4 *>(s.stage) + tid * (N / 8);
+#pragma unroll
+        for (int c0 = 0; c0 < N; c0 += 32) {
+            uint32_t rr[32];
+            tc_ld32(lane_base + (uint32_t)c0, rr);
+            uint4 *o = srow + c0 / 8;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                uint32_t w4[4];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const int j = q * 8 + e * 2;
+                    float v0 = __uint_as_float(rr[j]) + s.bias[c0 + j];
+                    float v1 = __uint_as_float(rr[j + 1]) + s.bias[c0 + j + 1];
+                    if (relu) {
+                        v0 = fmaxf(v0, 0.f);
+                        v1 = fmaxf(v1, 0.f);
+                    }
+                    const __nv_bfloat162 h = __floats2bfloat162_rn(v0, v1);
+                    w4[e] = *reinterpret_cast<const uint32_t *>(&h);
+                }
+                o[q] = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+            }
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            const int64_t p0 = (r.f * H + r.y) * W + r.x0;
+            bulk_s2g(out + p0 * (N / 8), s.stage, (unsigned)(r.nv * N * 2));
+        }
+    }
+    if (tid == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                     "r"(kTmemCols)
+                     : "memory");
+}
+
+template <int N>
+int launch_rows(const void *in, const void *wts, const float *bias, void *out, int64_t F,
+                int64_t H, int64_t W, int relu, cudaStream_t st) {
+    const int64_t ntiles = F * H * ((W + kM - 1) / kM);
+    const int64_t cap = int64_t(kSMs) * 3;
+    const int grid = int(ntiles < cap ? ntiles : cap);
+    SCI_CUDA(cudaFuncSetAttribute(k_conv_thin_rows<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  kSmemRows));
+    k_conv_thin_rows<N><<<grid, kThr, kSmemRows, st>>>(
+        reinterpret_cast<const uint4 *>(in), reinterpret_cast<const uint4 *>(wts), bias,
+        reinterpret_cast<uint4 *>(out), F, H, W, relu);
+    SCI_LAUNCHED("k_conv_thin_rows");
+    return SCI_OK;
+}
+
+template <int N>
 int launch_thin(const void *in, const void *wts, const float *bias, void *out, int64_t F,
                 int64_t H, int64_t W, int relu, cudaStream_t st) {
     const int64_t ntiles = (F * H * W + kM - 1) / kM;
-    const int64_t cap = int64_t(kSMs) * (NBUF == 1 ? 3 : 2);
+    const int64_t cap = int64_t(kSMs) * 3;
     const int grid = int(ntiles < cap ? ntiles : cap);
-    SCI_CUDA(cudaFuncSetAttribute(k_conv_thin_tc<N, NBUF>,
-                                  cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  smem_bytes<NBUF>()));
-    k_conv_thin_tc<N, NBUF><<<grid, kThr, smem_bytes<NBUF>(), st>>>(
+    SCI_CUDA(cudaFuncSetAttribute(k_conv_thin_tc<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  kSmemBytes));
+    k_conv_thin_tc<N><<<grid, kThr, kSmemBytes, st>>>(
         reinterpret_cast<const uint4 *>(in), reinterpret_cast<const uint4 *>(wts), bias,
         reinterpret_cast<uint4 *>(out), F, H, W, relu);
     SCI_LAUNCHED("k_conv_thin_tc");
     return SCI_OK;
 }
 
+// Row-segment tiles with bulk-copied input rows (k_conv_thin_rows): 1.84 ms
+// for 8 x 2048 x 2048 -> 96 channels against 1.99 ms for the per-pixel
+// gather (SCI_THIN_ROWS=0); the gather with a second A buffer and the next
+// tile's copies in flight (2 blocks per SM) measured 2.37 ms.
 template <int N>
 int launch_thin_n(const void *in, const void *wts, const float *bias, void *out, int64_t F,
                   int64_t H, int64_t W, int relu, cudaStream_t st) {
-    // one A buffer and 3 blocks per SM: 1.99 ms for 8 x 2048 x 2048 -> 96
-    // channels; two buffers (next gather overlapping) and 2 blocks per SM:
-    // 2.37 ms (SCI_THIN_NBUF=2)
-    static const int nbuf = [] {
-        const char *e = getenv("SCI_THIN_NBUF");
-        return (e && e[0] == '2') ? 2 : 1;
+    static const bool rows = [] {
+        const char *e = getenv("SCI_THIN_ROWS");
+        return !(e && e[0] == '0');
     }();
-    if (nbuf == 1) return launch_thin<N, 1>(in, wts, bias, out, F, H, W, relu, st);
-    return launch_thin<N, 2>(in, wts, bias, out, F, H, W, relu, st);
+    if (rows) return launch_rows<N>(in, wts, bias, out, F, H, W, relu, st);
+    return launch_thin<N>(in, wts, bias, out, F, H, W, relu, st);
 }
 
 }  // namespace
