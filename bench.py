@@ -20,6 +20,10 @@ Also reported on the same JSON line:
                 of the same loop, and the gradients' relative difference
   batched       64 uneven measurements (H = W in 128..1024, B in 8..32), 50
                 GAP-TV iterations each, one graph: ms per batch
+  parity        per configuration, the GPU result against the float64 oracle on
+                the same seeded inputs: relative L2 and the PSNR-to-ground-truth
+                difference (the 2048 x 2048 x 24 GAP and ADMM solves in full;
+                ``--parity-size`` for a smaller instance, ``--no-parity`` to skip)
 
 ``--impl reference`` times the reference's CPU implementation (the numpy
 port in oracle/, the reference being Python) on a bounded sample instead.
@@ -168,6 +172,132 @@ def cpu_sample(crop=1024, iters=2):
     return value, note, dt
 
 
+def _psnr_frames(x, orig):
+    """Mean over frames of the per-frame PSNR (data range 1) of planar
+    (B, H, W) stacks, in float64 -- the reference's per-frame compare_psnr
+    averaged as its drivers report it."""
+    mse = ((np.asarray(x, np.float64) - orig) ** 2).mean(axis=(1, 2))
+    return float(np.mean(10.0 * np.log10(1.0 / np.maximum(mse, 1e-30))))
+
+
+def _parity(x, ref, orig):
+    """Relative L2 of the GPU result to the float64 oracle's, and the PSNR
+    to ground truth of both (B, H, W stacks)."""
+    x = np.asarray(x, np.float64)
+    p, q = _psnr_frames(x, orig), _psnr_frames(ref, orig)
+    return {"rel_l2": float(np.linalg.norm(x - ref) / np.linalg.norm(ref)),
+            "psnr_db": p, "psnr_oracle_db": q, "delta_psnr_db": p - q}
+
+
+def parity_report(dev, n=H):
+    """Each configuration solved on the GPU through the public API and by
+    the float64 oracle (the OpenMP C restatement for the video paths, the
+    numpy port for the spectral one) on the same seeded inputs.
+
+    video_256x256x8     40 GAP-acc iterations, tv_weight 0.1, x0 = At(y/Phi_sum)
+    video_NxNx24        GAP-acc and ADMM (gamma 0.01), 60 iterations, weight
+                        annealed 0.2 -> 0.05, noise 0.01 max y; N = 2048 (the
+                        timed workload; about 40 s of float64 work per solve
+                        on 16 cores) or a smaller instance of the generator
+    cassi_256x256x28    80 GAP-acc iterations, tv_weight 0.05
+    batch               items of the 64-item uneven batch (two of 128^2, two
+                        of 256^2, one of 512^2), solved together in one
+                        BatchSolver launch, 50 iterations
+    """
+    import torch
+    import sci_algorithms_gb300 as sci
+    from sci_algorithms_gb300 import _dev
+    from oracle import c_oracle, reference_port as port, cassi as oc
+    out = {}
+
+    def planar(a):
+        a = a.detach().cpu().numpy() if isinstance(a, torch.Tensor) else a
+        return np.asarray(a, np.float64)
+
+    # 256 x 256 x 8 through the plug-in driver gap_denoise
+    orig, mask, meas = sci.datasets.config0()
+    msum = mask.sum(axis=2)
+    msum[msum == 0] = 1
+    v0 = mask * (meas / msum)[..., None]
+    A, At = sci.make_ops(mask)
+    x = sci.gap_denoise(meas, msum, A, At, _lambda=1, accelerate=True, iter_max=40,
+                        tv_weight=0.1, tv_iter_max=5, x0=v0)[0]
+    t0 = time.perf_counter()
+    ref, _ = c_oracle.gap_tv(meas, c_oracle.planar(mask), msum, c_oracle.planar(v0), 40, 1.0,
+                             0.1, tv_iter_max=5, accelerate=True)
+    out["video_256x256x8_gap"] = dict(_parity(c_oracle.planar(x), ref, c_oracle.planar(orig)),
+                                      oracle_s=time.perf_counter() - t0)
+
+    # the headline generator: GAP-acc and ADMM through Solver, as timed
+    orig, mask, meas = sci.datasets.video_config(n, n, B, noise_rel=0.01)
+    msum = mask.sum(axis=2)
+    msum[msum == 0] = 1
+    weights = np.array([0.2 * 0.25 ** (k / (ITERS - 1)) for k in range(ITERS)], np.float32)
+    op = sci.MaskOperator(mask)
+    y = _dev.plane(meas, dev)
+    phi, og = c_oracle.planar(mask), c_oracle.planar(orig)
+    x0 = c_oracle.planar(mask * meas[..., None])          # At(y), the solver's start
+    del orig
+    for kind, kw in (("gap", {"accelerate": True}), ("admm", {"gamma": 0.01})):
+        s = sci.Solver(op, kind, ITERS, 1.0, weights, TV_ITERS, **kw)
+        x = planar(s.run(y))
+        del s
+        t0 = time.perf_counter()
+        if kind == "gap":
+            ref, _ = c_oracle.gap_tv(meas, phi, msum, x0, ITERS, 1.0, weights.astype(np.float64),
+                                     tv_iter_max=TV_ITERS, accelerate=True)
+        else:
+            ref, _ = c_oracle.admm_tv(meas, phi, msum, x0, ITERS, 1.0, weights.astype(np.float64),
+                                      gamma=0.01, tv_iter_max=TV_ITERS)
+        out["video_%dx%dx%d_%s" % (n, n, B, kind)] = dict(_parity(x, ref, og),
+                                                          oracle_s=time.perf_counter() - t0)
+        del x, ref
+    del op, y, phi, og, x0
+    torch.cuda.empty_cache()
+
+    # spectral: 256 x 256 x 28, 2-pixel dispersion, 80 iterations
+    L, it = 28, 80
+    cube = sci.datasets.spectral_cube(256, 256, L, seed=0)
+    ap = sci.datasets.bernoulli_mask(256, 256, 1, seed=1)[..., 0]
+    yc = oc.cassi_A(cube, ap, 2)
+    cs = sci.CassiSolver(sci.CassiOperator(ap, L, 2), it, 1.0, 0.05, 5)
+    x = planar(cs.run(torch.from_numpy(yc).float().to(dev)))
+    t0 = time.perf_counter()
+    ref = port.gap_denoise(yc, oc.cassi_phisum(ap, L, 2), lambda v: oc.cassi_A(v, ap, 2),
+                           lambda r: oc.cassi_At(r, ap, L, 2), _lambda=1, accelerate=True,
+                           iter_max=it, tv_weight=0.05, tv_iter_max=5, show_iqa=False)[0]
+    out["cassi_256x256x28_gap"] = dict(_parity(x, c_oracle.planar(ref), c_oracle.planar(cube)),
+                                       oracle_s=time.perf_counter() - t0)
+
+    # batched: a subset of the uneven batch's own items, one launch
+    shapes = sci.datasets.batch_shapes(64, seed=0)
+    pick, want = [], {128: 2, 256: 2, 512: 1}
+    for i, (s, _, b, p) in enumerate(shapes):
+        if want.get(s, 0) > 0:
+            want[s] -= 1
+            pick.append(i)
+    items = [sci.datasets.video_config(shapes[i][0], shapes[i][1], shapes[i][2], p=shapes[i][3],
+                                       seeds=(1000 + i, 1001 + i, 1002 + i)) for i in pick]
+    bs = sci.BatchSolver([m for _, _, m in items], [k for _, k, _ in items], iters=50,
+                         tv_weight=0.1, autotune=True)
+    res = [planar(v) for v in bs.run()]
+    del bs
+    worst, t0 = None, time.perf_counter()
+    for i, (orig, mask, meas), x in zip(pick, items, res):
+        msum = mask.sum(axis=2)
+        msum[msum == 0] = 1
+        ref, _ = c_oracle.gap_tv(meas, c_oracle.planar(mask), msum,
+                                 c_oracle.planar(mask * (meas / msum)[..., None]), 50, 1.0, 0.1,
+                                 tv_iter_max=5, accelerate=True)
+        r = _parity(x, ref, c_oracle.planar(orig))
+        if worst is None or r["rel_l2"] > worst["rel_l2"]:
+            worst = dict(r, item=i, shape=list(shapes[i][:3]))
+    out["batch_items_gap"] = dict(worst, items=pick, reported="the item of largest rel_l2",
+                                  oracle_s=time.perf_counter() - t0)
+    out["oracle_threads"] = c_oracle.lib().orc_num_threads()
+    return out
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -290,11 +420,16 @@ def run_gpu(args):
     ms_e2e_serial = max_over_ranks((time.perf_counter() - t0) * 1e3 / e2e_steps, dev)
 
     extras = {} if args.no_extras else side_workloads(dev)
+    del gap, admm, op, y, xin, xout, ws, y1
+    torch.cuda.empty_cache()
 
     if rank == 0:
         cpu_v, cpu_note, _ = (None, None, None)
         if world == 1 and not args.no_cpu:
             cpu_v, cpu_note, _ = cpu_sample(crop=args.ref_crop, iters=2)
+        parity = None
+        if world == 1 and not args.no_parity:
+            parity = parity_report(dev, n=args.parity_size)
         per_iter_bytes = proj_bytes + tv_bytes
         line = {
             "metric": METRIC, "value": world * ITERS * 1e3 / ms_gap, "unit": "iter/s",
@@ -326,6 +461,8 @@ def run_gpu(args):
             "clocks": clk,
         }
         line.update(extras)
+        if parity is not None:
+            line["parity"] = parity
         if cpu_v is not None:
             line["cpu_baseline"] = {"value": cpu_v, "unit": "iter/s", "cores": 1,
                                     "kind": "port", "sample": cpu_note}
@@ -654,6 +791,10 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the spectral and differentiable side workloads")
+    ap.add_argument("--no-parity", action="store_true",
+                    help="skip the per-configuration comparison with the float64 oracle")
+    ap.add_argument("--parity-size", type=int, default=H,
+                    help="H = W of the 60-iteration video parity solves (2048: the timed workload)")
     ap.add_argument("--kernel", choices=["tv", "proj", "proj_admm", "unrolled", "cnn"],
                     default=None,
                     help="profiling mode: time one kernel on a 2048x2048xFRAMES stack")
