@@ -172,6 +172,36 @@ def cpu_sample(crop=1024, iters=2):
     return value, note, dt
 
 
+def host_info():
+    """Host cores this process may use and the CPU model, for the CPU
+    baseline's description."""
+    try:
+        cores = len(os.sched_getaffinity(0))
+    except AttributeError:
+        cores = os.cpu_count()
+    model = None
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    model = line.split(":", 1)[1].strip()
+                    break
+    except OSError:
+        pass
+    if model is None:
+        try:
+            out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+            for line in out.splitlines():
+                if line.strip().lower().startswith("model name"):
+                    model = line.split(":", 1)[1].strip()
+                    break
+        except (OSError, subprocess.SubprocessError):
+            pass
+    import platform
+    return {"host_cores": cores, "cpu_model": model or platform.machine(),
+            "arch": platform.machine()}
+
+
 def _psnr_frames(x, orig):
     """Mean over frames of the per-frame PSNR (data range 1) of planar
     (B, H, W) stacks, in float64 -- the reference's per-frame compare_psnr
@@ -314,8 +344,8 @@ def run_reference(args):
             "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": base_config(),
-            "cpu_baseline": {"value": value, "unit": "iter/s", "cores": 1, "kind": "port",
-                             "sample": note},
+            "cpu_baseline": dict({"value": value, "unit": "iter/s", "cores": 1, "kind": "port",
+                                  "sample": note}, **host_info()),
             "e2e": {"value": value, "unit": "iter/s", "h2d_bytes_per_step": 0,
                     "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
@@ -464,8 +494,8 @@ def run_gpu(args):
         if parity is not None:
             line["parity"] = parity
         if cpu_v is not None:
-            line["cpu_baseline"] = {"value": cpu_v, "unit": "iter/s", "cores": 1,
-                                    "kind": "port", "sample": cpu_note}
+            line["cpu_baseline"] = dict({"value": cpu_v, "unit": "iter/s", "cores": 1,
+                                         "kind": "port", "sample": cpu_note}, **host_info())
         print(json.dumps(line))
     if world > 1:
         torch.distributed.destroy_process_group()
