@@ -255,7 +255,8 @@ int sci_cassi_workspace_bytes(int64_t L, int64_t H, int64_t W, int step,
 /* GAP-TV with the CASSI operators (gap_denoise, pnp_sci_algo.py:536-706,
  * with A/At = the operators above; per-band Chambolle TV).  Uses
  * opts->iters, lambdas, weights, tv_iter_max, eps, accelerate, orig,
- * sqerr, tv_steps. */
+ * sqerr, tv_steps and use_graph (the loop captured once into a cached CUDA
+ * graph, as sci_gap_tv does). */
 int sci_cassi_gap_tv(const float *y, const float *phi, const float *phisum,
                      const float *x0, float *x_out, int64_t L, int64_t H,
                      int64_t W, int step, const sci_solve_opts *opts,

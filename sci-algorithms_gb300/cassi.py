@@ -64,7 +64,7 @@ class CassiSolver:
     """GAP-TV on one CASSI measurement (native loop)."""
 
     def __init__(self, op, iters=80, lambdas=1.0, tv_weight=0.1, tv_iter_max=5, eps=2e-4,
-                 accelerate=True):
+                 accelerate=True, use_graph=True):
         self.op = op
         self.iters = int(iters)
         self._lam = _dev.schedule(lambdas, self.iters)
@@ -76,6 +76,7 @@ class CassiSolver:
         o.tv_iter_max = int(tv_iter_max)
         o.eps = float(eps)
         o.accelerate = 1 if accelerate else 0
+        o.use_graph = 1 if use_graph else 0
         n = ctypes.c_size_t()
         call("sci_cassi_workspace_bytes", op.L, op.H, op.W, op.step, int(tv_iter_max),
              ctypes.byref(n))

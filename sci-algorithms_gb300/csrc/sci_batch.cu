@@ -22,6 +22,7 @@
 #include <vector>
 
 #include "sci_bulk.cuh"
+#include "sci_graph.cuh"
 #include "sci_tv.cuh"
 
 namespace sci {
@@ -325,15 +326,6 @@ void build_table(const sci_batch_item *items, int n, int K, float eps, char *ws,
     }
 }
 
-struct GraphCache {
-    std::mutex mu;
-    std::list<std::pair<std::string, cudaGraphExec_t>> e;
-};
-GraphCache &cache() {
-    static GraphCache c;
-    return c;
-}
-
 int enqueue(const Table &T, Table *dT, const Layout &L, char *ws, int n, int iters, int K,
             int accelerate, int init_x0, cudaStream_t s) {
     const int pb = T.proj_prefix[n], tb = (T.tv_prefix[n] + tv::WPB - 1) / tv::WPB;
@@ -474,50 +466,12 @@ int sci_batch_gap_tv(const sci_batch_item *items, int n, int iters, int tv_iter_
         return rc;
     }
     std::string key(reinterpret_cast<const char *>(hT), sizeof(Table));
-    key.append(reinterpret_cast<const char *>(&iters), sizeof(int));
-    key.append(reinterpret_cast<const char *>(&accelerate), sizeof(int));
-    key.append(reinterpret_cast<const char *>(&init_x0), sizeof(int));
-    GraphCache &gc = cache();
-    {
-        std::lock_guard<std::mutex> lk(gc.mu);
-        for (auto &kv : gc.e)
-            if (kv.first == key) {
-                delete hT;
-                SCI_CUDA(cudaGraphLaunch(kv.second, s));
-                return SCI_OK;
-            }
-    }
-    cudaStream_t cs;
-    ce = cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking);
-    if (ce != cudaSuccess) {
-        delete hT;
-        return cuda_status(ce, "cudaStreamCreate");
-    }
-    ce = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-    if (ce == cudaSuccess) rc = enqueue(*hT, dT, L, ws, n, iters, tv_iter_max, accelerate, init_x0, cs);
-    cudaGraph_t graph = nullptr;
-    const cudaError_t ce2 = (ce == cudaSuccess) ? cudaStreamEndCapture(cs, &graph) : ce;
-    cudaStreamDestroy(cs);
+    key_append(key, iters, accelerate, init_x0);
+    rc = run_graph("batch graph capture", key, s, [&](cudaStream_t cs) {
+        return enqueue(*hT, dT, L, ws, n, iters, tv_iter_max, accelerate, init_x0, cs);
+    });
     delete hT;
-    if (rc) {
-        if (graph) cudaGraphDestroy(graph);
-        return rc;
-    }
-    if (ce2 != cudaSuccess) return cuda_status(ce2, "batch graph capture");
-    cudaGraphExec_t exec = nullptr;
-    ce = cudaGraphInstantiate(&exec, graph, 0);
-    cudaGraphDestroy(graph);
-    if (ce != cudaSuccess) return cuda_status(ce, "cudaGraphInstantiate");
-    {
-        std::lock_guard<std::mutex> lk(gc.mu);
-        gc.e.emplace_front(key, exec);
-        while (gc.e.size() > 8) {
-            cudaGraphExecDestroy(gc.e.back().second);
-            gc.e.pop_back();
-        }
-    }
-    SCI_CUDA(cudaGraphLaunch(exec, s));
-    return SCI_OK;
+    return rc;
 }
 
 }  // extern "C"

@@ -12,7 +12,12 @@
 // projection is the video one (pnp_sci_algo.py:640-645) with these
 // operators: one detector-grid kernel (A, y1 update, residual) and one
 // cube-grid kernel (x += lambda At(r)).
+#include <algorithm>
+#include <cstdlib>
+#include <string>
+
 #include "sci_common.cuh"
+#include "sci_graph.cuh"
 
 namespace sci {
 
@@ -127,6 +132,56 @@ __global__ void k_cassi_update(const float *__restrict__ x, const float *__restr
     }
 }
 
+// The projection of one iteration with a detector row per block: the
+// row's residual r (detector grid, k_cassi_resid's arithmetic) into shared
+// memory, then x_out_b = x_b + lambda (r[h, w + step b] phi[h, w]) for every
+// band of that row (k_cassi_update's arithmetic) -- one launch, and r never
+// leaves the chip.  Needs Wd floats of shared memory.
+template <bool ACC>
+__global__ void __launch_bounds__(256) k_cassi_proj_rows(
+    const float *__restrict__ x, const float *__restrict__ phi, const float *__restrict__ y,
+    float *__restrict__ y1, const float *__restrict__ ps, float *__restrict__ xo, float lam,
+    int L, int H, int W, int step) {
+    extern __shared__ float rs[];
+    const int Wd = W + step * (L - 1);
+    const int64_t hw = (int64_t)H * W;
+    for (int h = blockIdx.x; h < H; h += gridDim.x) {
+        for (int wd = threadIdx.x; wd < Wd; wd += blockDim.x) {
+            const int64_t i = (int64_t)h * Wd + wd;
+            int b0, b1;
+            band_range(wd, W, L, step, b0, b1);
+            float s = 0.f;
+            for (int b = b0; b <= b1; ++b) {
+                const int64_t p = (int64_t)h * W + (wd - step * b);
+                s = fmaf(__ldg(x + b * hw + p), __ldg(phi + p), s);
+            }
+            if (ACC) {
+                const float t = y1[i] + (y[i] - s);
+                y1[i] = t;
+                rs[wd] = __fdiv_rn(t - s, ps[i]);
+            } else {
+                rs[wd] = __fdiv_rn(y[i] - s, ps[i]);
+            }
+        }
+        __syncthreads();
+        for (int e = threadIdx.x; e < L * W; e += blockDim.x) {
+            const int b = e / W, w = e - b * W;
+            const int64_t p = (int64_t)h * W + w;
+            xo[b * hw + p] = fmaf(lam, rs[w + step * b] * __ldg(phi + p), __ldg(x + b * hw + p));
+        }
+        __syncthreads();
+    }
+}
+
+constexpr size_t kRowSmemMax = 48 * 1024;  // default dynamic shared memory limit
+
+// The row-fused projection is the default; SCI_CASSI_ROWS=0 selects the
+// detector-grid and cube-grid kernel pair (bitwise the same result).
+bool rows_enabled() {
+    const char *e = getenv("SCI_CASSI_ROWS");
+    return !(e && atoi(e) == 0);
+}
+
 int check(int64_t L, int64_t H, int64_t W, int step) {
     SCI_CHECK_ARG(L >= 1 && H >= 1 && W >= 1 && step >= 1, "cassi: invalid sizes or step");
     SCI_CHECK_ARG(L <= 4096 && H * (W + step * (L - 1)) < (int64_t(1) << 40) && W < (1 << 30),
@@ -221,33 +276,58 @@ int sci_cassi_gap_tv(const float *y, const float *phi, const float *phisum, cons
     size_t tvb;
     cassi_ws(L, H, W, step, o->tv_iter_max, static_cast<char *>(workspace), &y1, &r, &xp, &tv,
              &tvb);
-    cudaStream_t s = as_stream(stream);
     const int64_t n = L * H * W, nd = H * (W + step * (L - 1));
-    if (x0 != x_out) SCI_CUDA(cudaMemcpyAsync(x_out, x0, 4 * n, cudaMemcpyDeviceToDevice, s));
-    if (o->accelerate) SCI_CUDA(cudaMemsetAsync(y1, 0, 4 * nd, s));
-    if (o->sqerr) SCI_CUDA(cudaMemsetAsync(o->sqerr, 0, sizeof(double) * o->iters, s));
-    for (int it = 0; it < o->iters; ++it) {
-        SCI_CHECK_ARG(o->weights[it] > 0.f, "sci_cassi_gap_tv: tv_weight must be > 0");
-        if (o->accelerate)
-            k_cassi_resid<true><<<grid1(nd, 256), 256, 0, s>>>(x_out, phi, y, y1, phisum, r,
-                                                               (int)L, (int)H, (int)W, step);
-        else
-            k_cassi_resid<false><<<grid1(nd, 256), 256, 0, s>>>(x_out, phi, y, y1, phisum, r,
-                                                                (int)L, (int)H, (int)W, step);
-        SCI_LAUNCHED("k_cassi_resid");
-        k_cassi_update<<<grid1(n, 256), 256, 0, s>>>(x_out, phi, r, xp, o->lambdas[it], (int)L,
-                                                     (int)H, (int)W, step);
-        SCI_LAUNCHED("k_cassi_update");
-        int e = tv_launch(xp, x_out, nullptr, L, H, W, H * W, o->weights[it], o->eps,
-                          o->tv_iter_max, o->tv_steps ? o->tv_steps + (int64_t)it * L : nullptr,
-                          nullptr, tv, tvb, s, 0);
-        if (e) return e;
-        if (o->orig && o->sqerr) {
-            e = sci_sqerr_accum(o->orig, x_out, n, o->sqerr + it, s);
+    const size_t row_smem = sizeof(float) * (size_t)(W + step * (L - 1));
+    const bool rows = row_smem <= kRowSmemMax && rows_enabled();
+    auto enqueue = [&](cudaStream_t s) -> int {
+        if (x0 != x_out) SCI_CUDA(cudaMemcpyAsync(x_out, x0, 4 * n, cudaMemcpyDeviceToDevice, s));
+        if (o->accelerate) SCI_CUDA(cudaMemsetAsync(y1, 0, 4 * nd, s));
+        if (o->sqerr) SCI_CUDA(cudaMemsetAsync(o->sqerr, 0, sizeof(double) * o->iters, s));
+        for (int it = 0; it < o->iters; ++it) {
+            SCI_CHECK_ARG(o->weights[it] > 0.f, "sci_cassi_gap_tv: tv_weight must be > 0");
+            if (rows) {
+                const unsigned g = (unsigned)std::min<int64_t>(H, (int64_t)kSMs * 8);
+                if (o->accelerate)
+                    k_cassi_proj_rows<true><<<g, 256, row_smem, s>>>(
+                        x_out, phi, y, y1, phisum, xp, o->lambdas[it], (int)L, (int)H, (int)W,
+                        step);
+                else
+                    k_cassi_proj_rows<false><<<g, 256, row_smem, s>>>(
+                        x_out, phi, y, y1, phisum, xp, o->lambdas[it], (int)L, (int)H, (int)W,
+                        step);
+                SCI_LAUNCHED("k_cassi_proj_rows");
+            } else {
+                if (o->accelerate)
+                    k_cassi_resid<true><<<grid1(nd, 256), 256, 0, s>>>(
+                        x_out, phi, y, y1, phisum, r, (int)L, (int)H, (int)W, step);
+                else
+                    k_cassi_resid<false><<<grid1(nd, 256), 256, 0, s>>>(
+                        x_out, phi, y, y1, phisum, r, (int)L, (int)H, (int)W, step);
+                SCI_LAUNCHED("k_cassi_resid");
+                k_cassi_update<<<grid1(n, 256), 256, 0, s>>>(x_out, phi, r, xp, o->lambdas[it],
+                                                             (int)L, (int)H, (int)W, step);
+                SCI_LAUNCHED("k_cassi_update");
+            }
+            int e = tv_launch(xp, x_out, nullptr, L, H, W, H * W, o->weights[it], o->eps,
+                              o->tv_iter_max,
+                              o->tv_steps ? o->tv_steps + (int64_t)it * L : nullptr, nullptr, tv,
+                              tvb, s, 0);
             if (e) return e;
+            if (o->orig && o->sqerr) {
+                e = sci_sqerr_accum(o->orig, x_out, n, o->sqerr + it, s);
+                if (e) return e;
+            }
         }
-    }
-    return SCI_OK;
+        return SCI_OK;
+    };
+    cudaStream_t s = as_stream(stream);
+    if (!o->use_graph || o->iters == 0) return enqueue(s);
+    std::string key;
+    key_append(key, y, phi, phisum, x0, x_out, L, H, W, step, workspace, o->iters,
+               o->tv_iter_max, o->eps, o->accelerate, o->orig, o->sqerr, o->tv_steps);
+    key.append(reinterpret_cast<const char *>(o->lambdas), sizeof(float) * o->iters);
+    key.append(reinterpret_cast<const char *>(o->weights), sizeof(float) * o->iters);
+    return run_graph("cassi graph capture", key, s, enqueue);
 }
 
 }  // extern "C"

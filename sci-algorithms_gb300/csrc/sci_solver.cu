@@ -11,6 +11,7 @@
 #include <utility>
 
 #include "sci_common.cuh"
+#include "sci_graph.cuh"
 
 namespace sci {
 
@@ -78,33 +79,6 @@ size_t solver_layout(bool admm, int64_t B, int64_t H, int64_t W, int K, int tvm,
         w->tv_bytes = tvb;
     }
     return off;
-}
-
-// ------------------------------------------------------------ graph cache
-struct GraphCache {
-    std::mutex mu;
-    std::list<std::pair<std::string, cudaGraphExec_t>> entries;  // most recent first
-    static constexpr size_t kMax = 16;
-
-    cudaGraphExec_t find(const std::string &key) {
-        for (auto it = entries.begin(); it != entries.end(); ++it)
-            if (it->first == key) {
-                entries.splice(entries.begin(), entries, it);
-                return entries.front().second;
-            }
-        return nullptr;
-    }
-    void put(const std::string &key, cudaGraphExec_t g) {
-        entries.emplace_front(key, g);
-        while (entries.size() > kMax) {
-            cudaGraphExecDestroy(entries.back().second);
-            entries.pop_back();
-        }
-    }
-};
-GraphCache &graph_cache() {
-    static GraphCache c;
-    return c;
 }
 
 template <typename T>
@@ -296,42 +270,8 @@ int solve(const Args &a, void *stream) {
     }
     if (!o.use_graph) return enqueue(a, s);
 
-    GraphCache &gc = graph_cache();
-    const std::string key = a.key();
-    {
-        std::lock_guard<std::mutex> lk(gc.mu);
-        if (cudaGraphExec_t g = gc.find(key)) {
-            SCI_CUDA(cudaGraphLaunch(g, s));
-            return SCI_OK;
-        }
-    }
-    // capture on a private stream, then replay on the caller's stream
-    cudaStream_t cs;
-    SCI_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
-    cudaError_t ce = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-    if (ce != cudaSuccess) {
-        cudaStreamDestroy(cs);
-        return cuda_status(ce, "cudaStreamBeginCapture");
-    }
-    const int e = enqueue(a, cs);
-    cudaGraph_t graph = nullptr;
-    ce = cudaStreamEndCapture(cs, &graph);
-    cudaStreamDestroy(cs);
-    if (e) {
-        if (graph) cudaGraphDestroy(graph);
-        return e;
-    }
-    if (ce != cudaSuccess) return cuda_status(ce, "cudaStreamEndCapture");
-    cudaGraphExec_t exec = nullptr;
-    ce = cudaGraphInstantiate(&exec, graph, 0);
-    cudaGraphDestroy(graph);
-    if (ce != cudaSuccess) return cuda_status(ce, "cudaGraphInstantiate");
-    {
-        std::lock_guard<std::mutex> lk(gc.mu);
-        gc.put(key, exec);
-    }
-    SCI_CUDA(cudaGraphLaunch(exec, s));
-    return SCI_OK;
+    return run_graph("solver graph capture", a.key(), s,
+                     [&](cudaStream_t cs) { return enqueue(a, cs); });
 }
 
 }  // namespace

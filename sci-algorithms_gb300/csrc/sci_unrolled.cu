@@ -25,6 +25,7 @@
 #include <string>
 
 #include "sci_common.cuh"
+#include "sci_graph.cuh"
 
 namespace sci {
 
@@ -554,57 +555,9 @@ int forward(const float *logits, const float *lambdas, const float *xt, int64_t 
     return SCI_OK;
 }
 
-// Cached CUDA graphs of whole forward / reverse passes (keyed by every
-// argument): the reverse pass is ~20 launches per outer iteration.
-struct GraphCache {
-    std::mutex mu;
-    std::list<std::pair<std::string, cudaGraphExec_t>> e;
-};
-GraphCache &cache() {
-    static GraphCache c;
-    return c;
-}
-
-template <typename F>
-int run_graph(const std::string &key, cudaStream_t s, F enqueue) {
-    GraphCache &gc = cache();
-    {
-        std::lock_guard<std::mutex> lk(gc.mu);
-        for (auto &kv : gc.e)
-            if (kv.first == key) {
-                SCI_CUDA(cudaGraphLaunch(kv.second, s));
-                return SCI_OK;
-            }
-    }
-    cudaStream_t cs;
-    SCI_CUDA(cudaStreamCreateWithFlags(&cs, cudaStreamNonBlocking));
-    cudaError_t ce = cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal);
-    int rc = SCI_OK;
-    if (ce == cudaSuccess) rc = enqueue(cs);
-    cudaGraph_t graph = nullptr;
-    const cudaError_t ce2 = (ce == cudaSuccess) ? cudaStreamEndCapture(cs, &graph) : ce;
-    cudaStreamDestroy(cs);
-    if (rc) {
-        if (graph) cudaGraphDestroy(graph);
-        return rc;
-    }
-    if (ce2 != cudaSuccess) return cuda_status(ce2, "unrolled graph capture");
-    cudaGraphExec_t exec = nullptr;
-    ce = cudaGraphInstantiate(&exec, graph, 0);
-    cudaGraphDestroy(graph);
-    if (ce != cudaSuccess) return cuda_status(ce, "cudaGraphInstantiate");
-    {
-        std::lock_guard<std::mutex> lk(gc.mu);
-        gc.e.emplace_front(key, exec);
-        while (gc.e.size() > 8) {
-            cudaGraphExecDestroy(gc.e.back().second);
-            gc.e.pop_back();
-        }
-    }
-    SCI_CUDA(cudaGraphLaunch(exec, s));
-    return SCI_OK;
-}
-
+// Whole forward / reverse passes run as cached CUDA graphs (sci_graph.cuh),
+// keyed by every argument: the reverse pass is ~20 launches per outer
+// iteration.
 template <typename... T>
 std::string make_key(const T &...v) {
     std::string k;
@@ -653,7 +606,7 @@ int sci_unrolled_fwd(const float *logits, const float *lambdas, const float *x_t
     };
     const std::string key = make_key(1, logits, lambdas, x_true, N, B, H, W, K, tv_iters,
                                      tv_weight, loss, x_out, workspace, (int)w.stored);
-    return run_graph(key, as_stream(stream), body);
+    return run_graph("unrolled graph capture", key, as_stream(stream), body);
 }
 
 int sci_unrolled_bwd(const float *logits, const float *lambdas, const float *x_true, int64_t N,
@@ -672,7 +625,7 @@ int sci_unrolled_bwd(const float *logits, const float *lambdas, const float *x_t
     const std::string key = make_key(2, logits, lambdas, x_true, N, B, H, W, K, tv_iters,
                                      tv_weight, grad_loss, grad_logits, grad_lambdas, workspace,
                                      (int)w.stored);
-    return run_graph(key, as_stream(stream), [&](cudaStream_t s) -> int {
+    return run_graph("unrolled graph capture", key, as_stream(stream), [&](cudaStream_t s) -> int {
     // The checkpoints of the preceding sci_unrolled_fwd call on this
     // workspace (same arguments) are used as they are.
     const int64_t hw = H * W, nbhw = N * B * hw, nhw = N * hw, nf = N * B;

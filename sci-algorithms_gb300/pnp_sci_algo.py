@@ -85,7 +85,8 @@ def _solve(projmeth, y, Phi_sum, A, At, iters, _lambda, tv_weight, tv_iter_max, 
     if isinstance(op, CassiOperator) and tvm != "tv_chambolle":
         raise ValueError("the spectral (CASSI) solver runs the scikit-image TV only")
     if isinstance(op, CassiOperator) and projmeth == "gap":
-        solver = CassiSolver(op, iters, _lambda, tv_weight, tv_iter_max, eps, accelerate)
+        solver = CassiSolver(op, iters, _lambda, tv_weight, tv_iter_max, eps, accelerate,
+                             use_graph=use_graph)
         x0_d = None if x0 is None else _dev.planar(x0)
         orig_d = _dev.planar(X_orig) if want_iqa else None
         x = solver.run(y_d, x0=x0_d, phisum=ps_d, orig=orig_d)

@@ -86,3 +86,22 @@ def test_cassi_admm_plugin_path():
     x = sci.admm_denoise(y, ps, Ag, Atg, gamma=0.01, iter_max=10, tv_weight=0.05,
                          tv_iter_max=5)[0]
     assert rel(x, ref) < 1e-4
+
+
+@pytest.mark.parametrize("accelerate", [True, False])
+def test_cassi_row_projection_and_graph_are_bitwise_equal(monkeypatch, accelerate):
+    """The row-fused projection (residual row in shared memory) against the
+    detector-grid + cube-grid kernel pair, and the captured graph (first
+    run and replay) against direct launches: identical solves."""
+    cube, phi, y = cassi_problem()
+    op = sci.CassiOperator(phi, 28, 2)
+    yd = torch.from_numpy(y).float().to(op.dev)
+    out = []
+    for rows, graph in (("1", True), ("1", False), ("0", False), ("0", True)):
+        monkeypatch.setenv("SCI_CASSI_ROWS", rows)
+        s = sci.CassiSolver(op, 12, 1.0, 0.05, 5, accelerate=accelerate, use_graph=graph)
+        out.append(s.run(yd).clone())
+        if graph:
+            out.append(s.run(yd).clone())  # replay of the cached graph
+    for o in out[1:]:
+        assert torch.equal(o, out[0])
