@@ -547,6 +547,8 @@ def run_kernel(args):
         return run_unrolled(args)
     if args.kernel == "cnn":
         return run_cnn(args)
+    if args.kernel == "cassi":
+        return run_cassi(args)
     dev = _dev.device()
     F = args.frames
     orig, mask, meas = sci.datasets.video_config(H, W, F, noise_rel=0.01)
@@ -585,6 +587,32 @@ def run_kernel(args):
     torch.cuda.synchronize()
     print(json.dumps({"kernel": args.kernel, "frames": F, "H": H, "W": W,
                       "ms_per_launch": e0.elapsed_time(e1) / args.launches}))
+
+
+def run_cassi(args):
+    """Profiling mode for the spectral solve: ``--launches`` GAP-TV solves of
+    the 256 x 256 x 28 cube (2-pixel dispersion, 80 iterations), the loop
+    replayed from its CUDA graph after one warm-up solve."""
+    import torch
+    import sci_algorithms_gb300 as sci
+    L, it = 28, 80
+    cube = sci.datasets.spectral_cube(256, 256, L, seed=0)
+    phi = sci.datasets.bernoulli_mask(256, 256, 1, seed=1)[..., 0]
+    op = sci.CassiOperator(phi, L, 2)
+    yd = op.forward(torch.from_numpy(cube).float().to(op.dev))
+    cs = sci.CassiSolver(op, it, 1.0, 0.05, 5)
+    cs.run(yd)
+    torch.cuda.synchronize()
+    s = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(args.launches):
+        cs.run(yd)
+    e1.record(s)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.launches
+    print(json.dumps({"kernel": "cassi", "workload": "cassi_256x256x28_step2", "iters": it,
+                      "ms_per_solve": ms, "iter_per_s": it * 1e3 / ms}))
 
 
 def run_cnn(args):
@@ -825,7 +853,7 @@ def main():
                     help="skip the per-configuration comparison with the float64 oracle")
     ap.add_argument("--parity-size", type=int, default=H,
                     help="H = W of the 60-iteration video parity solves (2048: the timed workload)")
-    ap.add_argument("--kernel", choices=["tv", "proj", "proj_admm", "unrolled", "cnn"],
+    ap.add_argument("--kernel", choices=["tv", "proj", "proj_admm", "unrolled", "cnn", "cassi"],
                     default=None,
                     help="profiling mode: time one kernel on a 2048x2048xFRAMES stack")
     ap.add_argument("--frames", type=int, default=8)

@@ -1,9 +1,14 @@
 // The process-wide cache of instantiated CUDA graphs (sci_graph.cuh).
+#include <algorithm>
+#include <cstring>
 #include <list>
 #include <mutex>
 #include <utility>
+#include <vector>
 
 #include "sci_graph.cuh"
+
+extern char **environ;
 
 namespace sci {
 namespace {
@@ -21,6 +26,19 @@ GraphCache &cache() {
 }
 
 }  // namespace
+
+std::string env_switches() {
+    std::vector<std::string> v;
+    for (char **e = environ; e && *e; ++e)
+        if (std::strncmp(*e, "SCI_", 4) == 0) v.emplace_back(*e);
+    std::sort(v.begin(), v.end());
+    std::string k;
+    for (const std::string &s : v) {
+        k += s;
+        k += '\n';
+    }
+    return k;
+}
 
 int graph_replay(const std::string &key, cudaStream_t s, bool *found) {
     GraphCache &c = cache();

@@ -1,7 +1,7 @@
 // Cached CUDA graphs of whole enqueued sequences: a GAP / ADMM solve, a
 // batched solve, an unrolled forward or reverse pass, a spectral solve.
 // Each is keyed by every argument that shapes the launches (pointers,
-// sizes, schedules); the first call captures the sequence on a private
+// sizes, schedules) and by the SCI_* environment switches; the first call captures the sequence on a private
 // stream and instantiates it, later calls replay it with one launch.  One
 // process-wide cache (most recently used first, bounded) behind a mutex.
 #pragma once
@@ -10,6 +10,10 @@
 #include "sci_common.cuh"
 
 namespace sci {
+
+// The SCI_* environment switches (sorted "name=value" pairs): they select
+// kernels and launch shapes at capture time, so they are part of every key.
+std::string env_switches();
 
 // Launches the graph cached under key on s (under the cache's lock, so that
 // no other thread evicts it meanwhile); *found says whether there was one.
@@ -29,7 +33,7 @@ void key_append(std::string &k, const T &...v) {
 // error messages and keeps the keys of different callers apart.
 template <typename F>
 int run_graph(const char *what, const std::string &key, cudaStream_t s, F enqueue) {
-    const std::string k = std::string(what) + '\0' + key;
+    const std::string k = std::string(what) + '\0' + env_switches() + '\0' + key;
     bool found = false;
     const int r = graph_replay(k, s, &found);
     if (found || r) return r;

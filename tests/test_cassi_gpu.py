@@ -90,14 +90,15 @@ def test_cassi_admm_plugin_path():
 
 @pytest.mark.parametrize("accelerate", [True, False])
 def test_cassi_row_projection_and_graph_are_bitwise_equal(monkeypatch, accelerate):
-    """The row-fused projection (residual row in shared memory) against the
-    detector-grid + cube-grid kernel pair, and the captured graph (first
-    run and replay) against direct launches: identical solves."""
+    """The row-fused projection (residual row in shared memory; staged with
+    the row's cube values, the default, or not) against the detector-grid +
+    cube-grid kernel pair, and the captured graph (first run and replay)
+    against direct launches: identical solves."""
     cube, phi, y = cassi_problem()
     op = sci.CassiOperator(phi, 28, 2)
     yd = torch.from_numpy(y).float().to(op.dev)
     out = []
-    for rows, graph in (("1", True), ("1", False), ("0", False), ("0", True)):
+    for rows, graph in (("2", True), ("2", False), ("1", False), ("0", False), ("0", True)):
         monkeypatch.setenv("SCI_CASSI_ROWS", rows)
         s = sci.CassiSolver(op, 12, 1.0, 0.05, 5, accelerate=accelerate, use_graph=graph)
         out.append(s.run(yd).clone())
