@@ -226,13 +226,13 @@ __global__ void __launch_bounds__(256) k_cassi_proj_rows_staged(
 
 constexpr size_t kRowSmemMax = 48 * 1024;  // default dynamic shared memory limit
 
-// Projection form (SCI_CASSI_ROWS; all bitwise the same result): 2, the
-// default, the row-fused kernel staged in shared memory when the row's cube
-// values fit; 1 the row-fused kernel without staging; 0 the detector-grid
-// and cube-grid kernel pair.
+// Projection form (SCI_CASSI_ROWS; all bitwise the same result): 1, the
+// default, the row-fused kernel; 2 the row-fused kernel staged in shared
+// memory when the row's cube values fit; 0 the detector-grid and cube-grid
+// kernel pair.
 int rows_mode() {
     const char *e = getenv("SCI_CASSI_ROWS");
-    const int v = e ? atoi(e) : 2;
+    const int v = e ? atoi(e) : 1;
     return v < 0 ? 0 : (v > 2 ? 2 : v);
 }
 

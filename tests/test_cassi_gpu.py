@@ -90,8 +90,8 @@ def test_cassi_admm_plugin_path():
 
 @pytest.mark.parametrize("accelerate", [True, False])
 def test_cassi_row_projection_and_graph_are_bitwise_equal(monkeypatch, accelerate):
-    """The row-fused projection (residual row in shared memory; staged with
-    the row's cube values, the default, or not) against the detector-grid +
+    """The row-fused projection (residual row in shared memory; the default,
+    or staged with the row's cube values) against the detector-grid +
     cube-grid kernel pair, and the captured graph (first run and replay)
     against direct launches: identical solves."""
     cube, phi, y = cassi_problem()
