@@ -138,7 +138,7 @@ __global__ void k_cassi_update(const float *__restrict__ x, const float *__restr
 // band of that row (k_cassi_update's arithmetic) -- one launch, and r never
 // leaves the chip.  Needs Wd floats of shared memory.
 template <bool ACC>
-__global__ void __launch_bounds__(256) k_cassi_proj_rows(
+__global__ void __launch_bounds__(1024) k_cassi_proj_rows(
     const float *__restrict__ x, const float *__restrict__ phi, const float *__restrict__ y,
     float *__restrict__ y1, const float *__restrict__ ps, float *__restrict__ xo, float lam,
     int L, int H, int W, int step) {
@@ -173,67 +173,27 @@ __global__ void __launch_bounds__(256) k_cassi_proj_rows(
     }
 }
 
-// The same projection with the row's L x W cube values and its aperture
-// row staged in shared memory first (coalesced loads, all in flight at
-// once), so that the per-column band sums read shared memory instead of
-// waiting on one global load per band.  Bitwise the same arithmetic.
-// Needs (L W + W + Wd) floats of shared memory.
-template <bool ACC>
-__global__ void __launch_bounds__(256) k_cassi_proj_rows_staged(
-    const float *__restrict__ x, const float *__restrict__ phi, const float *__restrict__ y,
-    float *__restrict__ y1, const float *__restrict__ ps, float *__restrict__ xo, float lam,
-    int L, int H, int W, int step) {
-    extern __shared__ float sm[];
-    float *xs = sm;           // [L][W] the row of every band
-    float *ph = xs + L * W;   // [W]    the aperture row
-    float *rs = ph + W;       // [Wd]   the residual row
-    const int Wd = W + step * (L - 1);
-    const int64_t hw = (int64_t)H * W;
-    for (int h = blockIdx.x; h < H; h += gridDim.x) {
-        const int64_t ro = (int64_t)h * W;
-#pragma unroll 4
-        for (int e = threadIdx.x; e < L * W; e += blockDim.x) {
-            const int b = e / W, w = e - b * W;
-            xs[e] = __ldg(x + b * hw + ro + w);
-        }
-        for (int w = threadIdx.x; w < W; w += blockDim.x) ph[w] = __ldg(phi + ro + w);
-        __syncthreads();
-        for (int wd = threadIdx.x; wd < Wd; wd += blockDim.x) {
-            const int64_t i = (int64_t)h * Wd + wd;
-            int b0, b1;
-            band_range(wd, W, L, step, b0, b1);
-            float s = 0.f;
-            for (int b = b0; b <= b1; ++b) {
-                const int c = wd - step * b;
-                s = fmaf(xs[b * W + c], ph[c], s);
-            }
-            if (ACC) {
-                const float t = y1[i] + (y[i] - s);
-                y1[i] = t;
-                rs[wd] = __fdiv_rn(t - s, ps[i]);
-            } else {
-                rs[wd] = __fdiv_rn(y[i] - s, ps[i]);
-            }
-        }
-        __syncthreads();
-        for (int e = threadIdx.x; e < L * W; e += blockDim.x) {
-            const int b = e / W, w = e - b * W;
-            xo[b * hw + ro + w] = fmaf(lam, rs[w + step * b] * ph[w], xs[e]);
-        }
-        __syncthreads();
-    }
-}
-
 constexpr size_t kRowSmemMax = 48 * 1024;  // default dynamic shared memory limit
 
-// Projection form (SCI_CASSI_ROWS; all bitwise the same result): 1, the
-// default, the row-fused kernel; 2 the row-fused kernel staged in shared
-// memory when the row's cube values fit; 0 the detector-grid and cube-grid
-// kernel pair.
-int rows_mode() {
+// Projection form (SCI_CASSI_ROWS; bitwise the same result): 1, the
+// default, the row-fused kernel; 0 the detector-grid and cube-grid kernel
+// pair.
+bool rows_enabled() {
     const char *e = getenv("SCI_CASSI_ROWS");
-    const int v = e ? atoi(e) : 1;
-    return v < 0 ? 0 : (v > 2 ? 2 : v);
+    return !(e && atoi(e) == 0);
+}
+
+// Threads per row of the row-fused kernel (SCI_CASSI_ROWT overrides).
+// Measured on 256 x 256 x 28 (80 iterations, graph): 128 threads 3.71 ms
+// per solve, 256 3.19, 512 3.03, 1024 3.03 -- the kernel is latency-bound
+// (about 14 us of arithmetic-light work per launch), and wider rows
+// shorten each thread's chain.
+int row_threads() {
+    if (const char *e = getenv("SCI_CASSI_ROWT")) {
+        const int v = atoi(e);
+        if (v == 128 || v == 256 || v == 512 || v == 1024) return v;
+    }
+    return 512;
 }
 
 int check(int64_t L, int64_t H, int64_t W, int step) {
@@ -332,35 +292,22 @@ int sci_cassi_gap_tv(const float *y, const float *phi, const float *phisum, cons
              &tvb);
     const int64_t n = L * H * W, nd = H * (W + step * (L - 1));
     const size_t row_smem = sizeof(float) * (size_t)(W + step * (L - 1));
-    const int mode = rows_mode();
-    const bool rows = row_smem <= kRowSmemMax && mode >= 1;
-    const size_t staged_smem = sizeof(float) * (size_t)(L * W + W) + row_smem;
-    const bool staged = rows && mode == 2 && staged_smem <= kRowSmemMax;
+    const bool rows = row_smem <= kRowSmemMax && rows_enabled();
+    const int rt = row_threads();
     auto enqueue = [&](cudaStream_t s) -> int {
         if (x0 != x_out) SCI_CUDA(cudaMemcpyAsync(x_out, x0, 4 * n, cudaMemcpyDeviceToDevice, s));
         if (o->accelerate) SCI_CUDA(cudaMemsetAsync(y1, 0, 4 * nd, s));
         if (o->sqerr) SCI_CUDA(cudaMemsetAsync(o->sqerr, 0, sizeof(double) * o->iters, s));
         for (int it = 0; it < o->iters; ++it) {
             SCI_CHECK_ARG(o->weights[it] > 0.f, "sci_cassi_gap_tv: tv_weight must be > 0");
-            if (staged) {
+            if (rows) {
                 const unsigned g = (unsigned)std::min<int64_t>(H, (int64_t)kSMs * 8);
                 if (o->accelerate)
-                    k_cassi_proj_rows_staged<true><<<g, 256, staged_smem, s>>>(
+                    k_cassi_proj_rows<true><<<g, rt, row_smem, s>>>(
                         x_out, phi, y, y1, phisum, xp, o->lambdas[it], (int)L, (int)H, (int)W,
                         step);
                 else
-                    k_cassi_proj_rows_staged<false><<<g, 256, staged_smem, s>>>(
-                        x_out, phi, y, y1, phisum, xp, o->lambdas[it], (int)L, (int)H, (int)W,
-                        step);
-                SCI_LAUNCHED("k_cassi_proj_rows_staged");
-            } else if (rows) {
-                const unsigned g = (unsigned)std::min<int64_t>(H, (int64_t)kSMs * 8);
-                if (o->accelerate)
-                    k_cassi_proj_rows<true><<<g, 256, row_smem, s>>>(
-                        x_out, phi, y, y1, phisum, xp, o->lambdas[it], (int)L, (int)H, (int)W,
-                        step);
-                else
-                    k_cassi_proj_rows<false><<<g, 256, row_smem, s>>>(
+                    k_cassi_proj_rows<false><<<g, rt, row_smem, s>>>(
                         x_out, phi, y, y1, phisum, xp, o->lambdas[it], (int)L, (int)H, (int)W,
                         step);
                 SCI_LAUNCHED("k_cassi_proj_rows");

@@ -90,15 +90,18 @@ def test_cassi_admm_plugin_path():
 
 @pytest.mark.parametrize("accelerate", [True, False])
 def test_cassi_row_projection_and_graph_are_bitwise_equal(monkeypatch, accelerate):
-    """The row-fused projection (residual row in shared memory; the default,
-    or staged with the row's cube values) against the detector-grid +
+    """The row-fused projection (residual row in shared memory; 512 or 1024
+    threads per row) against the detector-grid +
     cube-grid kernel pair, and the captured graph (first run and replay)
     against direct launches: identical solves."""
     cube, phi, y = cassi_problem()
     op = sci.CassiOperator(phi, 28, 2)
     yd = torch.from_numpy(y).float().to(op.dev)
     out = []
-    for rows, graph in (("2", True), ("2", False), ("1", False), ("0", False), ("0", True)):
+    for rows, graph in (("1", True), ("1", False), ("1024", False), ("0", False), ("0", True)):
+        if rows == "1024":
+            monkeypatch.setenv("SCI_CASSI_ROWT", rows)
+            rows = "1"
         monkeypatch.setenv("SCI_CASSI_ROWS", rows)
         s = sci.CassiSolver(op, 12, 1.0, 0.05, 5, accelerate=accelerate, use_graph=graph)
         out.append(s.run(yd).clone())
