@@ -32,6 +32,8 @@ struct Workspace {
     double *energy;  // [nf][K][2]
     int *done;       // [nf]
     float *pa, *pb;  // [nf][2][H][W] each (multi-pass only)
+    int *stopj;      // [nf]: the stop decision of the current pass
+    unsigned *ticket;  // right after the energies, so that one memset clears both
 };
 
 static size_t ws_layout(int64_t nf, int64_t H, int64_t W, int K, Workspace *w, char *base) {
@@ -41,8 +43,10 @@ static size_t ws_layout(int64_t nf, int64_t H, int64_t W, int K, Workspace *w, c
         off += (bytes + 255) & ~size_t(255);
         return o;
     };
-    const size_t oe = take(sizeof(double) * (size_t)(nf * K * 2));
+    const size_t ne = sizeof(double) * (size_t)(nf * K * 2);
+    const size_t oe = take(ne + sizeof(double));
     const size_t od = take(sizeof(int) * (size_t)nf);
+    const size_t oj = take(sizeof(int) * (size_t)nf);
     size_t opa = 0, opb = 0;
     if (K - 1 > SMAX) {
         opa = take(sizeof(float) * (size_t)(nf * 2 * H * W));
@@ -50,7 +54,9 @@ static size_t ws_layout(int64_t nf, int64_t H, int64_t W, int K, Workspace *w, c
     }
     if (w) {
         w->energy = reinterpret_cast<double *>(base + oe);
+        w->ticket = reinterpret_cast<unsigned *>(base + oe + ne);
         w->done = reinterpret_cast<int *>(base + od);
+        w->stopj = reinterpret_cast<int *>(base + oj);
         w->pa = (K - 1 > SMAX) ? reinterpret_cast<float *>(base + opa) : nullptr;
         w->pb = (K - 1 > SMAX) ? reinterpret_cast<float *>(base + opb) : nullptr;
     }
@@ -156,7 +162,13 @@ static int tv_launch_core(const float *f, float *u, float *resid, int64_t nf, in
     Workspace w;
     ws_layout(nf, H, W, K, &w, static_cast<char *>(workspace));
     double *energy = energy_out ? energy_out : w.energy;
-    SCI_CUDA(cudaMemsetAsync(energy, 0, sizeof(double) * (size_t)(nf * K * 2), s));
+    const size_t ne = sizeof(double) * (size_t)(nf * K * 2);
+    if (energy == w.energy) {
+        SCI_CUDA(cudaMemsetAsync(energy, 0, ne + sizeof(unsigned), s));  // and the ticket
+    } else {
+        SCI_CUDA(cudaMemsetAsync(energy, 0, ne, s));
+        SCI_CUDA(cudaMemsetAsync(w.ticket, 0, sizeof(unsigned), s));
+    }
     const int U = K - 1;  // dual updates
     // done flags are read only by later passes; steps are written by the
     // stop-test launch of the last window (K >= 3) or here
@@ -220,6 +232,12 @@ static int tv_launch_core(const float *f, float *u, float *resid, int64_t nf, in
         P.vec = vec ? 1 : 0;
         P.tape_p = ra.tape_p;
         P.tape_u = ra.tape_u;
+        // the stop test can change the result only when a step k in
+        // [1, K-2] lies in this pass's window; then the main launch's last
+        // block decides it per frame
+        const bool stop_test = !no_stop && std::max(1, a) <= std::min(a + SG - 1, K - 2);
+        P.stopj = stop_test ? w.stopj : nullptr;
+        P.ticket = stop_test ? w.ticket : nullptr;
         const int per_frame_blocks = (P.nbands * P.nchunks + WPB - 1) / WPB;
         P.gpf = std::max(1, std::min(per_frame_blocks, 16));
         if (tape) {
@@ -240,9 +258,7 @@ static int tv_launch_core(const float *f, float *u, float *resid, int64_t nf, in
             launch_main123(P, SG, PIN, s);
         }
         SCI_LAUNCHED("k_tv_main");
-        // the stop test can change the result only when a step k in
-        // [1, K-2] lies in this pass's window
-        if (!no_stop && std::max(1, a) <= std::min(a + SG - 1, K - 2)) {
+        if (stop_test) {
             if (proj) launch_fixup_proj(P, s);
             else launch_fixup(P, PIN, s);
             SCI_LAUNCHED("k_tv_fixup");

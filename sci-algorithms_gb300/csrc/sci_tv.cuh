@@ -27,11 +27,12 @@
 // Stop test.  The per-frame energies E_k need whole-frame sums, which a
 // tiled pipeline sees only after every tile has finished.  The pass
 // therefore runs all of its steps speculatively, accumulating per-frame
-// float64 sums of (div p_k)^2 and n_k; a second launch of the same kernel
-// ("fixup") evaluates the stop rule per frame in float64 and re-runs only
-// the frames that would have stopped inside the pass, with the shorter step
-// count.  Frames that do not stop (nearly all, for n_iter_max = 5) cost the
-// fixup one read of a few doubles.
+// float64 sums of (div p_k)^2 and n_k; the work item that finishes last
+// (the last ticket of the launch) evaluates the stop rule per frame in
+// float64, and a second launch ("fixup") re-runs only the frames that would
+// have stopped inside the pass, with the shorter step count.  Frames that
+// do not stop (nearly all, for n_iter_max = 5) cost the fixup one read of
+// an int per work item.
 //
 // More than 4 dual updates are split into passes of at most 4 that carry p
 // through a workspace (p_in / p_out), with the same speculative scheme per
@@ -89,6 +90,13 @@ struct Pass {
     // writes its p_k to tape_p [S][nf][2][H][W] and, for k < S, its u_k to
     // tape_u [S-1][nf][H][W] (the reverse pass of the unrolled solver).
     float *tape_p, *tape_u;
+    // Stop decisions of the pass (nullable; kernels with energies): the
+    // main launch's last block to finish writes stopj[frame] = the stop
+    // index j in this pass's window, -1 for none, -2 for a frame stopped in
+    // an earlier window; ticket counts the main launch's finished blocks
+    // (zero when it starts; the last block resets it).
+    int *stopj;
+    unsigned *ticket;
 };
 
 // Dual update rules of the pipeline (the dual p is held as p / lambda for
@@ -493,6 +501,8 @@ __device__ __forceinline__ void run(const Pass &P, int frame, int chunk, int ban
             for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
             if (lane == 0) atomicAdd(eb + 2 * (P.a + k), v);
         }
+        // the sums are in before the block draws its ticket (decide_stops)
+        if (lane == 0 && P.ticket) __threadfence();
     }
 }
 
@@ -725,6 +735,8 @@ __device__ __forceinline__ void run2(const Pass &P, int frame, int chunk, int ba
             for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(FULL, v, o);
             if (lane == 0) atomicAdd(eb + 2 * (P.a + k), v);
         }
+        // the sums are in before the block draws its ticket (decide_stops)
+        if (lane == 0 && P.ticket) __threadfence();
     }
 }
 
@@ -772,17 +784,21 @@ __device__ __forceinline__ bool decode_item(const Pass &P, int &frame, int &chun
 }
 
 // First j in this pass's window with |E_{j-1} - E_j| < eps * E_0, or -1.
+// CG: read the sums from L2 (they were added by other blocks' atomics
+// during the same launch).
+template <bool CG = false>
 __device__ __forceinline__ int find_stop(const Pass &P, int frame) {
     const int SG = P.S;
     const double *eb = P.energy + (int64_t)frame * P.K * 2;
+    auto ld = [&](int i) { return CG ? __ldcg(eb + i) : eb[i]; };
     const double inv = 1.0 / ((double)P.H * (double)P.W);
     const double w = (double)P.weight;
     const int j0 = max(1, P.a), j1 = min(P.a + SG - 1, P.K - 2);
     if (j0 > j1) return -1;
-    const double e0 = (eb[0] + w * eb[1]) * inv;
-    double eprev = (eb[2 * (j0 - 1)] + w * eb[2 * (j0 - 1) + 1]) * inv;
+    const double e0 = (ld(0) + w * ld(1)) * inv;
+    double eprev = (ld(2 * (j0 - 1)) + w * ld(2 * (j0 - 1) + 1)) * inv;
     for (int j = j0; j <= j1; ++j) {
-        const double e = (eb[2 * j] + w * eb[2 * j + 1]) * inv;
+        const double e = (ld(2 * j) + w * ld(2 * j + 1)) * inv;
         if (fabs(eprev - e) < (double)P.eps * e0) return j;
         eprev = e;
     }
@@ -792,16 +808,39 @@ __device__ __forceinline__ int find_stop(const Pass &P, int frame) {
 template <int CPL>
 constexpr int min_blocks() { return CPL == 2 ? 4 : 3; }
 
+// The main launch's last work item to finish evaluates the stop rule of
+// every frame into P.stopj (a warp learns that it is the last from the
+// ticket its lane 0 draws after the warp's energy sums are in; no warp
+// waits), so that the stop-test launch reads one int per work item instead
+// of the sums.  Every work item (warp) of the launch draws one ticket.
+__device__ __forceinline__ void decide_stops(const Pass &P, int lane) {
+    const unsigned items = (unsigned)((int64_t)P.nbands * P.nchunks * P.nf);
+    unsigned t = 0;
+    if (lane == 0) t = atomicAdd(P.ticket, 1u);
+    t = __shfl_sync(FULL, t, 0);
+    if (t != items - 1) return;
+    __threadfence();
+    for (int f = lane; f < P.nf; f += 32) {
+        const int d = P.a > 0 ? P.done[f] : -1;
+        P.stopj[f] = (d >= 0 && d < P.a) ? -2 : find_stop<true>(P, f);
+    }
+    if (lane == 0) *P.ticket = 0u;
+}
+
 // Main launch of one pass: every frame not yet stopped runs all SG updates.
 template <int SG, bool PIN, bool FINAL, int CPL, int LAG = 1, int PROJ = 0,
           int RULE = RULE_SKIMAGE, bool TAPE = false>
 __global__ void __launch_bounds__(WPB * 32, min_blocks<CPL>()) k_tv_main(Pass P) {
     int frame, chunk, band;
     if (!decode_item(P, frame, chunk, band)) return;
-    if (PIN && P.done[frame] >= 0) return;  // stopped in an earlier pass
     // the MATLAB rules and the taped runs have no stop test and need no energies
-    run_mode<SG, CPL, PIN, FINAL, RULE == RULE_SKIMAGE && !TAPE, LAG, PROJ, RULE, TAPE>(
-        P, frame, chunk, band, threadIdx.x & 31);
+    constexpr bool EN = RULE == RULE_SKIMAGE && !TAPE;
+    const int lane = threadIdx.x & 31;
+    if (!(PIN && P.done[frame] >= 0))  // not stopped in an earlier pass
+        run_mode<SG, CPL, PIN, FINAL, EN, LAG, PROJ, RULE, TAPE>(P, frame, chunk, band, lane);
+    if constexpr (EN) {
+        if (P.ticket) decide_stops(P, lane);
+    }
 }
 
 // Stop-test launch of one pass over the same work items as the main launch:
@@ -812,11 +851,17 @@ template <bool PIN, int CPL, int PROJ = 0>
 __global__ void __launch_bounds__(WPB * 32, min_blocks<CPL>()) k_tv_fixup(Pass P) {
     int frame, chunk, band;
     if (!decode_item(P, frame, chunk, band)) return;
-    if (PIN) {
-        const int d = P.done[frame];
-        if (d >= 0 && d < P.a) return;  // stopped in an earlier window
+    int j;
+    if (P.stopj) {
+        j = P.stopj[frame];  // decided by the main launch
+        if (j == -2) return;  // stopped in an earlier window
+    } else {
+        if (PIN) {
+            const int d = P.done[frame];
+            if (d >= 0 && d < P.a) return;  // stopped in an earlier window
+        }
+        j = find_stop(P, frame);
     }
-    const int j = find_stop(P, frame);
     const int lane = threadIdx.x & 31;
     const bool lead = (chunk == 0 && band == 0 && lane == 0);
     if (j < 0) {
