@@ -429,7 +429,7 @@ __device__ __forceinline__ void step(const Pass &P, const St<S, CPL> &in, St<S, 
 }
 
 template <int S, int CPL, bool PIN, bool OUT_U, bool ENERGY, int MODE, int PROJ,
-          int RULE = RULE_SKIMAGE, bool TAPE = false>
+          int RULE = RULE_SKIMAGE, bool TAPE = false, bool RES = true>
 __device__ __forceinline__ void run(const Pass &P, int frame, int chunk, int band, int lane) {
     const int H = P.H, W = P.W;
     Lane<CPL> L;
@@ -451,7 +451,8 @@ __device__ __forceinline__ void run(const Pass &P, int frame, int chunk, int ban
     const float *fb = P.f + (int64_t)frame * P.fs;
     const float *pinb = PIN ? P.p_in + (int64_t)frame * 2 * hw : nullptr;
     float *ob = OUT_U ? P.u + (int64_t)frame * P.fs : P.p_out + (int64_t)frame * 2 * hw;
-    float *rb = (OUT_U && P.resid) ? P.resid + (int64_t)frame * P.fs : nullptr;
+    // RES = false: compiled without the residual output (P.resid is null)
+    float *rb = (RES && OUT_U && P.resid) ? P.resid + (int64_t)frame * P.fs : nullptr;
     const bool vec = P.vec != 0;
 
     St<S, CPL> A, B;
@@ -741,7 +742,7 @@ __device__ __forceinline__ void run2(const Pass &P, int frame, int chunk, int ba
 }
 
 template <int S, int CPL, bool PIN, bool OUT_U, bool ENERGY, int LAG = 1, int PROJ = 0,
-          int RULE = RULE_SKIMAGE, bool TAPE = false>
+          int RULE = RULE_SKIMAGE, bool TAPE = false, bool RES = true>
 __device__ __forceinline__ void run_mode(const Pass &P, int frame, int chunk, int band, int lane) {
     const int c0 = band * P.own - P.hl;
     const bool interior = P.vec && c0 >= 0 && c0 + 32 * CPL - 1 <= P.W - 1;
@@ -751,10 +752,11 @@ __device__ __forceinline__ void run_mode(const Pass &P, int frame, int chunk, in
         else run2<S, CPL, PIN, OUT_U, ENERGY, EDGE>(P, frame, chunk, band, lane);
     } else {
         if (interior)
-            run<S, CPL, PIN, OUT_U, ENERGY, INTERIOR, PROJ, RULE, TAPE>(P, frame, chunk, band,
-                                                                         lane);
+            run<S, CPL, PIN, OUT_U, ENERGY, INTERIOR, PROJ, RULE, TAPE, RES>(P, frame, chunk,
+                                                                              band, lane);
         else
-            run<S, CPL, PIN, OUT_U, ENERGY, EDGE, PROJ, RULE, TAPE>(P, frame, chunk, band, lane);
+            run<S, CPL, PIN, OUT_U, ENERGY, EDGE, PROJ, RULE, TAPE, RES>(P, frame, chunk, band,
+                                                                          lane);
     }
 }
 
@@ -829,7 +831,7 @@ __device__ __forceinline__ void decide_stops(const Pass &P, int lane) {
 
 // Main launch of one pass: every frame not yet stopped runs all SG updates.
 template <int SG, bool PIN, bool FINAL, int CPL, int LAG = 1, int PROJ = 0,
-          int RULE = RULE_SKIMAGE, bool TAPE = false>
+          int RULE = RULE_SKIMAGE, bool TAPE = false, bool RES = true>
 __global__ void __launch_bounds__(WPB * 32, min_blocks<CPL>()) k_tv_main(Pass P) {
     int frame, chunk, band;
     if (!decode_item(P, frame, chunk, band)) return;
@@ -837,7 +839,8 @@ __global__ void __launch_bounds__(WPB * 32, min_blocks<CPL>()) k_tv_main(Pass P)
     constexpr bool EN = RULE == RULE_SKIMAGE && !TAPE;
     const int lane = threadIdx.x & 31;
     if (!(PIN && P.done[frame] >= 0))  // not stopped in an earlier pass
-        run_mode<SG, CPL, PIN, FINAL, EN, LAG, PROJ, RULE, TAPE>(P, frame, chunk, band, lane);
+        run_mode<SG, CPL, PIN, FINAL, EN, LAG, PROJ, RULE, TAPE, RES>(P, frame, chunk, band,
+                                                                      lane);
     if constexpr (EN) {
         if (P.ticket) decide_stops(P, lane);
     }

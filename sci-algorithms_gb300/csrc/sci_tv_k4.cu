@@ -8,7 +8,10 @@ namespace tv {
 
 void launch_main4_c4(const Pass &P, bool pin, bool final_pass, cudaStream_t s) {
     const unsigned g = pass_blocks(P);
-    if (!pin && final_pass) k_tv_main<4, false, true, 4><<<g, WPB * 32, 0, s>>>(P);
+    // without a residual output the kernel is compiled without its code
+    if (!pin && final_pass && !P.resid)
+        k_tv_main<4, false, true, 4, 1, 0, RULE_SKIMAGE, false, false><<<g, WPB * 32, 0, s>>>(P);
+    else if (!pin && final_pass) k_tv_main<4, false, true, 4><<<g, WPB * 32, 0, s>>>(P);
     else if (!pin) k_tv_main<4, false, false, 4><<<g, WPB * 32, 0, s>>>(P);
     else if (final_pass) k_tv_main<4, true, true, 4><<<g, WPB * 32, 0, s>>>(P);
     else k_tv_main<4, true, false, 4><<<g, WPB * 32, 0, s>>>(P);
