@@ -157,9 +157,9 @@ __device__ __forceinline__ void issue_theta(float *xs, uint64_t *bars, int buf, 
 // Unroll of the band loops: the 16-byte loads of the second stack (b, or
 // the previous TV input) are in flight together per thread.  Measured on
 // the ADMM-TV solve at 2048 x 2048 x 24 (60 iterations), bitwise equal:
-// unroll 4 38.9 ms, 8 37.6 ms, 12 37.0 ms.
+// unroll 4 38.9 ms, 8 37.6 ms, 12 37.0 ms, 24 36.5 ms.
 #ifndef SCI_ADMM_UNROLL
-#define SCI_ADMM_UNROLL 12
+#define SCI_ADMM_UNROLL 24
 #endif
 constexpr int kAdmmUnroll = SCI_ADMM_UNROLL;
 
