@@ -107,6 +107,24 @@ def test_proj_gap_matches_reference_step(accelerate, packed, W):
         assert rel(y1d.cpu().numpy(), y1r) < RTOL
 
 
+def test_proj_gap_unit_mask_one_frame_gives_y():
+    """Known answer: Phi = 1, B = 1, lambda = 1 -- one GAP projection maps
+    any x to y (pnp_sci_algo.py:645 with A x = x, Phi_sum = 1)."""
+    rng = np.random.default_rng(12)
+    H, W = 33, 64
+    mask = np.ones((H, W, 1))
+    x = rng.random((H, W, 1))
+    y = rng.random((H, W))
+    op = sci.MaskOperator(mask)
+    xd, yd = _dev.planar(x), _dev.plane(y)
+    y1d = torch.zeros_like(yd)
+    psd = _dev.plane(np.ones((H, W)))
+    out = torch.empty_like(xd)
+    call("sci_proj_gap", xd.data_ptr(), op.phi.data_ptr(), _dev.ptr(op.bits), yd.data_ptr(),
+         y1d.data_ptr(), psd.data_ptr(), out.data_ptr(), 1.0, 0, 1, H, W, _dev.stream_handle())
+    np.testing.assert_allclose(out[0].cpu().numpy(), y.astype(np.float32), rtol=0, atol=1e-6)
+
+
 def device_status():
     v = ctypes.c_uint(0)
     call("sci_device_status", ctypes.byref(v), 1)

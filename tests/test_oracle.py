@@ -212,3 +212,37 @@ def test_c_oracle_solver_matches_golden(golden, case):
     # x_ of the driver is stored as float32 (pnp_sci_algo.py:494)
     assert rel < 1e-7
     np.testing.assert_allclose(pa, g["psnrall"][0], rtol=1e-6)
+
+
+def test_gap_step_with_unit_mask_and_one_frame_returns_y():
+    """Known answer: with Phi = 1 and B = 1, A x = x and Phi_sum = 1, so one
+    GAP projection (lambda = 1, pnp_sci_algo.py:645) maps any x to y."""
+    rng = np.random.default_rng(3)
+    mask = np.ones((20, 24, 1))
+    x = rng.random((20, 24, 1))
+    y = rng.random((20, 24))
+    msum = mask.sum(axis=2)
+    x1 = x + 1.0 * port.At_((y - port.A_(x, mask)) / msum, mask)
+    np.testing.assert_allclose(x1[..., 0], y, rtol=0, atol=1e-15)
+
+
+def test_tv_dual_objective_is_non_increasing():
+    """Chambolle's iteration decreases its dual objective ||f - div p_k||^2
+    = ||u_k||^2 step by step (Chambolle 2004, for the step 1/4 scikit-image
+    uses as well, checked here), while scikit-image's reported energy
+    E_k = (||f - u_k||^2 + w TV(u_k)) / (H W) need not decrease (its stop
+    rule compares successive values only)."""
+    rng = np.random.default_rng(4)
+    f = np.concatenate([rng.random((1, 40, 50)),
+                        np.cumsum(rng.standard_normal((1, 40, 50)), axis=2) * 0.05])
+    rises = 0
+    for w in (0.02, 0.1, 0.5):
+        norms = []
+        for K in range(1, 16):
+            u, steps, en = c_oracle.tv_chambolle(f, w, K, eps=0.0)
+            norms.append((u ** 2).sum(axis=(1, 2)))
+        d = np.diff(np.array(norms), axis=0)
+        assert np.all(d <= 1e-12 * norms[0]), w
+        e = c_oracle.tv_chambolle(f, w, 15, eps=0.0)[2]
+        rises += int((np.diff(e, axis=1) > 0).sum())
+    assert rises > 0  # the reported energy is not monotone: no test may assume it
