@@ -14,7 +14,6 @@
 #include <algorithm>
 #include <cstdlib>
 #include <cstring>
-#include <list>
 #include <map>
 #include <mutex>
 #include <string>

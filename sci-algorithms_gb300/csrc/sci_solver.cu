@@ -5,8 +5,6 @@
 // a CUDA graph that is cached per argument set and replayed with a single
 // launch.
 #include <cstring>
-#include <list>
-#include <mutex>
 #include <string>
 #include <utility>
 

@@ -20,8 +20,6 @@
 // then the adjoint of the projection (including d/dPhi through A, At and
 // Phi_sum, and d/dlambda_k), and finally of the measurement and x^0.
 #include <cstdlib>
-#include <list>
-#include <mutex>
 #include <string>
 
 #include "sci_common.cuh"
