@@ -110,3 +110,38 @@ def test_no_gpu_fails_loudly(monkeypatch):
     monkeypatch.setattr(torch.cuda, "is_available", lambda: False)
     with pytest.raises(RuntimeError, match="CUDA GPU"):
         sci.A_(np.zeros((4, 4, 2)), np.ones((4, 4, 2)))
+
+
+def test_argument_checks_of_the_wider_entry_points(L):
+    """Argument errors of the spectral, batched, unrolled, MATLAB-TV, metrics
+    and CNN entry points return -1 with a message before any device work
+    (no GPU needed)."""
+    s = None
+    n = ctypes.c_size_t()
+    # spectral: step must be >= 1; null buffers
+    assert L.sci_cassi_workspace_bytes(28, 256, 256, 0, 5, ctypes.byref(n)) == -1
+    assert "step" in _lib.last_error()
+    o = _lib.SolveOpts()
+    o.iters, o.tv_iter_max = 4, 5
+    assert L.sci_cassi_gap_tv(None, 1, 1, 1, 1, 28, 256, 256, 2, ctypes.byref(o), 1, 1, s) == -1
+    assert "null" in _lib.last_error()
+    # batched: 1..256 items, tv_iter_max in [2, 5]
+    items = (_lib.BatchItem * 1)()
+    assert L.sci_batch_workspace_bytes(items, 0, 5, ctypes.byref(n)) == -1
+    assert "items" in _lib.last_error()
+    assert L.sci_batch_workspace_bytes(items, 1, 9, ctypes.byref(n)) == -1
+    assert "tv_iter_max" in _lib.last_error()
+    # unrolled: tv_iters in [2, 5], K >= 1
+    assert L.sci_unrolled_workspace_bytes(16, 8, 256, 256, 20, 7, ctypes.byref(n)) == -1
+    assert "tv_iters" in _lib.last_error()
+    assert L.sci_unrolled_workspace_bytes(16, 8, 256, 256, 0, 5, ctypes.byref(n)) == -1
+    # MATLAB TVs: unknown kind, aliasing input and output
+    assert L.sci_tv_matlab(99, 1, 2, 4, 64, 64, ctypes.c_float(0.1), 5, None, 0, s) == -1
+    assert "kind" in _lib.last_error()
+    assert L.sci_tv_matlab(1, 1, 1, 4, 64, 64, ctypes.c_float(0.1), 5, None, 0, s) == -1
+    # per-frame metrics: frames of at least 7 x 7
+    assert L.sci_frame_metrics(1, 2, 4, 5, 64, 1.0, 3, 4, s) == -1
+    assert "7 x 7" in _lib.last_error()
+    # CNN first layer: null input
+    assert L.sci_cnn_conv_thin(None, 16, 32, 48, 8, 64, 64, 96, 1, s) == -1
+    assert "null" in _lib.last_error()
