@@ -142,7 +142,8 @@ int sci_tv_chambolle(const float *f, float *u, float *resid, int64_t nframes,
  * scratch is a fixed 64 KiB array in the library's device image (kept on
  * every GPU that loads the library until exit), so it needs no workspace
  * argument.  Limits: n_iter_max <= 5 and nframes * n_iter_max * 16 bytes
- * (+ 4 bytes per frame) <= 64 KiB (nframes <= 777 at n_iter_max = 5);
+ * (+ 8 bytes per frame, with alignment) <= 64 KiB (nframes <= 742 at
+ * n_iter_max = 5);
  * larger requests return SCI_ERR_INVALID_ARG.  All calls share the array:
  * calls whose work overlaps on the GPU race and must be ordered by the
  * caller.  The first call on a device looks up the array's address; make

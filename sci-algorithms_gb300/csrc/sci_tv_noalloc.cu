@@ -12,8 +12,9 @@
 // Limits and behaviour:
 //  * the scratch array is 64 KiB; a call fits when n_iter_max <= 5 (one
 //    pipeline pass, so the dual field stays on chip) and the per-frame
-//    energy slots fit: nframes * n_iter_max * 16 bytes (+ 4 bytes a frame)
-//    <= 64 KiB, i.e. nframes <= 777 at n_iter_max = 5.  Larger requests
+//    energy slots fit: nframes * n_iter_max * 16 bytes (+ 8 bytes a frame
+//    for the stop flags and decisions, with alignment) <= 64 KiB, i.e.
+//    nframes <= 742 at n_iter_max = 5.  Larger requests
 //    are rejected with SCI_ERR_INVALID_ARG and a message;
 //  * every GPU that loads the library keeps the 64 KiB until the process
 //    exits;

@@ -145,3 +145,11 @@ def test_argument_checks_of_the_wider_entry_points(L):
     # CNN first layer: null input
     assert L.sci_cnn_conv_thin(None, 16, 32, 48, 8, 64, 64, 96, 1, s) == -1
     assert "null" in _lib.last_error()
+
+
+def test_noalloc_scratch_limit_is_as_documented(L):
+    """The allocation-free TV's fixed 64 KiB scratch holds the workspace of
+    742 frames at n_iter_max = 5 and not of 743 (sci_gb300.h)."""
+    n = ctypes.c_size_t()
+    assert L.sci_tv_workspace_bytes(742, 64, 64, 5, ctypes.byref(n)) == 0 and n.value <= 64 * 1024
+    assert L.sci_tv_workspace_bytes(743, 64, 64, 5, ctypes.byref(n)) == 0 and n.value > 64 * 1024
