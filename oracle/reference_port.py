@@ -126,14 +126,31 @@ def _check_denoiser(denoiser, tvm):
         raise ValueError('oracle supports denoiser "tv" (tv_chambolle), "ffdnet", "fastdvdnet"')
 
 
-def _denoise(x, denoiser, w, eps, tv_iter_max, multichannel, nsig, model):
+def _denoise(x, denoiser, w, eps, tv_iter_max, multichannel, nsig, model, threads=1):
     """The denoiser switch of gap_denoise / admm_denoise (pnp_sci_algo.py:647-672)."""
     d = denoiser.lower()
     if d == 'ffdnet':
         return _cnn.ffdnet_vdenoiser(x, nsig, model)
     if d == 'fastdvdnet':
         return _cnn.fastdvdnet_denoiser(x, nsig, model, gray=True)
-    return denoise_tv_chambolle(x, w, eps=eps, n_iter_max=tv_iter_max, multichannel=multichannel)
+    return denoise_tv_chambolle(x, w, eps=eps, n_iter_max=tv_iter_max, multichannel=multichannel,
+                                threads=threads)
+
+
+def gap_iteration(y, y1, x, Phi_sum, A, At, lam, w, accelerate=True, denoiser='tv',
+                  eps=2.e-4, tv_iter_max=5, multichannel=True, nsig=None, model=None,
+                  threads=1):
+    """One iteration of ``gap_denoise``'s loop (``pnp_sci_algo.py:639-650``):
+    the GAP (``:645``) or accelerated GAP (``:641-643``) projection, then the
+    denoiser (its frames on ``threads`` threads).  Returns the new (x, y1)."""
+    yb = A(x)
+    if accelerate:
+        y1 = y1 + (y - yb)
+        x = x + lam * (At((y1 - yb) / Phi_sum))
+    else:
+        x = x + lam * (At((y - yb) / Phi_sum))
+    x = _denoise(x, denoiser, w, eps, tv_iter_max, multichannel, nsig, model, threads)
+    return x, y1
 
 
 def gap_denoise(y, Phi_sum, A, At, _lambda=1, accelerate=True,
@@ -162,15 +179,9 @@ def gap_denoise(y, Phi_sum, A, At, _lambda=1, accelerate=True,
     k = 0
     for idx, nsig in enumerate(sigma):
         for it in range(iter_max[idx]):
-            lam = _at(_lambda, k)
-            w = _at(tv_weight, k)
-            yb = A(x)
-            if accelerate:
-                y1 = y1 + (y - yb)
-                x = x + lam * (At((y1 - yb) / Phi_sum))
-            else:
-                x = x + lam * (At((y - yb) / Phi_sum))
-            x = _denoise(x, denoiser, w, eps, tv_iter_max, multichannel, nsig, model)
+            x, y1 = gap_iteration(y, y1, x, Phi_sum, A, At, _at(_lambda, k), _at(tv_weight, k),
+                                  accelerate, denoiser, eps, tv_iter_max, multichannel, nsig,
+                                  model)
             if show_iqa and X_orig is not None:
                 psnr_all.append(psnr(X_orig, x))
                 if verbose and (k + 1) % 5 == 0:

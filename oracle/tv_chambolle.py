@@ -29,9 +29,11 @@ The arithmetic below keeps scikit-image's order of numpy operations, so a
 run in float64 is meant to be bit-identical to it.  scikit-image itself is
 not installed anywhere this project runs, so that claim is UNPINNED: the
 restatement is checked only through the known-answer properties in
-``tests/test_oracle.py`` (constant frames, n_iter_max=1, energy decrease,
-the in-repo MATLAB Chambolle variant
-``PnP_SCI/matlab/algorithms/tvdenoisers/tvdenoise_cham_ITV2D.m:49-93``).
+``tests/test_oracle.py``: constant frames are fixed points, n_iter_max=1
+returns the input, the stop rule, the decrease of Chambolle's dual
+objective ||f - div p_k||^2 (the reported energy E_k itself is not
+monotone and no test relies on it), and the in-repo MATLAB Chambolle
+variant ``PnP_SCI/matlab/algorithms/tvdenoisers/tvdenoise_cham_ITV2D.m:49-93``.
 """
 import numpy as np
 
@@ -91,21 +93,31 @@ def _tv_chambolle_nd(image, weight, eps, n_iter_max):
 
 
 def denoise_tv_chambolle(image, weight=0.1, eps=2.e-4, n_iter_max=200,
-                         multichannel=False):
+                         multichannel=False, threads=1):
     """scikit-image 0.16 ``denoise_tv_chambolle`` semantics (see module doc).
 
     With ``multichannel=True`` every slice ``image[..., c]`` is denoised as
     an independent image, which is how the GAP/ADMM drivers use it on an
-    H x W x B frame stack.
+    H x W x B frame stack.  ``threads`` > 1 denoises the slices on a thread
+    pool (numpy releases the interpreter lock inside its array loops); the
+    slices are independent, so the result is the same.
     """
     image = np.asarray(image)
     if image.dtype.kind != 'f':
         raise TypeError("the oracle TV takes floating-point images only")
     if multichannel:
         out = np.zeros_like(image)
-        for c in range(image.shape[-1]):
-            out[..., c] = _tv_chambolle_nd(image[..., c], weight, eps,
-                                           n_iter_max)[0]
+
+        def one(c):
+            out[..., c] = _tv_chambolle_nd(image[..., c], weight, eps, n_iter_max)[0]
+
+        if threads > 1:
+            from concurrent.futures import ThreadPoolExecutor
+            with ThreadPoolExecutor(max_workers=threads) as ex:
+                list(ex.map(one, range(image.shape[-1])))
+        else:
+            for c in range(image.shape[-1]):
+                one(c)
         return out
     return _tv_chambolle_nd(image, weight, eps, n_iter_max)[0]
 

@@ -79,7 +79,45 @@ static int choose_R(int64_t nf, int nbands, int H) {
     return R;
 }
 
+// Rows per chunk for the register-lean pass: the grid runs in waves of
+// `resident` warps, each work item of R rows costs about R + S + 4 pipeline
+// steps, so the chunking that minimises waves x (R + S + 4) is taken (a
+// last wave that is half empty costs a whole wave).
+static int choose_R_slim(int64_t nf, int nbands, int H, int S, int64_t resident) {
+    if (const char *e = getenv("SCI_TV_R")) {
+        const int v = atoi(e);
+        if (v >= 8) return v;
+    }
+    int best_R = H;
+    double best = -1.0;
+    const int max_chunks = std::max(1, H / 16);
+    for (int nc = 1; nc <= max_chunks; ++nc) {
+        const int R = (H + nc - 1) / nc;
+        const int64_t items = nf * nbands * (int64_t)((H + R - 1) / R);
+        const int64_t waves = (items + resident - 1) / resident;
+        const double cost = (double)waves * (R + S + 4);
+        if (best < 0.0 || cost < best - 1e-9) {
+            best = cost;
+            best_R = R;
+        }
+    }
+    return best_R;
+}
+
 }  // namespace tv
+
+// Register-lean TV pass (sci_tv_slim.cuh) for single-pass scikit-image runs
+// on 16-byte aligned frames at least 512 columns wide; SCI_TV_SLIM=0 selects
+// the generic pipeline instead.  SCI_SLIM_MINB picks its register budget
+// (3 or 4 resident blocks per SM).
+static bool slim_enabled() {
+    const char *e = getenv("SCI_TV_SLIM");
+    return !e || atoi(e) != 0;
+}
+static int slim_minb() {
+    const char *e = getenv("SCI_SLIM_MINB");
+    return (e && atoi(e) == 3) ? 3 : 4;
+}
 
 // Columns per lane: 4 halves the halo overhead of a band (8 of 128 columns
 // instead of 8 of 64) but doubles the registers of the pipeline state; 2
@@ -183,6 +221,9 @@ static int tv_launch_core(const float *f, float *u, float *resid, int64_t nf, in
     const bool vec = (W % cpl == 0) && (fs % cpl == 0) &&
                      ((reinterpret_cast<uintptr_t>(f) | reinterpret_cast<uintptr_t>(u) |
                        reinterpret_cast<uintptr_t>(resid)) % (4 * cpl) == 0);
+    const bool slim = slim_enabled() && ra.rule == RULE_SKIMAGE && !tape && !proj && !resid &&
+                      U <= SMAX && cpl == 4 && lag == 1 && vec && W >= 4;
+    const int minb = slim_minb();
     const float *pin = nullptr;
     float *pbuf[2] = {w.pa, w.pb};
     int pi = 0;
@@ -226,7 +267,11 @@ static int tv_launch_core(const float *f, float *u, float *resid, int64_t nf, in
         P.lam = proj_lam;
         P.frame_fast = frame_fast_order(proj);
         P.nbands = (int)((W + P.own - 1) / P.own);
-        P.R = force_R > 0 ? force_R : choose_R(nf, P.nbands, (int)H);
+        if (force_R > 0) P.R = force_R;
+        else if (slim)
+            P.R = choose_R_slim(nf, P.nbands, (int)H, SG,
+                                (int64_t)kSMs * slim_resident_blocks(SG, minb) * WPB);
+        else P.R = choose_R(nf, P.nbands, (int)H);
         P.nchunks = (int)((H + P.R - 1) / P.R);
         P.S = SG;
         P.vec = vec ? 1 : 0;
@@ -240,7 +285,9 @@ static int tv_launch_core(const float *f, float *u, float *resid, int64_t nf, in
         P.ticket = stop_test ? w.ticket : nullptr;
         const int per_frame_blocks = (P.nbands * P.nchunks + WPB - 1) / WPB;
         P.gpf = std::max(1, std::min(per_frame_blocks, 16));
-        if (tape) {
+        if (slim) {
+            launch_slim(P, SG, minb, s);
+        } else if (tape) {
             launch_tape(P, SG, s);
         } else if (ra.rule == RULE_CHAM_ITV) {
             launch_rule1(P, SG, PIN, FINAL, s);
@@ -259,7 +306,8 @@ static int tv_launch_core(const float *f, float *u, float *resid, int64_t nf, in
         }
         SCI_LAUNCHED("k_tv_main");
         if (stop_test) {
-            if (proj) launch_fixup_proj(P, s);
+            if (slim) launch_slim_fix(P, minb, s);
+            else if (proj) launch_fixup_proj(P, s);
             else launch_fixup(P, PIN, s);
             SCI_LAUNCHED("k_tv_fixup");
         }

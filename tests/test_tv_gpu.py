@@ -113,3 +113,76 @@ def test_denoise_tv_chambolle_api():
     assert out3.is_cuda and torch.allclose(out3.double().cpu(), torch.from_numpy(out), atol=1e-6)
     with pytest.raises(NotImplementedError):
         sci.denoise_tv_chambolle(f, 0.1, multichannel=False)
+
+
+# Frames wider than 512 columns run the register-lean single-pass kernel
+# (sci_tv_slim.cuh); SCI_TV_SLIM=0 selects the generic pipeline.  The two
+# perform the same float32 operations in the same order, so their frames are
+# bit-identical and their stop steps equal.
+SLIM_SHAPES = [(64, 1024, 3), (257, 516, 2), (130, 2048, 2), (33, 640, 5), (40, 520, 2),
+               (200, 1028, 3), (7, 1536, 2)]
+
+
+def _tv_env(monkeypatch, fp, weight, K, eps, slim, R=None):
+    monkeypatch.setenv("SCI_TV_SLIM", slim)
+    if R is None:
+        monkeypatch.delenv("SCI_TV_R", raising=False)
+    else:
+        monkeypatch.setenv("SCI_TV_R", str(R))
+    nf = fp.shape[0]
+    steps = torch.zeros(nf, dtype=torch.int32, device=fp.device)
+    energy = torch.zeros((nf, K, 2), dtype=torch.float64, device=fp.device)
+    u = sci.tv_frames(fp, weight, K, eps, steps=steps, energy=energy)
+    torch.cuda.synchronize()
+    return u, steps.cpu().numpy(), energy.cpu().numpy()
+
+
+@pytest.mark.parametrize("H,W,F", SLIM_SHAPES)
+@pytest.mark.parametrize("K", [2, 3, 4, 5])
+def test_tv_slim_bitwise_equals_generic(H, W, F, K, monkeypatch):
+    f = smooth_frames(H, W, F, seed=7 * H + W + K)
+    fp = _dev.planar(f)
+    u0, s0, e0 = _tv_env(monkeypatch, fp, 0.1, K, 2e-4, "0")
+    u1, s1, e1 = _tv_env(monkeypatch, fp, 0.1, K, 2e-4, "1")
+    assert torch.equal(u0, u1)
+    assert list(s0) == list(s1)
+    # the energy sums are float32 per lane and chunk (the two kernels may
+    # chunk the rows differently), then float64
+    np.testing.assert_allclose(e1, e0, rtol=1e-6, atol=0)
+
+
+@pytest.mark.parametrize("H,W,F", [(64, 1024, 3), (257, 516, 2), (33, 640, 5)])
+def test_tv_slim_matches_oracle(H, W, F, monkeypatch):
+    f = smooth_frames(H, W, F, seed=H + W)
+    ref, steps_ref, _ = tv_chambolle_frames(f, 0.1, n_iter_max=5)
+    u, steps, _ = _tv_env(monkeypatch, _dev.planar(f), 0.1, 5, 2e-4, "1")
+    assert np.max(np.abs(_dev.unplanar(u, f) - ref)) < ATOL
+    assert list(steps) == steps_ref
+
+
+@pytest.mark.parametrize("R", [8, 16, 29, 64])
+def test_tv_slim_row_chunks_and_early_stop(R, monkeypatch):
+    # forced chunk heights and stop rules that fire at steps 1..3 (the
+    # re-run launch of the lean kernel)
+    f = smooth_frames(150, 1032, 4, seed=R)
+    fp = _dev.planar(f)
+    for eps in (0.5, 0.2, 0.05, 0.02, 2e-4):
+        ref, steps_ref, _ = tv_chambolle_frames(f, 0.2, eps=eps, n_iter_max=5)
+        u1, s1, _ = _tv_env(monkeypatch, fp, 0.2, 5, eps, "1", R=R)
+        u0, s0, _ = _tv_env(monkeypatch, fp, 0.2, 5, eps, "0", R=R)
+        assert list(s1) == steps_ref, eps
+        assert list(s0) == list(s1), eps
+        assert torch.equal(u0, u1), eps
+        assert np.max(np.abs(_dev.unplanar(u1, f) - ref)) < ATOL
+
+
+def test_tv_slim_occupancy_variants(monkeypatch):
+    # the 3- and 4-blocks-per-SM builds of the lean kernel agree bit for bit
+    f = smooth_frames(96, 2048, 3, seed=3)
+    fp = _dev.planar(f)
+    monkeypatch.setenv("SCI_SLIM_MINB", "3")
+    u3, s3, _ = _tv_env(monkeypatch, fp, 0.1, 5, 2e-4, "1")
+    monkeypatch.setenv("SCI_SLIM_MINB", "4")
+    u4, s4, _ = _tv_env(monkeypatch, fp, 0.1, 5, 2e-4, "1")
+    assert torch.equal(u3, u4)
+    assert list(s3) == list(s4)
