@@ -492,13 +492,27 @@ def run_gpu(args):
              y1.data_ptr(), op.phisum.data_ptr(), xout.data_ptr(), 1.0, 1, B, H, W,
              stream.cuda_stream)
 
+    cmap = torch.empty((H, W), dtype=torch.float32, device=dev)
+
+    def resid_once():
+        call("sci_gap_residual", xin.data_ptr(), None, op.bits.data_ptr(), y.data_ptr(),
+             y1.data_ptr(), op.phisum.data_ptr(), cmap.data_ptr(), 1, B, H, W,
+             stream.cuda_stream)
+
     ms_tv = timed(tv_once, 20, 3)
     ms_proj = timed(proj_once, 20, 3)
+    ms_resid = timed(resid_once, 20, 3)
     peak, peak_kind = load_peaks()
+    hw = float(H * W)
     tv_bytes = 8.0 * n                      # read x, write u (p stays on chip)
-    proj_bytes = 8.0 * n + 4.0 * H * W + 16.0 * H * W  # x r/w, mask words, y/y1/phisum/y1
+    proj_bytes = 8.0 * n + 4.0 * hw + 16.0 * hw  # x r/w, mask words, y/y1/phisum/y1
+    resid_bytes = 4.0 * n + 24.0 * hw       # read x, mask words, y/y1/phisum; write c, y1
     tv_gbs = tv_bytes / (ms_tv * 1e-3) / 1e9
     proj_gbs = proj_bytes / (ms_proj * 1e-3) / 1e9
+    # the iteration the solver runs: the fused form (residual pass, then the TV
+    # pass applying the projection as it loads x: 8N + 8HW) unless it is off
+    fused = os.environ.get("SCI_FUSED_PROJ", "1") != "0"
+    iter_bytes = (resid_bytes + tv_bytes + 8.0 * hw) if fused else (proj_bytes + tv_bytes)
 
     # end to end through the public API with host buffers: one call per
     # sequence of measurements (run_host_many: every step's measurement
@@ -537,7 +551,7 @@ def run_gpu(args):
         parity = None
         if world == 1 and not args.no_parity:
             parity = parity_report(dev, n=args.parity_size)
-        per_iter_bytes = proj_bytes + tv_bytes
+        per_iter_bytes = iter_bytes
         line = {
             "metric": METRIC, "value": world * ITERS * 1e3 / ms_gap, "unit": "iter/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
@@ -559,8 +573,14 @@ def run_gpu(args):
                            "proj_kernel": "k_proj_gap_tma<128> (bulk-copy staged)",
                            "proj_gbs": proj_gbs, "proj_frac": proj_gbs / peak,
                            "proj_traffic": ncu_traffic("k_proj_gap_tma"),
+                           "resid_ms": ms_resid,
+                           "resid_gbs": resid_bytes / (ms_resid * 1e-3) / 1e9,
+                           "iteration": ("residual pass + TV pass with the projection applied "
+                                         "on load" if fused else "projection + TV pass"),
                            "per_iteration_algorithmic_bytes": per_iter_bytes,
-                           "per_iteration_gbs": per_iter_bytes * ITERS / (ms_gap * 1e-3) / 1e9}
+                           "per_iteration_gbs": per_iter_bytes * ITERS / (ms_gap * 1e-3) / 1e9,
+                           "per_iteration_frac": (per_iter_bytes * ITERS / (ms_gap * 1e-3) / 1e9
+                                                  / peak)}
         if cpu_v is not None:
             line["cpu_baseline"] = dict({"value": cpu_v, "unit": "iter/s", "cores": cpu_threads,
                                          "kind": "port", "sample": cpu_note}, **host_info())
@@ -633,6 +653,8 @@ def run_kernel(args):
         return run_cnn(args)
     if args.kernel == "cassi":
         return run_cassi(args)
+    if args.kernel == "batch":
+        return run_batch(args)
     dev = _dev.device()
     F = args.frames
     orig, mask, meas = sci.datasets.video_config(H, W, F, noise_rel=0.01)
@@ -660,7 +682,34 @@ def run_kernel(args):
              y.data_ptr(), op.phisum.data_ptr(), out.data_ptr(), None, 1.0, 0.01, F, H, W,
              s.cuda_stream)
 
-    fn = {"tv": tv_once, "proj": proj_once, "proj_admm": proj_admm_once}[args.kernel]
+    cmap = torch.empty_like(y)
+
+    def resid_once():
+        call("sci_gap_residual", x.data_ptr(), None, op.bits.data_ptr(), y.data_ptr(),
+             y1.data_ptr(), op.phisum.data_ptr(), cmap.data_ptr(), 1, F, H, W, s.cuda_stream)
+
+    gap = None
+    if args.kernel == "gap":
+        # whole solves (residual pass, TV pass with the projection applied
+        # on load, stop test), 60 iterations, annealed weight
+        weights = np.array([0.2 * 0.25 ** (k / (ITERS - 1)) for k in range(ITERS)], np.float32)
+        gap = sci.Solver(op, "gap", ITERS, 1.0, weights, TV_ITERS, accelerate=True,
+                         use_graph=False)
+    sums = torch.zeros((2, F), dtype=torch.float64, device=dev)
+    if args.kernel == "metrics":
+        out.copy_(x * 0.9)
+
+    def metrics_once():
+        call("sci_frame_metrics", x.data_ptr(), out.data_ptr(), F, H, W, 1.0,
+             sums[0].data_ptr(), sums[1].data_ptr(), s.cuda_stream)
+
+    wsm = (sci.tv.tv_matlab_workspace(7, F, H, W, 5, dev) if args.kernel == "itv3d" else None)
+
+    def itv3d_once():  # tvdenoise_cham_ITV3D, gapdenoise.m's 5 iterations
+        sci.tv_matlab_frames(x, 7, 1.0 / 0.07, 5, u=out, workspace=wsm)
+
+    fn = {"tv": tv_once, "proj": proj_once, "proj_admm": proj_admm_once, "resid": resid_once,
+          "gap": (lambda: gap.run(y)), "metrics": metrics_once, "itv3d": itv3d_once}[args.kernel]
     fn()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -671,6 +720,36 @@ def run_kernel(args):
     torch.cuda.synchronize()
     print(json.dumps({"kernel": args.kernel, "frames": F, "H": H, "W": W,
                       "ms_per_launch": e0.elapsed_time(e1) / args.launches}))
+
+
+def run_batch(args):
+    """Profiling mode for the batched solve: ``--launches`` solves of the
+    first ``--frames`` items of the 64-item uneven batch (50 iterations,
+    autotuned), one persistent work-queue launch each."""
+    import torch
+    import sci_algorithms_gb300 as sci
+    meas, masks, elems = [], [], 0
+    for i, (orig, mask, y) in enumerate(sci.datasets.batch_config(64, seed=0)):
+        if i >= args.frames:
+            break
+        meas.append(y)
+        masks.append(mask)
+        elems += mask.size
+        del orig
+    bs = sci.BatchSolver(meas, masks, iters=50, tv_weight=0.1, autotune=True, use_graph=False)
+    bs.run()
+    torch.cuda.synchronize()
+    s = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(s)
+    for _ in range(args.launches):
+        bs.run()
+    e1.record(s)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / args.launches
+    print(json.dumps({"kernel": "batch", "items": len(meas), "elements": elems,
+                      "ms_per_solve": ms, "element_iters_per_s": elems * 50 / (ms * 1e-3),
+                      "iters_per_launch": bs.iters_per_launch or 50}))
 
 
 def run_cassi(args):
@@ -822,7 +901,10 @@ def side_workloads(dev):
     out["batched"] = {"workload": "batch64_uneven_128-1024_B8-32", "items": 64, "iters": 50,
                       "elements": elems, "ms_per_batch": ms_b,
                       "element_iters_per_s": elems * 50 / (ms_b * 1e-3),
-                      "chunk_rows": sorted(set(bsol.chunk_rows()))}
+                      "form": "persistent work-queue launches",
+                      "iters_per_launch": bsol.iters_per_launch or 50,
+                      "chunk_rows": sorted(set(bsol.chunk_rows())),
+                      "columns_per_lane": sorted(set(bsol.columns_per_lane()))}
     del bsol, meas
 
     # the MATLAB twin's TV denoisers (gapdenoise.m tvm switch, its
@@ -936,7 +1018,8 @@ def main():
                     help="skip the per-configuration comparison with the float64 oracle")
     ap.add_argument("--parity-size", type=int, default=H,
                     help="H = W of the 60-iteration video parity solves (2048: the timed workload)")
-    ap.add_argument("--kernel", choices=["tv", "proj", "proj_admm", "unrolled", "cnn", "cassi"],
+    ap.add_argument("--kernel", choices=["tv", "proj", "proj_admm", "resid", "gap", "metrics",
+                                         "itv3d", "batch", "unrolled", "cnn", "cassi"],
                     default=None,
                     help="profiling mode: time one kernel on a 2048x2048xFRAMES stack")
     ap.add_argument("--frames", type=int, default=8)

@@ -44,9 +44,11 @@ int sci_last_error(char *buf, size_t n);
 
 /* Reads the device status word into *status and, with clear != 0, resets
  * it.  Bit 0 is set when a bounded device-side wait of a bulk-copy kernel
- * (the GAP projection of sci_proj_gap with a packed mask) gave up; the
- * results of such a launch are not valid.  Synchronous.  No counterpart in
- * the reference (library plumbing). */
+ * (the GAP projection of sci_proj_gap with a packed mask, the batched and
+ * convolution kernels) gave up; bit 1 when a wait of the batched solve's
+ * work queue (sci_batch_gap_tv) gave up.  The results of such a launch are
+ * not valid.  Synchronous.  No counterpart in the reference (library
+ * plumbing). */
 int sci_device_status(unsigned int *status, int clear);
 
 /* Exercises the error path of the bounded device-side waits: one block
@@ -210,6 +212,12 @@ typedef struct sci_solve_opts {
                               * stop test eps); SCI_TVM_*: that MATLAB
                               * denoiser with tv_iter_max iterations and
                               * weights as gapdenoise.m's tvweight           */
+    double *resid_norm;      /* nullable device double[iters]: ||r_k||^2 of
+                              * iteration k's projection residual, summed in
+                              * FP64 by the projection kernel: r = (y1 - A x)
+                              * / Phi_sum for GAP_acc, (y - A x) / Phi_sum for
+                              * GAP (pnp_sci_algo.py:640-645), (y - A(theta +
+                              * b)) / (Phi_sum + gamma) for ADMM (:808-809)  */
 } sci_solve_opts;
 
 /* Workspace bytes for sci_gap_tv / sci_admm_tv. */
@@ -278,27 +286,47 @@ typedef struct sci_batch_item {
     float lambda;
     float tv_weight;
     int R;
+    int cpl;  /* TV columns per lane, 2 or 4 (0: 4; sci_batch_autotune fills it) */
 } sci_batch_item;
 
 int sci_batch_workspace_bytes(const sci_batch_item *items, int n, int tv_iter_max,
                               size_t *bytes);
 
-/* Times the TV pass of each distinct (B, H, W) for a set of row-chunk
- * heights on the item's own data and writes the fastest into items[i].R
- * (cached per process).  Synchronises the stream. */
-int sci_batch_autotune(sci_batch_item *items, int n, int tv_iter_max,
+/* Autotuner of the batched solve.  (1) Per distinct (B, H, W), times the TV
+ * pass on the item's own data for each column width (2 or 4 columns per
+ * lane) and row-chunk height and writes the fastest into items[i].cpl and
+ * items[i].R (cached per process).  (2) With a non-null iters_per_launch,
+ * times a few iterations of the whole batch for several iterations per
+ * persistent launch and writes the fastest (0: all in one launch); this
+ * solves the batch from x0 = At(y / phisum), overwriting every item's x.
+ * Synchronises the stream. */
+int sci_batch_autotune(sci_batch_item *items, int n, int iters, int tv_iter_max,
+                       float eps, int accelerate, int *iters_per_launch,
                        void *workspace, size_t workspace_bytes, void *stream);
 
 /* GAP-TV (pnp_sci_algo.py:536-706, denoiser='tv') of n <= 256 independent
- * measurements: `iters` iterations, all items advancing together; each
- * phase is one launch over the tiles of every item, and with use_graph the
- * whole loop is captured once into a cached CUDA graph.  init_x0: start
- * from At(y / phisum) (else from x).  tv_iter_max in [2, 5].  The item
- * table is uploaded synchronously before the work is enqueued. */
+ * measurements, all items advancing together: persistent launches over a
+ * device work queue, each running iters_per_launch iterations (0: all) of
+ * every item -- per iteration the projection tiles, TV work items and stop
+ * tests of all items, a task waiting (bounded) only for earlier tasks of
+ * its own item.  With use_graph the whole loop is captured once into a
+ * cached CUDA graph.  init_x0: start from At(y / phisum) (else from x).
+ * tv_iter_max in [2, 5].  The item table is uploaded synchronously before
+ * the work is enqueued.  A wait that gave up sets bit 1 of the device
+ * status (sci_device_status). */
 int sci_batch_gap_tv(const sci_batch_item *items, int n, int iters,
                      int tv_iter_max, float eps, int accelerate, int init_x0,
-                     int use_graph, void *workspace, size_t workspace_bytes,
-                     void *stream);
+                     int use_graph, int iters_per_launch, void *workspace,
+                     size_t workspace_bytes, void *stream);
+
+/* Exercises the give-up path of the work queue's bounded waits: one warp
+ * waits, `polls` times at most (1 .. 2^20), for a task count that nothing
+ * raises, then raises the queue's abort flag, which sets bit 1 of the
+ * device status word.  workspace: any device buffer of at least 4 KB (the
+ * queue's counters are placed there).  For tests of that path; the context
+ * stays usable.  No counterpart in the reference. */
+int sci_batch_selftest_queue_wait(unsigned int polls, void *workspace,
+                                  size_t workspace_bytes, void *stream);
 
 /* ------------------------------- differentiable unrolled GAP-TV (K4) */
 /* A batch of N scenes x_true (N x B x H x W) sharing one learnable mask

@@ -139,16 +139,21 @@ def _denoise(x, denoiser, w, eps, tv_iter_max, multichannel, nsig, model, thread
 
 def gap_iteration(y, y1, x, Phi_sum, A, At, lam, w, accelerate=True, denoiser='tv',
                   eps=2.e-4, tv_iter_max=5, multichannel=True, nsig=None, model=None,
-                  threads=1):
+                  threads=1, resid=None):
     """One iteration of ``gap_denoise``'s loop (``pnp_sci_algo.py:639-650``):
     the GAP (``:645``) or accelerated GAP (``:641-643``) projection, then the
-    denoiser (its frames on ``threads`` threads).  Returns the new (x, y1)."""
+    denoiser (its frames on ``threads`` threads).  Returns the new (x, y1).
+    ``resid`` (a list) receives ||r||^2 of the projection's residual map
+    r = (y1 - yb) / Phi_sum (or (y - yb) / Phi_sum), in float64."""
     yb = A(x)
     if accelerate:
         y1 = y1 + (y - yb)
-        x = x + lam * (At((y1 - yb) / Phi_sum))
+        r = (y1 - yb) / Phi_sum
     else:
-        x = x + lam * (At((y - yb) / Phi_sum))
+        r = (y - yb) / Phi_sum
+    x = x + lam * (At(r))
+    if resid is not None:
+        resid.append(float(np.sum(np.asarray(r, np.float64) ** 2)))
     x = _denoise(x, denoiser, w, eps, tv_iter_max, multichannel, nsig, model, threads)
     return x, y1
 
@@ -157,7 +162,7 @@ def gap_denoise(y, Phi_sum, A, At, _lambda=1, accelerate=True,
                 denoiser='tv', iter_max=50, noise_estimate=False, sigma=None,
                 tv_weight=0.1, tv_iter_max=5, multichannel=True, x0=None,
                 X_orig=None, model=None, show_iqa=True, tvm='tv_chambolle',
-                eps=2.e-4, verbose=False):
+                eps=2.e-4, verbose=False, resid=None):
     """``PnP_SCI/python/pnp_sci_algo.py:536-706``.
 
     GAP (``:645``) or accelerated GAP (``:641-643``) projection, then the
@@ -181,7 +186,7 @@ def gap_denoise(y, Phi_sum, A, At, _lambda=1, accelerate=True,
         for it in range(iter_max[idx]):
             x, y1 = gap_iteration(y, y1, x, Phi_sum, A, At, _at(_lambda, k), _at(tv_weight, k),
                                   accelerate, denoiser, eps, tv_iter_max, multichannel, nsig,
-                                  model)
+                                  model, resid=resid)
             if show_iqa and X_orig is not None:
                 psnr_all.append(psnr(X_orig, x))
                 if verbose and (k + 1) % 5 == 0:
@@ -202,13 +207,14 @@ def admm_denoise(y, Phi_sum, A, At, _lambda=1, gamma=0.01,
                  denoiser='tv', iter_max=50, noise_estimate=False, sigma=None,
                  tv_weight=0.1, tv_iter_max=5, multichannel=True, x0=None,
                  model=None, X_orig=None, show_iqa=True, eps=2.e-4,
-                 verbose=False):
+                 verbose=False, resid=None):
     """``PnP_SCI/python/pnp_sci_algo.py:708-864``.
 
     yb = A(theta + b); x = theta + b + lambda At((y - yb)/(Phi_sum + gamma))
     (``:808-809``); theta = TV(x - b) (``:812-813``) or the CNN of
     ``oracle.cnn`` (``:822-825``); b = b - (x - theta) (``:836``).
-    Returns x, not theta (``:864``).
+    Returns x, not theta (``:864``).  ``resid`` (a list) receives ||r||^2 of
+    every iteration's residual map r = (y - yb) / (Phi_sum + gamma).
     """
     _check_denoiser(denoiser, 'tv_chambolle')
     if x0 is None:
@@ -227,7 +233,10 @@ def admm_denoise(y, Phi_sum, A, At, _lambda=1, gamma=0.01,
             lam = _at(_lambda, k)
             w = _at(tv_weight, k)
             yb = A(theta + b)
-            x = (theta + b) + lam * (At((y - yb) / (Phi_sum + gamma)))
+            r = (y - yb) / (Phi_sum + gamma)
+            x = (theta + b) + lam * (At(r))
+            if resid is not None:
+                resid.append(float(np.sum(np.asarray(r, np.float64) ** 2)))
             theta = _denoise(x - b, denoiser, w, eps, tv_iter_max, multichannel, nsig, model)
             b = b - (x - theta)
             if show_iqa and X_orig is not None:

@@ -40,14 +40,15 @@ class SolveOpts(ctypes.Structure):
                 ("sqerr", c_vp),
                 ("tv_steps", c_vp),
                 ("use_graph", ctypes.c_int),
-                ("tvm", ctypes.c_int)]
+                ("tvm", ctypes.c_int),
+                ("resid_norm", c_vp)]
 
 
 class BatchItem(ctypes.Structure):
     """``sci_batch_item`` of include/sci_gb300.h."""
     _fields_ = [("y", c_vp), ("mask_bits", c_vp), ("phisum", c_vp), ("x", c_vp),
                 ("B", c_i64), ("H", c_i64), ("W", c_i64), ("lam", c_f), ("tv_weight", c_f),
-                ("R", ctypes.c_int)]
+                ("R", ctypes.c_int), ("cpl", ctypes.c_int)]
 
 
 # name -> argtypes (all functions return int status)
@@ -92,10 +93,12 @@ _SIGS = {
                          ctypes.POINTER(SolveOpts), c_vp, c_sz, c_vp],
     "sci_batch_workspace_bytes": [ctypes.POINTER(BatchItem), ctypes.c_int, ctypes.c_int,
                                   ctypes.POINTER(c_sz)],
-    "sci_batch_autotune": [ctypes.POINTER(BatchItem), ctypes.c_int, ctypes.c_int, c_vp, c_sz,
-                           c_vp],
+    "sci_batch_autotune": [ctypes.POINTER(BatchItem), ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                           c_f, ctypes.c_int, ctypes.POINTER(ctypes.c_int), c_vp, c_sz, c_vp],
+    "sci_batch_selftest_queue_wait": [ctypes.c_uint, c_vp, c_sz, c_vp],
     "sci_batch_gap_tv": [ctypes.POINTER(BatchItem), ctypes.c_int, ctypes.c_int, ctypes.c_int,
-                         c_f, ctypes.c_int, ctypes.c_int, ctypes.c_int, c_vp, c_sz, c_vp],
+                         c_f, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, c_vp, c_sz,
+                         c_vp],
     "sci_cnn_ffdnet_pack": [c_vp, c_i64, c_i64, c_i64, c_vp, c_vp, ctypes.c_int, c_vp],
     "sci_cnn_ffdnet_unpack_sub": [c_vp, c_vp, c_i64, c_i64, c_i64, ctypes.c_int, ctypes.c_int,
                                   ctypes.c_int, c_vp, c_vp],

@@ -2,12 +2,15 @@
 
 ``BatchSolver`` builds one device item table for a list of measurements
 (each with its own binary mask, packed to one word per pixel) and calls
-``sci_batch_gap_tv``: every phase of an iteration is one launch over the
-tiles of all items, and the whole loop is captured once into a CUDA graph.
-``autotune=True`` lets ``sci_batch_autotune`` pick each shape's TV row-chunk
-height by timing it on the item's data.  Each item's result equals a
-single-measurement ``gap_denoise`` (``PnP_SCI/python/pnp_sci_algo.py:536``)
-with x0 = At(y / Phi_sum).
+``sci_batch_gap_tv``: persistent launches over a device work queue run the
+projection tiles, TV work items and stop tests of every item, each task
+waiting only for earlier tasks of its own item, and the whole loop is
+captured once into a CUDA graph.  ``autotune=True`` lets
+``sci_batch_autotune`` pick each shape's TV column width and row-chunk
+height, and the iterations per persistent launch, by timing them on the
+items' data.  Each item's result equals a single-measurement
+``gap_denoise`` (``PnP_SCI/python/pnp_sci_algo.py:536``) with
+x0 = At(y / Phi_sum).
 """
 import ctypes
 
@@ -42,22 +45,30 @@ class BatchSolver:
             it.y, it.mask_bits, it.phisum, it.x = (yd.data_ptr(), op.bits.data_ptr(),
                                                    op.phisum.data_ptr(), x.data_ptr())
             it.B, it.H, it.W = op.B, op.H, op.W
-            it.lam, it.tv_weight, it.R = float(lam), float(tv_weight), 0
+            it.lam, it.tv_weight, it.R, it.cpl = float(lam), float(tv_weight), 0, 0
         nb = ctypes.c_size_t()
         call("sci_batch_workspace_bytes", self.items, n, self.K, ctypes.byref(nb))
         self.ws = _dev.workspace(nb.value, self.dev)
+        # iterations per persistent launch of the work queue (0: all)
+        self.iters_per_launch = 0
         if autotune:
             self._call(0, 1, graph=False)  # x = x0, a realistic input to time on
-            call("sci_batch_autotune", self.items, n, self.K, self.ws.data_ptr(), self.ws.numel(),
+            ipl = ctypes.c_int(0)
+            call("sci_batch_autotune", self.items, n, self.iters, self.K, self.eps,
+                 self.accelerate, ctypes.byref(ipl), self.ws.data_ptr(), self.ws.numel(),
                  _dev.stream_handle())
+            self.iters_per_launch = ipl.value
 
     def _call(self, iters, init_x0, graph):
         call("sci_batch_gap_tv", self.items, len(self.xs), iters, self.K, self.eps,
-             self.accelerate, init_x0, int(graph), self.ws.data_ptr(), self.ws.numel(),
-             _dev.stream_handle())
+             self.accelerate, init_x0, int(graph), int(self.iters_per_launch),
+             self.ws.data_ptr(), self.ws.numel(), _dev.stream_handle())
 
     def chunk_rows(self):
         return [self.items[i].R for i in range(len(self.xs))]
+
+    def columns_per_lane(self):
+        return [self.items[i].cpl or 4 for i in range(len(self.xs))]
 
     def run(self, x0=None):
         """Solve all items; returns the list of (B, H, W) results (device

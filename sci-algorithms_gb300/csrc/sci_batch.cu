@@ -22,6 +22,7 @@
 
 #include "sci_bulk.cuh"
 #include "sci_graph.cuh"
+#include "sci_batch.cuh"
 #include "sci_tv.cuh"
 
 namespace sci {
@@ -32,40 +33,12 @@ __device__ unsigned int g_batch_status;
 int tv_launch(const float *f, float *u, float *resid, int64_t nf, int64_t H, int64_t W,
               int64_t fs, float weight, float eps, int K, int *steps, double *energy_out,
               void *workspace, size_t ws_bytes, cudaStream_t s, int force_R);
+int tv_launch_flags(const float *f, float *u, float *resid, int64_t nf, int64_t H, int64_t W,
+                    int64_t fs, float weight, float eps, int K, int *steps, double *energy_out,
+                    void *workspace, size_t ws_bytes, cudaStream_t s, int force_R, int flags);
 size_t tv_workspace_bytes(int64_t nf, int64_t H, int64_t W, int K);
 
 namespace batch {
-
-constexpr int MAXI = 256;  // items per batch
-constexpr int PROJ_T = 256;
-
-struct Item {
-    tv::Pass tv;  // f = xp (projected stack), u = x
-    const float *y;
-    const uint32_t *bits;
-    const float *phisum;
-    float *x, *xp, *y1;
-    int B;
-    int64_t hw;
-    float lam;
-};
-
-struct Table {
-    int n;
-    int proj_prefix[MAXI + 1];  // 256-pixel tiles
-    int tv_prefix[MAXI + 1];    // warp work items
-    Item it[MAXI];
-};
-
-__device__ __forceinline__ int find_item(const int *prefix, int n, int g) {
-    int lo = 0, hi = n;  // prefix[lo] <= g < prefix[hi]
-    while (hi - lo > 1) {
-        const int mid = (lo + hi) >> 1;
-        if (prefix[mid] <= g) lo = mid;
-        else hi = mid;
-    }
-    return lo;
-}
 
 // x0 = At(y / Phi_sum) for every item (the start point of the GAP loop).
 __global__ void __launch_bounds__(PROJ_T) k_batch_x0(const Table *__restrict__ T) {
@@ -222,8 +195,8 @@ __global__ void __launch_bounds__(tv::WPB * 32, 3) k_batch_tv(const Table *__res
 size_t r256(size_t b) { return (b + 255) & ~size_t(255); }
 
 struct Layout {
-    size_t table, xp, y1, energy, tvscratch, total;
-    std::vector<size_t> item_xp, item_y1, item_e;
+    size_t table, xp, y1, energy, stop, queue, tvscratch, total;
+    std::vector<size_t> item_xp, item_y1, item_e, item_e1, item_stop;
 };
 
 Layout layout(const sci_batch_item *items, int n, int K) {
@@ -238,12 +211,23 @@ Layout layout(const sci_batch_item *items, int n, int K) {
         L.item_y1.push_back(off);
         off += r256(4 * (size_t)hw);
     }
+    // per item the energy sums of even and odd iterations (the per-phase
+    // launches use the first), then its stop decisions and ticket
     L.energy = off;
     for (int i = 0; i < n; ++i) {
+        const size_t eb = r256(sizeof(double) * 2 * K * (size_t)items[i].B);
         L.item_e.push_back(off - L.energy);
-        off += r256(sizeof(double) * 2 * K * (size_t)items[i].B);
+        L.item_e1.push_back(off + eb - L.energy);
+        off += 2 * eb;
     }
     const size_t energy_end = off;
+    L.stop = off;
+    for (int i = 0; i < n; ++i) {
+        L.item_stop.push_back(off);
+        off += r256(sizeof(int) * (size_t)items[i].B + sizeof(unsigned));
+    }
+    L.queue = off;
+    off += r256(sizeof(Queue));
     L.tvscratch = off;
     size_t tvmax = 0;  // autotuning scratch: the largest single-item TV workspace
     for (int i = 0; i < n; ++i)
@@ -282,7 +266,7 @@ void build_table(const sci_batch_item *items, int n, int K, float eps, char *ws,
                  Table &T) {
     memset(&T, 0, sizeof(T));
     T.n = n;
-    T.proj_prefix[0] = T.tv_prefix[0] = 0;
+    T.proj_prefix[0] = T.tv_prefix[0] = T.qp_prefix[0] = T.tq_prefix[0] = 0;
     for (int i = 0; i < n; ++i) {
         const sci_batch_item &s = items[i];
         Item &I = T.it[i];
@@ -321,12 +305,60 @@ void build_table(const sci_batch_item *items, int n, int K, float eps, char *ws,
         P.lag = 1;
         P.frame_fast = 1;
         T.proj_prefix[i + 1] = T.proj_prefix[i] + (int)((I.hw + PROJ_T - 1) / PROJ_T);
+        T.qp_prefix[i + 1] = T.qp_prefix[i] + (int)((I.hw + QP_T - 1) / QP_T);
+        // the work-queue passes: the lean pipeline with the item's column
+        // width, energies of even / odd iterations, stop decisions by ticket
+        for (int par = 0; par < 2; ++par) {
+            tv::Pass &Q = I.tvq[par];
+            Q = P;
+            const int cpl = s.cpl == 2 ? 2 : 4;
+            const int ru = (P.S + cpl - 1) / cpl * cpl;
+            Q.cpl = cpl;
+            Q.hl = ru;
+            Q.own = 32 * cpl - 2 * ru;
+            Q.nbands = (int)((s.W + Q.own - 1) / Q.own);
+            Q.energy = reinterpret_cast<double *>(ws + L.energy +
+                                                  (par ? L.item_e1[i] : L.item_e[i]));
+            Q.stopj = reinterpret_cast<int *>(ws + L.item_stop[i]);
+            Q.ticket = reinterpret_cast<unsigned *>(ws + L.item_stop[i] + sizeof(int) * s.B);
+        }
         T.tv_prefix[i + 1] = T.tv_prefix[i] + P.nbands * P.nchunks * P.nf;
+        // both parities have the same geometry
+        T.tq_prefix[i + 1] =
+            T.tq_prefix[i] + I.tvq[0].nbands * I.tvq[0].nchunks * I.tvq[0].nf;
     }
 }
 
+// bit 1 of the batch status: a bounded wait of a work-queue launch gave up
+__global__ void k_batch_fold(const Queue *Q) {
+    if (threadIdx.x == 0 && Q->abort) atomicOr(&g_batch_status, 2u);
+}
+
+// The give-up path of the work queue's bounded waits, on purpose: one warp
+// waits at most `polls` polls for a count that nothing raises, then raises
+// the abort flag, which the fold turns into status bit 1.
+__global__ void k_queue_wait_selftest(Queue *Q, unsigned polls) {
+    wait_count(Q, &Q->done[0][0], 1u, threadIdx.x & 31, polls);
+}
+
+int queue_selftest(unsigned polls, Queue *dQ, cudaStream_t s) {
+    SCI_CUDA(cudaMemsetAsync(dQ, 0, sizeof(Queue), s));
+    k_queue_wait_selftest<<<1, 32, 0, s>>>(dQ, polls);
+    SCI_LAUNCHED("k_queue_wait_selftest");
+    k_batch_fold<<<1, 32, 0, s>>>(dQ);
+    SCI_LAUNCHED("k_batch_fold");
+    return SCI_OK;
+}
+
+// The work-queue form (sci_batch_queue.cu) unless SCI_BATCH_QUEUE=0.
+bool queue_enabled() {
+    const char *e = getenv("SCI_BATCH_QUEUE");
+    return !(e && atoi(e) == 0);
+}
+
+// per_launch: iterations per persistent launch of the work queue (0: all).
 int enqueue(const Table &T, Table *dT, const Layout &L, char *ws, int n, int iters, int K,
-            int accelerate, int init_x0, cudaStream_t s) {
+            int accelerate, int init_x0, int per_launch, cudaStream_t s) {
     const int pb = T.proj_prefix[n], tb = (T.tv_prefix[n] + tv::WPB - 1) / tv::WPB;
     if (init_x0) {
         k_batch_x0<<<pb, PROJ_T, 0, s>>>(dT);
@@ -334,6 +366,20 @@ int enqueue(const Table &T, Table *dT, const Layout &L, char *ws, int n, int ite
     }
     for (int i = 0; i < n; ++i)
         if (accelerate) SCI_CUDA(cudaMemsetAsync(T.it[i].y1, 0, 4 * T.it[i].hw, s));
+    if (queue_enabled()) {
+        Queue *dQ = reinterpret_cast<Queue *>(ws + L.queue);
+        const int m = per_launch > 0 ? per_launch : std::max(1, iters);
+        const int blocks = queue_blocks();
+        for (int k0 = 0; k0 < iters; k0 += m) {
+            SCI_CUDA(cudaMemsetAsync(dQ, 0, sizeof(Queue), s));
+            if (int e = queue_launch(dT, dQ, k0, std::min(iters, k0 + m), accelerate != 0, K - 1,
+                                     blocks, s))
+                return e;
+            k_batch_fold<<<1, 32, 0, s>>>(dQ);
+            SCI_LAUNCHED("k_batch_fold");
+        }
+        return SCI_OK;
+    }
     const size_t ebytes = L.tvscratch - L.energy;
     // bulk-copy projection unless a mask is not 16-byte aligned (the other
     // planes are checked by check(); SCI_PROJ_TMA=0 selects the plain kernel)
@@ -365,6 +411,42 @@ int enqueue(const Table &T, Table *dT, const Layout &L, char *ws, int n, int ite
     return SCI_OK;
 }
 
+// The whole solve of a batch (table upload, then the loop, captured once
+// into a cached CUDA graph when use_graph).
+int solve(const sci_batch_item *items, int n, int iters, int tv_iter_max, float eps,
+                 int accelerate, int init_x0, int use_graph, int per_launch, void *workspace,
+                 size_t workspace_bytes, cudaStream_t s) {
+    const Layout L = layout(items, n, tv_iter_max);
+    SCI_CHECK_ARG(workspace && workspace_bytes >= L.total,
+                  "batch: workspace of %zu bytes needed, got %zu", L.total, workspace_bytes);
+    char *ws = static_cast<char *>(workspace);
+    Table *hT = new Table;
+    build_table(items, n, tv_iter_max, eps, ws, L, *hT);
+    Table *dT = reinterpret_cast<Table *>(ws + L.table);
+    // the table is small; a stream-ordered copy from this host struct needs
+    // it to stay alive until the copy ran, so the copy is synchronous here
+    cudaError_t ce = cudaStreamSynchronize(s);
+    if (ce == cudaSuccess) ce = cudaMemcpy(dT, hT, sizeof(Table), cudaMemcpyHostToDevice);
+    if (ce != cudaSuccess) {
+        delete hT;
+        return cuda_status(ce, "batch table upload");
+    }
+    int rc = SCI_OK;
+    if (!use_graph) {
+        rc = enqueue(*hT, dT, L, ws, n, iters, tv_iter_max, accelerate, init_x0, per_launch, s);
+        delete hT;
+        return rc;
+    }
+    std::string key(reinterpret_cast<const char *>(hT), sizeof(Table));
+    key_append(key, iters, accelerate, init_x0, per_launch);
+    rc = run_graph("batch graph capture", key, s, [&](cudaStream_t cs) {
+        return enqueue(*hT, dT, L, ws, n, iters, tv_iter_max, accelerate, init_x0, per_launch,
+                       cs);
+    });
+    delete hT;
+    return rc;
+}
+
 }  // namespace batch
 }  // namespace sci
 
@@ -381,20 +463,36 @@ int sci_batch_workspace_bytes(const sci_batch_item *items, int n, int tv_iter_ma
     return SCI_OK;
 }
 
-int sci_batch_autotune(sci_batch_item *items, int n, int tv_iter_max, void *workspace,
+int sci_batch_autotune(sci_batch_item *items, int n, int iters, int tv_iter_max, float eps,
+                       int accelerate, int *iters_per_launch, void *workspace,
                        size_t workspace_bytes, void *stream) {
     if (int e = check(items, n, tv_iter_max)) return e;
     const Layout L = layout(items, n, tv_iter_max);
     SCI_CHECK_ARG(workspace && workspace_bytes >= L.total, "batch: workspace too small");
+    SCI_CHECK_ARG(iters >= 0, "batch: iters must be >= 0");
     char *ws = static_cast<char *>(workspace);
     cudaStream_t s = as_stream(stream);
-    // one timing per distinct (B, H, W): the TV pass of the item's own x
-    // into its projection buffer, for each candidate chunk height
+    // 1. per distinct (B, H, W): the TV pass of the item's own x into its
+    // projection buffer, for each column width (2 or 4 per lane) and row
+    // chunk height; the fastest pair is cached per process
     static std::mutex mu;
-    static std::map<std::tuple<int64_t, int64_t, int64_t, int>, int> tuned;
+    static std::map<std::tuple<int64_t, int64_t, int64_t, int>, std::pair<int, int>> tuned;
     cudaEvent_t e0, e1;
     SCI_CUDA(cudaEventCreate(&e0));
     SCI_CUDA(cudaEventCreate(&e1));
+    auto timed = [&](auto &&fn, int reps) -> float {  // the first run warms up
+        float ms = 0.f;
+        for (int rep = 0; rep <= reps; ++rep) {
+            cudaEventRecord(e0, s);
+            if (fn() != SCI_OK) return -1.f;
+            cudaEventRecord(e1, s);
+            cudaEventSynchronize(e1);
+            float t = 0.f;
+            cudaEventElapsedTime(&t, e0, e1);
+            if (rep > 0) ms += t;
+        }
+        return ms;
+    };
     int rc = SCI_OK;
     for (int i = 0; i < n && rc == SCI_OK; ++i) {
         sci_batch_item &it = items[i];
@@ -403,74 +501,89 @@ int sci_batch_autotune(sci_batch_item *items, int n, int tv_iter_max, void *work
             std::lock_guard<std::mutex> lk(mu);
             auto f = tuned.find(key);
             if (f != tuned.end()) {
-                it.R = f->second;
+                it.R = f->second.first;
+                it.cpl = f->second.second;
                 continue;
             }
         }
         float best = 1e30f;
-        int bestR = default_R(it.H, it.W, it.B);
-        for (int R : {32, 64, 128, 256, 512}) {
-            if (R > 2 * it.H && R != 32) break;
-            float ms = 0.f;
-            for (int rep = 0; rep < 3 && rc == SCI_OK; ++rep) {
-                cudaEventRecord(e0, s);
-                rc = tv_launch(it.x, reinterpret_cast<float *>(ws + L.item_xp[i]), nullptr, it.B,
-                               it.H, it.W, it.H * it.W, it.tv_weight, 2e-4f, tv_iter_max, nullptr,
-                               nullptr, ws + L.tvscratch, L.total - L.tvscratch, s, R);
-                cudaEventRecord(e1, s);
-                cudaEventSynchronize(e1);
-                float t = 0.f;
-                cudaEventElapsedTime(&t, e0, e1);
-                if (rep > 0) ms += t;  // the first run warms up
-            }
-            if (rc == SCI_OK && ms < best) {
-                best = ms;
-                bestR = R;
+        int bestR = default_R(it.H, it.W, it.B), bestC = 4;
+        for (int cpl : {4, 2}) {
+            for (int R : {16, 32, 64, 128, 256, 512}) {
+                if (R > 2 * it.H && R != 16) break;
+                const float ms = timed(
+                    [&] {
+                        return tv_launch_flags(it.x, reinterpret_cast<float *>(ws + L.item_xp[i]),
+                                               nullptr, it.B, it.H, it.W, it.H * it.W,
+                                               it.tv_weight, eps, tv_iter_max, nullptr, nullptr,
+                                               ws + L.tvscratch, L.total - L.tvscratch, s, R,
+                                               cpl << 8);
+                    },
+                    2);
+                if (ms < 0.f) {
+                    rc = SCI_ERR_CUDA;
+                    break;
+                }
+                if (ms < best) {
+                    best = ms;
+                    bestR = R;
+                    bestC = cpl;
+                }
             }
         }
         it.R = bestR;
+        it.cpl = bestC;
         std::lock_guard<std::mutex> lk(mu);
-        tuned[key] = bestR;
+        tuned[key] = std::make_pair(bestR, bestC);
+    }
+    // 2. iterations per persistent launch of the work queue: the batch's own
+    // solve (from x0 = At(y / Phi_sum), overwriting every item's x) of a few
+    // iterations for each candidate
+    if (rc == SCI_OK && iters_per_launch) {
+        const int probe = std::max(1, std::min(iters, 6));
+        float best = 1e30f;
+        int bestM = 0;
+        for (int m : {0, 1, 2, 3}) {
+            if (m >= probe) continue;
+            const float ms = timed(
+                [&] {
+                    return solve(items, n, probe, tv_iter_max, eps, accelerate, 1, 0, m, ws,
+                                 workspace_bytes, s);
+                },
+                2);
+            if (ms < 0.f) {
+                rc = SCI_ERR_CUDA;
+                break;
+            }
+            if (ms < best) {
+                best = ms;
+                bestM = m;
+            }
+        }
+        // a launch of all `probe` iterations stands for one of all iterations
+        *iters_per_launch = bestM;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     return rc;
 }
 
+int sci_batch_selftest_queue_wait(unsigned int polls, void *workspace, size_t workspace_bytes,
+                                  void *stream) {
+    SCI_CHECK_ARG(polls >= 1 && polls <= (1u << 20), "selftest: polls in [1, 2^20]");
+    SCI_CHECK_ARG(workspace && workspace_bytes >= sizeof(Queue),
+                  "selftest: a workspace of %zu bytes is needed", sizeof(Queue));
+    return queue_selftest(polls, static_cast<Queue *>(workspace), as_stream(stream));
+}
+
 int sci_batch_gap_tv(const sci_batch_item *items, int n, int iters, int tv_iter_max, float eps,
-                     int accelerate, int init_x0, int use_graph, void *workspace,
-                     size_t workspace_bytes, void *stream) {
+                     int accelerate, int init_x0, int use_graph, int iters_per_launch,
+                     void *workspace, size_t workspace_bytes, void *stream) {
     if (int e = check(items, n, tv_iter_max)) return e;
     SCI_CHECK_ARG(iters >= 0, "batch: iters must be >= 0");
-    const Layout L = layout(items, n, tv_iter_max);
-    SCI_CHECK_ARG(workspace && workspace_bytes >= L.total,
-                  "batch: workspace of %zu bytes needed, got %zu", L.total, workspace_bytes);
-    char *ws = static_cast<char *>(workspace);
-    cudaStream_t s = as_stream(stream);
-    Table *hT = new Table;
-    build_table(items, n, tv_iter_max, eps, ws, L, *hT);
-    Table *dT = reinterpret_cast<Table *>(ws + L.table);
-    // the table is tiny; a stream-ordered copy from this host struct needs
-    // it to stay alive until the copy ran, so the copy is synchronous here
-    cudaError_t ce = cudaStreamSynchronize(s);
-    if (ce == cudaSuccess) ce = cudaMemcpy(dT, hT, sizeof(Table), cudaMemcpyHostToDevice);
-    if (ce != cudaSuccess) {
-        delete hT;
-        return cuda_status(ce, "batch table upload");
-    }
-    int rc = SCI_OK;
-    if (!use_graph) {
-        rc = enqueue(*hT, dT, L, ws, n, iters, tv_iter_max, accelerate, init_x0, s);
-        delete hT;
-        return rc;
-    }
-    std::string key(reinterpret_cast<const char *>(hT), sizeof(Table));
-    key_append(key, iters, accelerate, init_x0);
-    rc = run_graph("batch graph capture", key, s, [&](cudaStream_t cs) {
-        return enqueue(*hT, dT, L, ws, n, iters, tv_iter_max, accelerate, init_x0, cs);
-    });
-    delete hT;
-    return rc;
+    SCI_CHECK_ARG(iters_per_launch >= 0, "batch: iters_per_launch must be >= 0");
+    return solve(items, n, iters, tv_iter_max, eps, accelerate, init_x0, use_graph,
+                 iters_per_launch, workspace, workspace_bytes, as_stream(stream));
 }
 
 }  // extern "C"

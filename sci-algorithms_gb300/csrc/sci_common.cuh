@@ -60,6 +60,44 @@ __device__ __forceinline__ float rcp_approx(float x) {
     return r;
 }
 
+// ---- FP64 sum of squares of a projection residual ----------------------
+// The projection kernels accumulate ||r||^2 of their residual map r (one
+// float per pixel) when given a non-null `rn`: the squares of a thread's
+// 4-pixel group are summed in FP32 and added to a per-thread FP64 partial;
+// rn_flush reduces the partials of the block (warp shuffles, shared memory)
+// and adds them to *rn with one FP64 atomic.  Every thread of the block
+// calls rn_flush (it synchronises the block).
+__device__ __forceinline__ void rn_add4(double &acc, float4 r) {
+    float q = r.x * r.x;
+    q = fmaf(r.y, r.y, q);
+    q = fmaf(r.z, r.z, q);
+    q = fmaf(r.w, r.w, q);
+    acc += (double)q;
+}
+__device__ __forceinline__ void rn_add1(double &acc, float r) { acc += (double)(r * r); }
+// Warp-level flush (one FP64 atomic per warp, no shared memory): for the
+// persistent bulk-copy kernels, whose blocks are one to four warps.
+__device__ __forceinline__ void rn_flush_warp(double acc, double *rn) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    if ((threadIdx.x & 31) == 0) atomicAdd(rn, acc);
+}
+__device__ __forceinline__ void rn_flush(double acc, double *rn) {
+    __shared__ double part[32];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+    const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+    if (lane == 0) part[w] = acc;
+    __syncthreads();
+    if (w == 0) {
+        const int nw = (int)((blockDim.x + 31) >> 5);
+        double v = lane < nw ? part[lane] : 0.0;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+        if (lane == 0) atomicAdd(rn, v);
+    }
+}
+
 // ---- packed FP32 pairs (sm_100+ f32x2 arithmetic) --------------------
 // A float2 is held as one 64-bit register pair; add/sub/mul/fma on both
 // halves issue as one instruction.

@@ -34,10 +34,10 @@ int cuda_status(cudaError_t e, const char *what) {
 
 int launch_proj_gap_tma(const float *x, const uint32_t *bits, const float *y, float *y1,
                         const float *phisum, float *xo, float lam, bool acc, int B, int64_t hw,
-                        cudaStream_t s);
+                        cudaStream_t s, double *rn);
 int launch_proj_admm_tma(const float *th, const float *bb, const uint32_t *bits, const float *y,
                          const float *phisum, float *v, float *xo, float lam, float gamma, int B,
-                         int64_t hw, cudaStream_t s, bool b_from_v = false);
+                         int64_t hw, cudaStream_t s, bool b_from_v, double *rn);
 
 // Grid for a grid-stride loop over `n` work units of one thread each.
 static inline dim3 grid_for(int64_t n, int threads) {
@@ -171,8 +171,9 @@ template <int MODE, bool ACC>
 __global__ void __launch_bounds__(256) k_proj_gap_vec(
     const float *__restrict__ x, Mask<MODE> M, const float *__restrict__ y,
     float *__restrict__ y1, const float *__restrict__ phisum, float *__restrict__ xo,
-    float lam, int B, int64_t hw) {
+    float lam, int B, int64_t hw, double *__restrict__ rn) {
     const int64_t n4 = hw >> 2;
+    double racc = 0.0;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n4;
          q += (int64_t)gridDim.x * blockDim.x) {
         const int64_t p = q << 2;
@@ -201,6 +202,7 @@ __global__ void __launch_bounds__(256) k_proj_gap_vec(
             r = make_float4(__fdiv_rn(yv.x - s.x, ps.x), __fdiv_rn(yv.y - s.y, ps.y),
                             __fdiv_rn(yv.z - s.z, ps.z), __fdiv_rn(yv.w - s.w, ps.w));
         }
+        if (rn) rn_add4(racc, r);
 #pragma unroll 4
         for (int b = 0; b < B; ++b) {
             const float4 a = ldg4(x + b * hw + p), m = M.at4(b, p, w);
@@ -209,13 +211,15 @@ __global__ void __launch_bounds__(256) k_proj_gap_vec(
                                fmaf(lam, r.z * m.z, a.z), fmaf(lam, r.w * m.w, a.w)));
         }
     }
+    if (rn) rn_flush(racc, rn);
 }
 
 template <int MODE, bool ACC>
 __global__ void k_proj_gap_scalar(const float *__restrict__ x, Mask<MODE> M,
                                   const float *__restrict__ y, float *__restrict__ y1,
                                   const float *__restrict__ phisum, float *__restrict__ xo,
-                                  float lam, int B, int64_t hw) {
+                                  float lam, int B, int64_t hw, double *__restrict__ rn) {
+    double racc = 0.0;
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < hw;
          p += (int64_t)gridDim.x * blockDim.x) {
         const uint32_t w = M.word1(p);
@@ -229,9 +233,11 @@ __global__ void k_proj_gap_scalar(const float *__restrict__ x, Mask<MODE> M,
         } else {
             r = __fdiv_rn(y[p] - s, phisum[p]);
         }
+        if (rn) rn_add1(racc, r);
         for (int b = 0; b < B; ++b)
             xo[b * hw + p] = fmaf(lam, r * M.at1(b, p, w), __ldg(x + b * hw + p));
     }
+    if (rn) rn_flush(racc, rn);
 }
 
 // --------------------------------------- register-resident projections
@@ -246,9 +252,10 @@ template <int MODE, bool ACC>
 __global__ void __launch_bounds__(256) k_proj_gap_smem(
     const float *__restrict__ x, Mask<MODE> M, const float *__restrict__ y,
     float *__restrict__ y1, const float *__restrict__ phisum, float *__restrict__ xo,
-    float lam, int B, int64_t hw) {
+    float lam, int B, int64_t hw, double *__restrict__ rn) {
     extern __shared__ float xs[];  // [B][blockDim.x]
     const int t = threadIdx.x, nt = blockDim.x;
+    double racc = 0.0;
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < hw;
          p += (int64_t)gridDim.x * blockDim.x) {
         const uint32_t w = M.word1(p);
@@ -268,10 +275,12 @@ __global__ void __launch_bounds__(256) k_proj_gap_smem(
         } else {
             r = __fdiv_rn(yv - s, ps);
         }
+        if (rn) rn_add1(racc, r);
 #pragma unroll 8
         for (int b = 0; b < B; ++b)
             __stcs(xo + b * hw + p, fmaf(lam, r * M.at1(b, p, w), xs[b * nt + t]));
     }
+    if (rn) rn_flush(racc, rn);
 }
 
 // ADMM projection staging t = theta + b and b in shared memory (slots
@@ -280,10 +289,11 @@ template <int MODE>
 __global__ void __launch_bounds__(128) k_proj_admm_smem(
     const float *__restrict__ th, const float *__restrict__ bb, Mask<MODE> M,
     const float *__restrict__ y, const float *__restrict__ phisum, float *__restrict__ v,
-    float *__restrict__ xo, float lam, float gamma, int B, int64_t hw) {
+    float *__restrict__ xo, float lam, float gamma, int B, int64_t hw, double *__restrict__ rn) {
     extern __shared__ float st[];  // [2][B][blockDim.x]: t, b
     const int t = threadIdx.x, nt = blockDim.x;
     float *ts = st, *bs = st + B * nt;
+    double racc = 0.0;
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < hw;
          p += (int64_t)gridDim.x * blockDim.x) {
         const uint32_t w = M.word1(p);
@@ -297,6 +307,7 @@ __global__ void __launch_bounds__(128) k_proj_admm_smem(
             s = fmaf(tv, M.at1(b, p, w), s);
         }
         const float r = __fdiv_rn(__ldg(y + p) - s, __ldg(phisum + p) + gamma);
+        if (rn) rn_add1(racc, r);
 #pragma unroll 8
         for (int b = 0; b < B; ++b) {
             const float xv = fmaf(lam, r * M.at1(b, p, w), ts[b * nt + t]);
@@ -304,25 +315,26 @@ __global__ void __launch_bounds__(128) k_proj_admm_smem(
             __stcs(v + b * hw + p, xv - bs[b * nt + t]);
         }
     }
+    if (rn) rn_flush(racc, rn);
 }
 
 template <int MODE, bool ACC>
 static void launch_gap_smem(const float *x, Mask<MODE> M, const float *y, float *y1,
                             const float *ps, float *xo, float lam, int B, int64_t hw,
-                            cudaStream_t s) {
+                            cudaStream_t s, double *rn) {
     const size_t smem = sizeof(float) * (size_t)B * 256;  // <= 32 KB for B <= 32
     k_proj_gap_smem<MODE, ACC><<<grid_for(hw, 256), 256, smem, s>>>(x, M, y, y1, ps, xo, lam, B,
-                                                                    hw);
+                                                                    hw, rn);
 }
 
 template <int MODE>
 static void launch_admm_smem(const float *th, const float *bb, Mask<MODE> M, const float *y,
                              const float *ps, float *v, float *xo, float lam, float gamma, int B,
-                             int64_t hw, cudaStream_t s) {
+                             int64_t hw, cudaStream_t s, double *rn) {
     // 128 threads: 2 * B * 128 floats <= 32 KB of shared memory for B <= 32
     const size_t smem = sizeof(float) * 2 * (size_t)B * 128;
     k_proj_admm_smem<MODE><<<grid_for(hw, 128), 128, smem, s>>>(th, bb, M, y, ps, v, xo, lam,
-                                                                gamma, B, hw);
+                                                                gamma, B, hw, rn);
 }
 
 // ------------------------------------------- GAP residual map (fused path)
@@ -333,8 +345,9 @@ template <int MODE, bool ACC>
 __global__ void __launch_bounds__(256) k_gap_resid_vec(
     const float *__restrict__ x, Mask<MODE> M, const float *__restrict__ y,
     float *__restrict__ y1, const float *__restrict__ phisum, float *__restrict__ c, int B,
-    int64_t hw) {
+    int64_t hw, double *__restrict__ rn) {
     const int64_t n4 = hw >> 2;
+    double racc = 0.0;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n4;
          q += (int64_t)gridDim.x * blockDim.x) {
         const int64_t p = q << 2;
@@ -363,8 +376,10 @@ __global__ void __launch_bounds__(256) k_gap_resid_vec(
             r = make_float4(__fdiv_rn(yv.x - s.x, ps.x), __fdiv_rn(yv.y - s.y, ps.y),
                             __fdiv_rn(yv.z - s.z, ps.z), __fdiv_rn(yv.w - s.w, ps.w));
         }
+        if (rn) rn_add4(racc, r);
         st4(c + p, r);
     }
+    if (rn) rn_flush(racc, rn);
 }
 
 // ----------------------------------------------------- ADMM projection
@@ -374,8 +389,9 @@ template <int MODE>
 __global__ void __launch_bounds__(256) k_proj_admm_vec(
     const float *__restrict__ th, const float *__restrict__ bb, Mask<MODE> M,
     const float *__restrict__ y, const float *__restrict__ phisum, float *__restrict__ v,
-    float *__restrict__ xo, float lam, float gamma, int B, int64_t hw) {
+    float *__restrict__ xo, float lam, float gamma, int B, int64_t hw, double *__restrict__ rn) {
     const int64_t n4 = hw >> 2;
+    double racc = 0.0;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n4;
          q += (int64_t)gridDim.x * blockDim.x) {
         const int64_t p = q << 2;
@@ -395,6 +411,7 @@ __global__ void __launch_bounds__(256) k_proj_admm_vec(
                                      __fdiv_rn(yv.y - s.y, ps.y + gamma),
                                      __fdiv_rn(yv.z - s.z, ps.z + gamma),
                                      __fdiv_rn(yv.w - s.w, ps.w + gamma));
+        if (rn) rn_add4(racc, r);
 #pragma unroll 4
         for (int b = 0; b < B; ++b) {
             const float4 a = ldg4(th + b * hw + p), c = ldg4(bb + b * hw + p);
@@ -408,6 +425,7 @@ __global__ void __launch_bounds__(256) k_proj_admm_vec(
                    make_float4(xv.x - c.x, xv.y - c.y, xv.z - c.z, xv.w - c.w));
         }
     }
+    if (rn) rn_flush(racc, rn);
 }
 
 template <int MODE>
@@ -415,7 +433,8 @@ __global__ void k_proj_admm_scalar(const float *__restrict__ th, const float *__
                                    Mask<MODE> M, const float *__restrict__ y,
                                    const float *__restrict__ phisum, float *__restrict__ v,
                                    float *__restrict__ xo, float lam, float gamma, int B,
-                                   int64_t hw) {
+                                   int64_t hw, double *__restrict__ rn) {
+    double racc = 0.0;
     for (int64_t p = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; p < hw;
          p += (int64_t)gridDim.x * blockDim.x) {
         const uint32_t w = M.word1(p);
@@ -423,6 +442,7 @@ __global__ void k_proj_admm_scalar(const float *__restrict__ th, const float *__
         for (int b = 0; b < B; ++b)
             s = fmaf(__ldg(th + b * hw + p) + __ldg(bb + b * hw + p), M.at1(b, p, w), s);
         const float r = __fdiv_rn(y[p] - s, phisum[p] + gamma);
+        if (rn) rn_add1(racc, r);
         for (int b = 0; b < B; ++b) {
             const float t = __ldg(th + b * hw + p) + __ldg(bb + b * hw + p);
             const float xv = fmaf(lam, r * M.at1(b, p, w), t);
@@ -430,6 +450,7 @@ __global__ void k_proj_admm_scalar(const float *__restrict__ th, const float *__
             v[b * hw + p] = xv - __ldg(bb + b * hw + p);
         }
     }
+    if (rn) rn_flush(racc, rn);
 }
 
 // ------------------------------------------------------- squared error
@@ -465,6 +486,126 @@ static bool vec_ok(int64_t hw, std::initializer_list<const void *> ptrs) {
     for (const void *p : ptrs)
         if (p && !aligned16(p)) return false;
     return true;
+}
+
+// Projection entry points with an optional FP64 ||r||^2 accumulator `rn`
+// (the C ABI's functions pass none; the native solver loops pass the
+// iteration's slot).
+int proj_gap_rn(const float *x, const float *phi, const uint32_t *mask_bits, const float *y,
+                 float *y1, const float *phisum, float *x_out, float lambda, int accelerate,
+                 int64_t B, int64_t H, int64_t W, void *stream, double *rn) {
+    if (int e = check_dims(B, H, W)) return e;
+    SCI_CHECK_ARG(x && y && phisum && x_out && (phi || mask_bits),
+                  "sci_proj_gap: null pointer");
+    SCI_CHECK_ARG(!accelerate || y1, "sci_proj_gap: accelerate needs y1");
+    SCI_CHECK_ARG(!mask_bits || B <= 32, "sci_proj_gap: packed mask needs B <= 32");
+    SCI_CHECK_ARG(x != x_out, "sci_proj_gap: x and x_out must not alias");
+    const int64_t hw = H * W;
+    cudaStream_t s = as_stream(stream);
+    const bool vec = vec_ok(hw, {x, phi, mask_bits, y, y1, phisum, x_out});
+    const int Bi = (int)B;
+#define LAUNCH_GAP(MODE, M)                                                                 \
+    do {                                                                                    \
+        if (vec) {                                                                          \
+            if (accelerate)                                                                 \
+                k_proj_gap_vec<MODE, true><<<grid_for(hw / 4, 256), 256, 0, s>>>(           \
+                    x, M, y, y1, phisum, x_out, lambda, Bi, hw, rn);                        \
+            else                                                                            \
+                k_proj_gap_vec<MODE, false><<<grid_for(hw / 4, 256), 256, 0, s>>>(          \
+                    x, M, y, y1, phisum, x_out, lambda, Bi, hw, rn);                        \
+        } else {                                                                            \
+            if (accelerate)                                                                 \
+                k_proj_gap_scalar<MODE, true><<<grid_for(hw, 256), 256, 0, s>>>(            \
+                    x, M, y, y1, phisum, x_out, lambda, Bi, hw, rn);                        \
+            else                                                                            \
+                k_proj_gap_scalar<MODE, false><<<grid_for(hw, 256), 256, 0, s>>>(           \
+                    x, M, y, y1, phisum, x_out, lambda, Bi, hw, rn);                        \
+        }                                                                                   \
+    } while (0)
+    const char *tma = getenv("SCI_PROJ_TMA");
+    if (mask_bits && !(tma && atoi(tma) == 0)) {
+        // bulk-copy staged kernel; SCI_ERR_UNSUPPORTED: alignment or B
+        const int e = launch_proj_gap_tma(x, mask_bits, y, y1, phisum, x_out, lambda,
+                                          accelerate != 0, Bi, hw, s, rn);
+        if (e != SCI_ERR_UNSUPPORTED) return e;
+    }
+    if (mask_bits) {
+        Mask<1> M{mask_bits, hw};
+        if (accelerate)
+            launch_gap_smem<1, true>(x, M, y, y1, phisum, x_out, lambda, Bi, hw, s, rn);
+        else
+            launch_gap_smem<1, false>(x, M, y, y1, phisum, x_out, lambda, Bi, hw, s, rn);
+    } else {
+        Mask<0> M{phi, hw};
+        LAUNCH_GAP(0, M);
+    }
+#undef LAUNCH_GAP
+    SCI_LAUNCHED("k_proj_gap");
+    return SCI_OK;
+}
+
+int gap_residual_rn(const float *x, const float *phi, const uint32_t *mask_bits,
+                     const float *y, float *y1, const float *phisum, float *c,
+                     int accelerate, int64_t B, int64_t H, int64_t W, void *stream, double *rn) {
+    if (int e = check_dims(B, H, W)) return e;
+    SCI_CHECK_ARG(x && y && phisum && c && (phi || mask_bits), "sci_gap_residual: null pointer");
+    SCI_CHECK_ARG(!accelerate || y1, "sci_gap_residual: accelerate needs y1");
+    SCI_CHECK_ARG(!mask_bits || B <= 32, "sci_gap_residual: packed mask needs B <= 32");
+    const int64_t hw = H * W;
+    SCI_CHECK_ARG(vec_ok(hw, {x, phi, mask_bits, y, y1, phisum, c}),
+                  "sci_gap_residual: needs H*W %% 4 == 0 and 16-byte aligned buffers");
+    cudaStream_t s = as_stream(stream);
+    const dim3 g = grid_for(hw / 4, 256);
+    if (mask_bits) {
+        Mask<1> M{mask_bits, hw};
+        if (accelerate) k_gap_resid_vec<1, true><<<g, 256, 0, s>>>(x, M, y, y1, phisum, c, (int)B, hw, rn);
+        else k_gap_resid_vec<1, false><<<g, 256, 0, s>>>(x, M, y, y1, phisum, c, (int)B, hw, rn);
+    } else {
+        Mask<0> M{phi, hw};
+        if (accelerate) k_gap_resid_vec<0, true><<<g, 256, 0, s>>>(x, M, y, y1, phisum, c, (int)B, hw, rn);
+        else k_gap_resid_vec<0, false><<<g, 256, 0, s>>>(x, M, y, y1, phisum, c, (int)B, hw, rn);
+    }
+    SCI_LAUNCHED("k_gap_resid");
+    return SCI_OK;
+}
+
+int proj_admm_rn(const float *theta, const float *b, const float *phi,
+                  const uint32_t *mask_bits, const float *y, const float *phisum, float *v,
+                  float *x_out, float lambda, float gamma, int64_t B, int64_t H, int64_t W,
+                  void *stream, double *rn) {
+    if (int e = check_dims(B, H, W)) return e;
+    SCI_CHECK_ARG(theta && b && y && phisum && v && (phi || mask_bits),
+                  "sci_proj_admm: null pointer");
+    SCI_CHECK_ARG(!mask_bits || B <= 32, "sci_proj_admm: packed mask needs B <= 32");
+    SCI_CHECK_ARG(v != theta && v != b && x_out != theta && x_out != b,
+                  "sci_proj_admm: outputs must not alias inputs");
+    const int64_t hw = H * W;
+    cudaStream_t s = as_stream(stream);
+    const bool vec = vec_ok(hw, {theta, b, phi, mask_bits, y, phisum, v, x_out});
+    const int Bi = (int)B;
+    const char *tma = getenv("SCI_PROJ_TMA");
+    if (mask_bits && !(tma && atoi(tma) == 0)) {
+        // bulk-copy staged kernel; SCI_ERR_UNSUPPORTED: alignment or B
+        const int e = launch_proj_admm_tma(theta, b, mask_bits, y, phisum, v, x_out, lambda,
+                                           gamma, Bi, hw, s, false, rn);
+        if (e != SCI_ERR_UNSUPPORTED) return e;
+    }
+    if (mask_bits) {
+        Mask<1> M{mask_bits, hw};
+        launch_admm_smem<1>(theta, b, M, y, phisum, v, x_out, lambda, gamma, Bi, hw, s, rn);
+    } else {
+        Mask<0> M{phi, hw};
+        if (vec)
+            k_proj_admm_vec<0><<<grid_for(hw / 4, 256), 256, 0, s>>>(theta, b, M, y, phisum, v,
+                                                                     x_out, lambda, gamma, Bi, hw,
+                                                                     rn);
+        else
+            k_proj_admm_scalar<0><<<grid_for(hw, 256), 256, 0, s>>>(theta, b, M, y, phisum, v,
+                                                                    x_out, lambda, gamma, Bi, hw,
+                                                                    rn);
+    }
+    SCI_LAUNCHED("k_proj_admm");
+    return SCI_OK;
 }
 
 }  // namespace sci
@@ -538,114 +679,23 @@ int sci_pack_mask(const float *phi, uint32_t *bits, int *flag, int64_t B, int64_
 int sci_proj_gap(const float *x, const float *phi, const uint32_t *mask_bits, const float *y,
                  float *y1, const float *phisum, float *x_out, float lambda, int accelerate,
                  int64_t B, int64_t H, int64_t W, void *stream) {
-    if (int e = check_dims(B, H, W)) return e;
-    SCI_CHECK_ARG(x && y && phisum && x_out && (phi || mask_bits),
-                  "sci_proj_gap: null pointer");
-    SCI_CHECK_ARG(!accelerate || y1, "sci_proj_gap: accelerate needs y1");
-    SCI_CHECK_ARG(!mask_bits || B <= 32, "sci_proj_gap: packed mask needs B <= 32");
-    SCI_CHECK_ARG(x != x_out, "sci_proj_gap: x and x_out must not alias");
-    const int64_t hw = H * W;
-    cudaStream_t s = as_stream(stream);
-    const bool vec = vec_ok(hw, {x, phi, mask_bits, y, y1, phisum, x_out});
-    const int Bi = (int)B;
-#define LAUNCH_GAP(MODE, M)                                                                 \
-    do {                                                                                    \
-        if (vec) {                                                                          \
-            if (accelerate)                                                                 \
-                k_proj_gap_vec<MODE, true><<<grid_for(hw / 4, 256), 256, 0, s>>>(           \
-                    x, M, y, y1, phisum, x_out, lambda, Bi, hw);                            \
-            else                                                                            \
-                k_proj_gap_vec<MODE, false><<<grid_for(hw / 4, 256), 256, 0, s>>>(          \
-                    x, M, y, y1, phisum, x_out, lambda, Bi, hw);                            \
-        } else {                                                                            \
-            if (accelerate)                                                                 \
-                k_proj_gap_scalar<MODE, true><<<grid_for(hw, 256), 256, 0, s>>>(            \
-                    x, M, y, y1, phisum, x_out, lambda, Bi, hw);                            \
-            else                                                                            \
-                k_proj_gap_scalar<MODE, false><<<grid_for(hw, 256), 256, 0, s>>>(           \
-                    x, M, y, y1, phisum, x_out, lambda, Bi, hw);                            \
-        }                                                                                   \
-    } while (0)
-    const char *tma = getenv("SCI_PROJ_TMA");
-    if (mask_bits && !(tma && atoi(tma) == 0)) {
-        // bulk-copy staged kernel; SCI_ERR_UNSUPPORTED: alignment or B
-        const int e = launch_proj_gap_tma(x, mask_bits, y, y1, phisum, x_out, lambda,
-                                          accelerate != 0, Bi, hw, s);
-        if (e != SCI_ERR_UNSUPPORTED) return e;
-    }
-    if (mask_bits) {
-        Mask<1> M{mask_bits, hw};
-        if (accelerate) launch_gap_smem<1, true>(x, M, y, y1, phisum, x_out, lambda, Bi, hw, s);
-        else launch_gap_smem<1, false>(x, M, y, y1, phisum, x_out, lambda, Bi, hw, s);
-    } else {
-        Mask<0> M{phi, hw};
-        LAUNCH_GAP(0, M);
-    }
-#undef LAUNCH_GAP
-    SCI_LAUNCHED("k_proj_gap");
-    return SCI_OK;
+    return sci::proj_gap_rn(x, phi, mask_bits, y, y1, phisum, x_out, lambda, accelerate, B, H,
+                            W, stream, nullptr);
 }
 
 int sci_gap_residual(const float *x, const float *phi, const uint32_t *mask_bits,
                      const float *y, float *y1, const float *phisum, float *c,
                      int accelerate, int64_t B, int64_t H, int64_t W, void *stream) {
-    if (int e = check_dims(B, H, W)) return e;
-    SCI_CHECK_ARG(x && y && phisum && c && (phi || mask_bits), "sci_gap_residual: null pointer");
-    SCI_CHECK_ARG(!accelerate || y1, "sci_gap_residual: accelerate needs y1");
-    SCI_CHECK_ARG(!mask_bits || B <= 32, "sci_gap_residual: packed mask needs B <= 32");
-    const int64_t hw = H * W;
-    SCI_CHECK_ARG(vec_ok(hw, {x, phi, mask_bits, y, y1, phisum, c}),
-                  "sci_gap_residual: needs H*W %% 4 == 0 and 16-byte aligned buffers");
-    cudaStream_t s = as_stream(stream);
-    const dim3 g = grid_for(hw / 4, 256);
-    if (mask_bits) {
-        Mask<1> M{mask_bits, hw};
-        if (accelerate) k_gap_resid_vec<1, true><<<g, 256, 0, s>>>(x, M, y, y1, phisum, c, (int)B, hw);
-        else k_gap_resid_vec<1, false><<<g, 256, 0, s>>>(x, M, y, y1, phisum, c, (int)B, hw);
-    } else {
-        Mask<0> M{phi, hw};
-        if (accelerate) k_gap_resid_vec<0, true><<<g, 256, 0, s>>>(x, M, y, y1, phisum, c, (int)B, hw);
-        else k_gap_resid_vec<0, false><<<g, 256, 0, s>>>(x, M, y, y1, phisum, c, (int)B, hw);
-    }
-    SCI_LAUNCHED("k_gap_resid");
-    return SCI_OK;
+    return sci::gap_residual_rn(x, phi, mask_bits, y, y1, phisum, c, accelerate, B, H, W,
+                                stream, nullptr);
 }
 
 int sci_proj_admm(const float *theta, const float *b, const float *phi,
                   const uint32_t *mask_bits, const float *y, const float *phisum, float *v,
                   float *x_out, float lambda, float gamma, int64_t B, int64_t H, int64_t W,
                   void *stream) {
-    if (int e = check_dims(B, H, W)) return e;
-    SCI_CHECK_ARG(theta && b && y && phisum && v && (phi || mask_bits),
-                  "sci_proj_admm: null pointer");
-    SCI_CHECK_ARG(!mask_bits || B <= 32, "sci_proj_admm: packed mask needs B <= 32");
-    SCI_CHECK_ARG(v != theta && v != b && x_out != theta && x_out != b,
-                  "sci_proj_admm: outputs must not alias inputs");
-    const int64_t hw = H * W;
-    cudaStream_t s = as_stream(stream);
-    const bool vec = vec_ok(hw, {theta, b, phi, mask_bits, y, phisum, v, x_out});
-    const int Bi = (int)B;
-    const char *tma = getenv("SCI_PROJ_TMA");
-    if (mask_bits && !(tma && atoi(tma) == 0)) {
-        // bulk-copy staged kernel; SCI_ERR_UNSUPPORTED: alignment or B
-        const int e = launch_proj_admm_tma(theta, b, mask_bits, y, phisum, v, x_out, lambda,
-                                           gamma, Bi, hw, s);
-        if (e != SCI_ERR_UNSUPPORTED) return e;
-    }
-    if (mask_bits) {
-        Mask<1> M{mask_bits, hw};
-        launch_admm_smem<1>(theta, b, M, y, phisum, v, x_out, lambda, gamma, Bi, hw, s);
-    } else {
-        Mask<0> M{phi, hw};
-        if (vec)
-            k_proj_admm_vec<0><<<grid_for(hw / 4, 256), 256, 0, s>>>(theta, b, M, y, phisum, v,
-                                                                     x_out, lambda, gamma, Bi, hw);
-        else
-            k_proj_admm_scalar<0><<<grid_for(hw, 256), 256, 0, s>>>(theta, b, M, y, phisum, v,
-                                                                    x_out, lambda, gamma, Bi, hw);
-    }
-    SCI_LAUNCHED("k_proj_admm");
-    return SCI_OK;
+    return sci::proj_admm_rn(theta, b, phi, mask_bits, y, phisum, v, x_out, lambda, gamma, B, H,
+                             W, stream, nullptr);
 }
 
 int sci_sqerr_accum(const float *a, const float *b, int64_t n, double *out, void *stream) {

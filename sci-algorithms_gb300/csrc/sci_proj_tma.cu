@@ -21,6 +21,9 @@
 // flight and ends the block.
 #include <algorithm>
 #include <cstdlib>
+#include <map>
+#include <mutex>
+#include <tuple>
 #include <type_traits>
 
 #include "sci_bulk.cuh"
@@ -33,6 +36,26 @@ __device__ unsigned int g_device_status;
 namespace {
 
 __device__ __forceinline__ float bit(uint32_t w, int b) { return ((w >> b) & 1u) ? 1.0f : 0.0f; }
+
+// Resident blocks per SM of a persistent kernel at `threads` threads and
+// `smem` bytes of dynamic shared memory, from the occupancy calculator
+// (cached per kernel and size; at least 1).
+int resident_blocks(const void *kern, int threads, size_t smem) {
+    static std::mutex mu;
+    static std::map<std::tuple<const void *, int, size_t>, int> cache;
+    const auto key = std::make_tuple(kern, threads, smem);
+    std::lock_guard<std::mutex> lock(mu);
+    auto f = cache.find(key);
+    if (f != cache.end()) return f->second;
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, kern, threads, smem) != cudaSuccess ||
+        n < 1) {
+        cudaGetLastError();
+        n = 1;
+    }
+    cache[key] = n;
+    return n;
+}
 
 // Issues the copies of tile t into buffer `buf` (thread 0 only).  The
 // per-pixel maps are read with plain loads: staging them as well (28 KB
@@ -52,9 +75,10 @@ template <int TP, bool ACC>
 __global__ void __launch_bounds__(TP / 4) k_proj_gap_tma(
     const float *__restrict__ x, const uint32_t *__restrict__ bits, const float *__restrict__ y,
     float *__restrict__ y1, const float *__restrict__ phisum, float *__restrict__ xo, float lam,
-    int B, int64_t hw) {
+    int B, int64_t hw, double *__restrict__ rn) {
     extern __shared__ __align__(128) float xs[];  // [2][B][TP]
     __shared__ __align__(8) uint64_t bars[2];
+    double racc = 0.0;  // FP64 partial of ||r||^2 (rn != nullptr)
     const int tid = threadIdx.x;
     const int64_t ntiles = (hw + TP - 1) / TP;
     const int64_t G = gridDim.x;
@@ -115,6 +139,7 @@ __global__ void __launch_bounds__(TP / 4) k_proj_gap_tma(
                 r = make_float4(__fdiv_rn(yv.x - s.x, ps.x), __fdiv_rn(yv.y - s.y, ps.y),
                                 __fdiv_rn(yv.z - s.z, ps.z), __fdiv_rn(yv.w - s.w, ps.w));
             }
+            if (rn) rn_add4(racc, r);
 #pragma unroll 4
             for (int b = 0; b < B; ++b) {
                 const float4 v = *reinterpret_cast<const float4 *>(xb + b * TP);
@@ -132,6 +157,7 @@ __global__ void __launch_bounds__(TP / 4) k_proj_gap_tma(
             issue_tile<TP>(xs, bars, buf, t + 2 * G, x, B, hw);
         }
     }
+    if (rn) rn_flush_warp(racc, rn);
 }
 
 // ADMM projection (pnp_sci_algo.py:808-812 with a packed mask), same
@@ -169,9 +195,10 @@ template <int TP, bool WANT_X, bool BFV = false>
 __global__ void __launch_bounds__(TP / 4) k_proj_admm_tma(
     const float *__restrict__ th, const float *__restrict__ bb, const uint32_t *__restrict__ bits,
     const float *__restrict__ y, const float *__restrict__ phisum, float *__restrict__ v,
-    float *__restrict__ xo, float lam, float gamma, int B, int64_t hw) {
+    float *__restrict__ xo, float lam, float gamma, int B, int64_t hw, double *__restrict__ rn) {
     extern __shared__ __align__(128) float xs[];  // [2][B][TP]: theta
     __shared__ __align__(8) uint64_t bars[2];
+    double racc = 0.0;  // FP64 partial of ||r||^2 (rn != nullptr)
     const int tid = threadIdx.x;
     const int64_t ntiles = (hw + TP - 1) / TP;
     const int64_t G = gridDim.x;
@@ -227,6 +254,7 @@ __global__ void __launch_bounds__(TP / 4) k_proj_admm_tma(
                                          __fdiv_rn(yv.y - s.y, ps.y + gamma),
                                          __fdiv_rn(yv.z - s.z, ps.z + gamma),
                                          __fdiv_rn(yv.w - s.w, ps.w + gamma));
+            if (rn) rn_add4(racc, r);
 #pragma unroll kAdmmUnroll
             for (int b = 0; b < B; ++b) {
                 const float4 a = *reinterpret_cast<const float4 *>(tb + b * TP);
@@ -246,23 +274,23 @@ __global__ void __launch_bounds__(TP / 4) k_proj_admm_tma(
             issue_theta<TP>(xs, bars, buf, t + 2 * G, th, B, hw);
         }
     }
+    if (rn) rn_flush_warp(racc, rn);
 }
 
 template <int TP>
 int launch_tp(const float *x, const uint32_t *bits, const float *y, float *y1,
               const float *phisum, float *xo, float lam, bool acc, int B, int64_t hw,
-              cudaStream_t s) {
+              cudaStream_t s, double *rn) {
     const size_t smem = sizeof(float) * 2 * (size_t)B * TP;
     const int64_t ntiles = (hw + TP - 1) / TP;
-    // resident blocks per SM: 227 KB of shared memory (+1 KB reserved per block)
-    const int64_t per_sm =
-        std::max<int64_t>(1, std::min<int64_t>(16, (227 * 1024) / (int64_t)(smem + 1024)));
-    const unsigned g = (unsigned)std::min<int64_t>(ntiles, per_sm * kSMs);
     auto kern = acc ? k_proj_gap_tma<TP, true> : k_proj_gap_tma<TP, false>;
     // above 48 KB of dynamic shared memory needs the opt-in attribute; a
     // host-side call, also valid while the stream is being captured
     SCI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    kern<<<g, TP / 4, smem, s>>>(x, bits, y, y1, phisum, xo, lam, B, hw);
+    // the persistent grid: every block resident at once
+    const unsigned g = (unsigned)std::min<int64_t>(
+        ntiles, (int64_t)resident_blocks(reinterpret_cast<const void *>(kern), TP / 4, smem) * kSMs);
+    kern<<<g, TP / 4, smem, s>>>(x, bits, y, y1, phisum, xo, lam, B, hw, rn);
     SCI_LAUNCHED("k_proj_gap_tma");
     return SCI_OK;
 }
@@ -273,7 +301,7 @@ int launch_tp(const float *x, const uint32_t *bits, const float *y, float *y1,
 // SCI_OK, or a negative code when the caller must use another kernel.
 int launch_proj_gap_tma(const float *x, const uint32_t *bits, const float *y, float *y1,
                         const float *phisum, float *xo, float lam, bool acc, int B, int64_t hw,
-                        cudaStream_t s) {
+                        cudaStream_t s, double *rn) {
     const uintptr_t a = reinterpret_cast<uintptr_t>(x) | reinterpret_cast<uintptr_t>(bits) |
                         reinterpret_cast<uintptr_t>(y) | reinterpret_cast<uintptr_t>(y1) |
                         reinterpret_cast<uintptr_t>(phisum) | reinterpret_cast<uintptr_t>(xo);
@@ -282,9 +310,9 @@ int launch_proj_gap_tma(const float *x, const uint32_t *bits, const float *y, fl
     // 24: 128 (one warp, 24 KB, 9 blocks per SM) 141 us, 256 146 us, 512 153 us.
     const char *e = getenv("SCI_PROJ_TP");
     const int tp = e ? atoi(e) : 128;
-    if (tp == 512) return launch_tp<512>(x, bits, y, y1, phisum, xo, lam, acc, B, hw, s);
-    if (tp == 256) return launch_tp<256>(x, bits, y, y1, phisum, xo, lam, acc, B, hw, s);
-    return launch_tp<128>(x, bits, y, y1, phisum, xo, lam, acc, B, hw, s);
+    if (tp == 512) return launch_tp<512>(x, bits, y, y1, phisum, xo, lam, acc, B, hw, s, rn);
+    if (tp == 256) return launch_tp<256>(x, bits, y, y1, phisum, xo, lam, acc, B, hw, s, rn);
+    return launch_tp<128>(x, bits, y, y1, phisum, xo, lam, acc, B, hw, s, rn);
 }
 
 // ADMM projection with a packed mask (B <= 32, 16-byte aligned planes,
@@ -293,7 +321,7 @@ int launch_proj_gap_tma(const float *x, const uint32_t *bits, const float *y, fl
 // is the previous TV input v and b = theta - v (bitwise the TV's residual).
 int launch_proj_admm_tma(const float *th, const float *bb, const uint32_t *bits, const float *y,
                          const float *phisum, float *v, float *xo, float lam, float gamma, int B,
-                         int64_t hw, cudaStream_t s, bool b_from_v) {
+                         int64_t hw, cudaStream_t s, bool b_from_v, double *rn) {
     const uintptr_t a = reinterpret_cast<uintptr_t>(th) | reinterpret_cast<uintptr_t>(bb) |
                         reinterpret_cast<uintptr_t>(bits) | reinterpret_cast<uintptr_t>(y) |
                         reinterpret_cast<uintptr_t>(phisum) | reinterpret_cast<uintptr_t>(v) |
@@ -305,16 +333,16 @@ int launch_proj_admm_tma(const float *th, const float *bb, const uint32_t *bits,
         constexpr int TP = decltype(tpc)::value;
         const size_t smem = sizeof(float) * 2 * (size_t)B * TP;
         const int64_t ntiles = (hw + TP - 1) / TP;
-        const int64_t per_sm =
-            std::max<int64_t>(1, std::min<int64_t>(16, (227 * 1024) / (int64_t)(smem + 1024)));
-        const unsigned g = (unsigned)std::min<int64_t>(ntiles, per_sm * kSMs);
         auto kern = b_from_v ? (xo ? k_proj_admm_tma<TP, true, true>
                                    : k_proj_admm_tma<TP, false, true>)
                              : (xo ? k_proj_admm_tma<TP, true, false>
                                    : k_proj_admm_tma<TP, false, false>);
         SCI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                       (int)smem));
-        kern<<<g, TP / 4, smem, s>>>(th, bb, bits, y, phisum, v, xo, lam, gamma, B, hw);
+        const unsigned g = (unsigned)std::min<int64_t>(
+            ntiles,
+            (int64_t)resident_blocks(reinterpret_cast<const void *>(kern), TP / 4, smem) * kSMs);
+        kern<<<g, TP / 4, smem, s>>>(th, bb, bits, y, phisum, v, xo, lam, gamma, B, hw, rn);
         SCI_LAUNCHED("k_proj_admm_tma");
         return SCI_OK;
     };

@@ -28,7 +28,17 @@ int tvx_launch(int kind, const float *f, float *u, float *resid, int64_t nf, int
 size_t tvx_workspace_bytes(int kind, int64_t nf, int64_t H, int64_t W, int iters);
 int launch_proj_admm_tma(const float *th, const float *bb, const uint32_t *bits, const float *y,
                          const float *phisum, float *v, float *xo, float lam, float gamma, int B,
-                         int64_t hw, cudaStream_t s, bool b_from_v);
+                         int64_t hw, cudaStream_t s, bool b_from_v, double *rn);
+int proj_gap_rn(const float *x, const float *phi, const uint32_t *mask_bits, const float *y,
+                float *y1, const float *phisum, float *x_out, float lambda, int accelerate,
+                int64_t B, int64_t H, int64_t W, void *stream, double *rn);
+int gap_residual_rn(const float *x, const float *phi, const uint32_t *mask_bits,
+                    const float *y, float *y1, const float *phisum, float *c,
+                    int accelerate, int64_t B, int64_t H, int64_t W, void *stream, double *rn);
+int proj_admm_rn(const float *theta, const float *b, const float *phi,
+                 const uint32_t *mask_bits, const float *y, const float *phisum, float *v,
+                 float *x_out, float lambda, float gamma, int64_t B, int64_t H, int64_t W,
+                 void *stream, double *rn);
 
 namespace {
 
@@ -116,6 +126,7 @@ struct Args {
         put_bytes(k, o.orig);
         put_bytes(k, o.sqerr);
         put_bytes(k, o.tv_steps);
+        put_bytes(k, o.resid_norm);
         put_bytes(k, ws);
         k.append(reinterpret_cast<const char *>(o.lambdas), sizeof(float) * o.iters);
         k.append(reinterpret_cast<const char *>(o.weights), sizeof(float) * o.iters);
@@ -146,6 +157,9 @@ int enqueue(const Args &a, cudaStream_t s) {
                          w.tv, w.tv_bytes, s, 0);
     };
     if (o.sqerr) SCI_CUDA(cudaMemsetAsync(o.sqerr, 0, sizeof(double) * o.iters, s));
+    if (o.resid_norm) SCI_CUDA(cudaMemsetAsync(o.resid_norm, 0, sizeof(double) * o.iters, s));
+    // FP64 ||r||^2 of iteration `it`'s projection residual (nullable)
+    auto rn = [&](int it) { return o.resid_norm ? o.resid_norm + it : nullptr; };
     const bool aligned = ((reinterpret_cast<uintptr_t>(a.x0) | reinterpret_cast<uintptr_t>(a.x_out) |
                            reinterpret_cast<uintptr_t>(a.y) | reinterpret_cast<uintptr_t>(a.phisum) |
                            reinterpret_cast<uintptr_t>(a.bits)) & 15u) == 0;
@@ -162,8 +176,8 @@ int enqueue(const Args &a, cudaStream_t s) {
         for (int it = 0; it < o.iters; ++it) {
             const float *cur = X[(start + it) & 1];
             float *nxt = X[(start + it + 1) & 1];
-            int e = sci_gap_residual(cur, nullptr, a.bits, a.y, w.y1, a.phisum, w.c, o.accelerate,
-                                     B, H, W, s);
+            int e = gap_residual_rn(cur, nullptr, a.bits, a.y, w.y1, a.phisum, w.c,
+                                    o.accelerate, B, H, W, s, rn(it));
             if (e) return e;
             e = tv_launch_impl(cur, nxt, nullptr, B, H, W, hw, o.weights[it], o.eps, K,
                                o.tv_steps ? o.tv_steps + (int64_t)it * B : nullptr, nullptr, w.tv,
@@ -182,8 +196,8 @@ int enqueue(const Args &a, cudaStream_t s) {
             SCI_CUDA(cudaMemcpyAsync(a.x_out, a.x0, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
         if (o.accelerate) SCI_CUDA(cudaMemsetAsync(w.y1, 0, sizeof(float) * hw, s));
         for (int it = 0; it < o.iters; ++it) {
-            int e = sci_proj_gap(a.x_out, a.phi, a.bits, a.y, w.y1, a.phisum, w.xp, o.lambdas[it],
-                                 o.accelerate, B, H, W, s);
+            int e = proj_gap_rn(a.x_out, a.phi, a.bits, a.y, w.y1, a.phisum, w.xp,
+                                o.lambdas[it], o.accelerate, B, H, W, s, rn(it));
             if (e) return e;
             e = denoise(w.xp, a.x_out, nullptr, it);
             if (e) return e;
@@ -210,7 +224,7 @@ int enqueue(const Args &a, cudaStream_t s) {
             const float gamma = o.gammas ? o.gammas[it] : o.gamma;
             int e = launch_proj_admm_tma(w.theta, vprev, a.bits, a.y, a.phisum, vcur,
                                          want_x ? a.x_out : nullptr, o.lambdas[it], gamma,
-                                         (int)B, hw, s, true);
+                                         (int)B, hw, s, true, rn(it));
             if (e) return e;
             e = denoise(vcur, w.theta, nullptr, it);
             if (e) return e;
@@ -227,8 +241,9 @@ int enqueue(const Args &a, cudaStream_t s) {
     for (int it = 0; it < o.iters; ++it) {
         const bool want_x = (it == o.iters - 1) || (o.orig && o.sqerr);
         const float gamma = o.gammas ? o.gammas[it] : o.gamma;
-        int e = sci_proj_admm(w.theta, bcur, a.phi, a.bits, a.y, a.phisum, w.v,
-                              want_x ? a.x_out : nullptr, o.lambdas[it], gamma, B, H, W, s);
+        int e = proj_admm_rn(w.theta, bcur, a.phi, a.bits, a.y, a.phisum, w.v,
+                             want_x ? a.x_out : nullptr, o.lambdas[it], gamma, B, H, W, s,
+                             rn(it));
         if (e) return e;
         // theta = TV(x - b);  b = b - (x - theta) = theta - v
         e = denoise(w.v, w.theta, bnext, it);

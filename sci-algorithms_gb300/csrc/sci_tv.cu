@@ -107,16 +107,18 @@ static int choose_R_slim(int64_t nf, int nbands, int H, int S, int64_t resident)
 }  // namespace tv
 
 // Register-lean TV pass (sci_tv_slim.cuh) for single-pass scikit-image runs
-// on 16-byte aligned frames at least 512 columns wide; SCI_TV_SLIM=0 selects
-// the generic pipeline instead.  SCI_SLIM_MINB picks its register budget
-// (3 or 4 resident blocks per SM).
+// on aligned frames; SCI_TV_SLIM=0 selects the generic pipeline instead.
+// SCI_SLIM_MINB picks its register budget for n_iter_max = 5 (resident
+// blocks per SM: 3 or 4 with 4 columns per lane, 5, 6 or 7 with 2).
 static bool slim_enabled() {
     const char *e = getenv("SCI_TV_SLIM");
     return !e || atoi(e) != 0;
 }
-static int slim_minb() {
+static int slim_minb(int cpl) {
     const char *e = getenv("SCI_SLIM_MINB");
-    return (e && atoi(e) == 3) ? 3 : 4;
+    const int v = e ? atoi(e) : 0;
+    if (cpl == 4) return v == 3 ? 3 : 4;
+    return (v == 5 || v == 7) ? v : 6;
 }
 
 // Columns per lane: 4 halves the halo overhead of a band (8 of 128 columns
@@ -215,15 +217,26 @@ static int tv_launch_core(const float *f, float *u, float *resid, int64_t nf, in
         SCI_LAUNCHED("k_init_done");
     }
 
-    // the on-load projection and the MATLAB rules are built for 4 columns
-    const int cpl = (proj || ra.rule != RULE_SKIMAGE) ? 4 : choose_cpl(W);
+    // the generic pipeline's on-load projection and MATLAB rules are built
+    // for 4 columns; the lean pass takes 2 or 4
     const int lag = (proj || tape || ra.rule != RULE_SKIMAGE) ? 1 : choose_lag();
+    const bool slim_ok = slim_enabled() && ra.rule == RULE_SKIMAGE && !tape && !resid &&
+                         U <= SMAX && lag == 1;
+    auto aligned_for = [&](int c) {
+        return (W % c == 0) && (fs % c == 0) && W >= c &&
+               ((reinterpret_cast<uintptr_t>(f) | reinterpret_cast<uintptr_t>(u) |
+                 reinterpret_cast<uintptr_t>(resid) | reinterpret_cast<uintptr_t>(proj_bits) |
+                 reinterpret_cast<uintptr_t>(proj_c)) % (4 * c) == 0);
+    };
+    // flags bits 8-11: columns per lane forced by the caller (2 or 4)
+    const int fcpl = (flags >> 8) & 0xf;
+    const int cpl_pick = (fcpl == 2 || fcpl == 4) ? fcpl : choose_cpl(W);
+    const bool slim = slim_ok && aligned_for(cpl_pick);
+    const int cpl = slim ? cpl_pick : ((proj || ra.rule != RULE_SKIMAGE) ? 4 : cpl_pick);
     const bool vec = (W % cpl == 0) && (fs % cpl == 0) &&
                      ((reinterpret_cast<uintptr_t>(f) | reinterpret_cast<uintptr_t>(u) |
                        reinterpret_cast<uintptr_t>(resid)) % (4 * cpl) == 0);
-    const bool slim = slim_enabled() && ra.rule == RULE_SKIMAGE && !tape && !proj && !resid &&
-                      U <= SMAX && cpl == 4 && lag == 1 && vec && W >= 4;
-    const int minb = slim_minb();
+    const int minb = slim_minb(cpl);
     const float *pin = nullptr;
     float *pbuf[2] = {w.pa, w.pb};
     int pi = 0;
@@ -270,7 +283,7 @@ static int tv_launch_core(const float *f, float *u, float *resid, int64_t nf, in
         if (force_R > 0) P.R = force_R;
         else if (slim)
             P.R = choose_R_slim(nf, P.nbands, (int)H, SG,
-                                (int64_t)kSMs * slim_resident_blocks(SG, minb) * WPB);
+                                (int64_t)kSMs * slim_resident_blocks(cpl, SG, minb, proj) * WPB);
         else P.R = choose_R(nf, P.nbands, (int)H);
         P.nchunks = (int)((H + P.R - 1) / P.R);
         P.S = SG;
@@ -286,7 +299,7 @@ static int tv_launch_core(const float *f, float *u, float *resid, int64_t nf, in
         const int per_frame_blocks = (P.nbands * P.nchunks + WPB - 1) / WPB;
         P.gpf = std::max(1, std::min(per_frame_blocks, 16));
         if (slim) {
-            launch_slim(P, SG, minb, s);
+            launch_slim(P, SG, minb, proj, s);
         } else if (tape) {
             launch_tape(P, SG, s);
         } else if (ra.rule == RULE_CHAM_ITV) {
@@ -306,7 +319,7 @@ static int tv_launch_core(const float *f, float *u, float *resid, int64_t nf, in
         }
         SCI_LAUNCHED("k_tv_main");
         if (stop_test) {
-            if (slim) launch_slim_fix(P, minb, s);
+            if (slim) launch_slim_fix(P, proj, s);
             else if (proj) launch_fixup_proj(P, s);
             else launch_fixup(P, PIN, s);
             SCI_LAUNCHED("k_tv_fixup");
@@ -373,14 +386,15 @@ int tv_launch(const float *f, float *u, float *resid, int64_t nf, int64_t H, int
 
 // The on-load projection path covers one measurement of <= 32 frames with a
 // packed mask, 2..5 Chambolle steps (one pass) and 16-byte aligned rows.
-// It is opt-in (SCI_FUSED_PROJ=1): measured at 2048 x 2048 x 24 the fused
-// TV pass (552 us) costs more than the plain pass plus the separate
-// projection saves (385 + 179 us vs 552 + 73 us), because the extra loads
-// and registers slow the register-limited pipeline.
+// On by default (SCI_FUSED_PROJ=0 turns it off): with the lean TV pass,
+// whose input rows come through shared-memory rings, the projection costs
+// the pass little, and the iteration at 2048 x 2048 x 24 goes from 2123 to
+// 2180-2187 iter/s (residual pass 73 us instead of the 141 us projection).
+// With the generic pipeline it was slower (552 + 73 us against 385 + 179).
 bool tv_proj_supported(int64_t nf, int64_t W, int K) {
     const char *e = getenv("SCI_FUSED_PROJ");
-    return e && atoi(e) != 0 && nf <= 32 && K >= 2 && K <= tv::SMAX + 1 && W % 4 == 0 &&
-           !getenv("SCI_TV_CPL") && !getenv("SCI_TV_LAG");
+    return !(e && atoi(e) == 0) && slim_enabled() && nf <= 32 && K >= 2 &&
+           K <= tv::SMAX + 1 && W % 4 == 0 && !getenv("SCI_TV_LAG");
 }
 
 size_t tv_workspace_bytes(int64_t nf, int64_t H, int64_t W, int K) {

@@ -920,11 +920,12 @@ void launch_rule_impl(const Pass &P, int SG, bool pin, bool final_pass, cudaStre
 #undef SCI_RULE_CASE
 }
 void launch_fixup(const Pass &P, bool pin, cudaStream_t s);
-// Register-lean single-pass kernels (sci_tv_slim.cu); minb: 3 or 4 resident
-// blocks per SM (the register budget).
-void launch_slim(const Pass &P, int SG, int minb, cudaStream_t s);
-void launch_slim_fix(const Pass &P, int minb, cudaStream_t s);
-int slim_resident_blocks(int SG, int minb);  // resident blocks per SM of the main kernel
+// Register-lean single-pass kernels (sci_tv_slim.cu, P.cpl = 2 or 4); minb:
+// the resident blocks per SM their registers are sized for (0: default);
+// proj: the GAP projection applied on load.
+void launch_slim(const Pass &P, int SG, int minb, bool proj, cudaStream_t s);
+void launch_slim_fix(const Pass &P, bool proj, cudaStream_t s);
+int slim_resident_blocks(int cpl, int SG, int minb, bool proj);  // of the main kernel
 
 inline unsigned pass_blocks(const Pass &P) {
     const int64_t items = (int64_t)P.nbands * P.nchunks * P.nf;

@@ -1,60 +1,53 @@
-// Launchers of the register-lean Chambolle TV pass (sci_tv_slim.cuh).
-#include <mutex>
+// Register-lean TV pass (sci_tv_slim.cuh), 4 columns per lane; the host
+// entry points for both column widths.
+#include <cstdlib>
 
-#include "sci_tv_slim.cuh"
+#include "sci_tv_slim_launch.cuh"
 
 namespace sci {
 namespace tv {
 
-template <int MINB>
-static void launch_minb(const Pass &P, int SG, cudaStream_t s) {
-    const unsigned g = pass_blocks(P);
-    switch (SG) {
-        case 1: slim::k_tv_slim<1, MINB><<<g, WPB * 32, 0, s>>>(P); break;
-        case 2: slim::k_tv_slim<2, MINB><<<g, WPB * 32, 0, s>>>(P); break;
-        case 3: slim::k_tv_slim<3, MINB><<<g, WPB * 32, 0, s>>>(P); break;
-        default: slim::k_tv_slim<4, MINB><<<g, WPB * 32, 0, s>>>(P); break;
+void launch_slim2(const Pass &P, int SG, int minb, bool proj, cudaStream_t s);  // sci_tv_slim2.cu
+void launch_slim2_fix(const Pass &P, bool proj, cudaStream_t s);
+int slim2_resident_blocks(int SG, int minb, bool proj);
+
+void launch_slim(const Pass &P, int SG, int minb, bool proj, cudaStream_t s) {
+    using namespace slim;
+    if (P.cpl == 2) return launch_slim2(P, SG, minb, proj, s);
+    // SCI_TV_FORM=1: the dual field held as 4 p (n_iter_max = 5, 4 columns
+    // per lane at 128 registers)
+    const char *e = getenv("SCI_TV_FORM");
+    const int form = (e && atoi(e) == 1) ? 1 : 0;
+    if (minb == 3) {
+        if (proj) launch_main<4, 3, 1>(P, SG, s);
+        else launch_main<4, 3, 0>(P, SG, s);
+    } else {
+        if (proj) launch_main<4, 4, 1>(P, SG, s, form);
+        else launch_main<4, 4, 0>(P, SG, s, form);
     }
 }
 
-void launch_slim(const Pass &P, int SG, int minb, cudaStream_t s) {
-    if (minb == 3) launch_minb<3>(P, SG, s);
-    else launch_minb<4>(P, SG, s);
+void launch_slim_fix(const Pass &P, bool proj, cudaStream_t s) {
+    using namespace slim;
+    if (P.cpl == 2) return launch_slim2_fix(P, proj, s);
+    constexpr int D = MinB<4>::def;
+    if (proj) k_tv_slim_fix<4, D, 1><<<pass_blocks(P), WPB * 32, 0, s>>>(P);
+    else k_tv_slim_fix<4, D, 0><<<pass_blocks(P), WPB * 32, 0, s>>>(P);
 }
 
-void launch_slim_fix(const Pass &P, int minb, cudaStream_t s) {
-    if (minb == 3) slim::k_tv_slim_fix<3><<<pass_blocks(P), WPB * 32, 0, s>>>(P);
-    else slim::k_tv_slim_fix<4><<<pass_blocks(P), WPB * 32, 0, s>>>(P);
-}
-
-template <int MINB>
-static const void *kernel_of(int SG) {
-    switch (SG) {
-        case 1: return reinterpret_cast<const void *>(&slim::k_tv_slim<1, MINB>);
-        case 2: return reinterpret_cast<const void *>(&slim::k_tv_slim<2, MINB>);
-        case 3: return reinterpret_cast<const void *>(&slim::k_tv_slim<3, MINB>);
-        default: return reinterpret_cast<const void *>(&slim::k_tv_slim<4, MINB>);
-    }
-}
-
-// Queried once per (SG, minb) on the current device; the grid sizing
-// falls back to minb blocks per SM if the query fails.
-int slim_resident_blocks(int SG, int minb) {
+int slim_resident_blocks(int cpl, int SG, int minb, bool proj) {
+    using namespace slim;
+    if (cpl == 2) return slim2_resident_blocks(SG, minb, proj);
     static std::mutex mu;
-    static int cache[2][5] = {};
-    const int mi = minb == 3 ? 0 : 1;
+    static int cache[2][2][5] = {};
     SG = SG < 1 ? 1 : (SG > 4 ? 4 : SG);
+    const int mi = minb == 3 ? 0 : 1;
     std::lock_guard<std::mutex> lock(mu);
-    int &v = cache[mi][SG];
+    int &v = cache[mi][proj ? 1 : 0][SG];
     if (v == 0) {
-        int n = 0;
-        const void *k = minb == 3 ? kernel_of<3>(SG) : kernel_of<4>(SG);
-        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, k, WPB * 32, 0) != cudaSuccess ||
-            n <= 0) {
-            cudaGetLastError();
-            n = minb;
-        }
-        v = n;
+        const void *k = minb == 3 ? (proj ? main_kernel<4, 3, 1>(SG) : main_kernel<4, 3, 0>(SG))
+                                  : (proj ? main_kernel<4, 4, 1>(SG) : main_kernel<4, 4, 0>(SG));
+        v = resident(k, minb == 3 ? 3 : 4);
     }
     return v;
 }

@@ -1,0 +1,51 @@
+// Register-lean TV pass (sci_tv_slim.cuh), 2 columns per lane.
+#include "sci_tv_slim_launch.cuh"
+
+namespace sci {
+namespace tv {
+
+void launch_slim2(const Pass &P, int SG, int minb, bool proj, cudaStream_t s) {
+    using namespace slim;
+    switch (minb) {
+        case 5:
+            if (proj) launch_main<2, 5, 1>(P, SG, s);
+            else launch_main<2, 5, 0>(P, SG, s);
+            break;
+        case 7:
+            if (proj) launch_main<2, 7, 1>(P, SG, s);
+            else launch_main<2, 7, 0>(P, SG, s);
+            break;
+        default:
+            if (proj) launch_main<2, 6, 1>(P, SG, s);
+            else launch_main<2, 6, 0>(P, SG, s);
+            break;
+    }
+}
+
+void launch_slim2_fix(const Pass &P, bool proj, cudaStream_t s) {
+    using namespace slim;
+    constexpr int D = MinB<2>::def;
+    if (proj) k_tv_slim_fix<2, D, 1><<<pass_blocks(P), WPB * 32, 0, s>>>(P);
+    else k_tv_slim_fix<2, D, 0><<<pass_blocks(P), WPB * 32, 0, s>>>(P);
+}
+
+int slim2_resident_blocks(int SG, int minb, bool proj) {
+    using namespace slim;
+    static std::mutex mu;
+    static int cache[3][2][5] = {};
+    SG = SG < 1 ? 1 : (SG > 4 ? 4 : SG);
+    const int mi = minb == 5 ? 0 : (minb == 7 ? 2 : 1);
+    std::lock_guard<std::mutex> lock(mu);
+    int &v = cache[mi][proj ? 1 : 0][SG];
+    if (v == 0) {
+        const void *k;
+        if (mi == 0) k = proj ? main_kernel<2, 5, 1>(SG) : main_kernel<2, 5, 0>(SG);
+        else if (mi == 2) k = proj ? main_kernel<2, 7, 1>(SG) : main_kernel<2, 7, 0>(SG);
+        else k = proj ? main_kernel<2, 6, 1>(SG) : main_kernel<2, 6, 0>(SG);
+        v = resident(k, mi == 0 ? 5 : (mi == 2 ? 7 : 6));
+    }
+    return v;
+}
+
+}  // namespace tv
+}  // namespace sci

@@ -28,7 +28,7 @@ class Solver:
 
     def __init__(self, op, projmeth="gap", iters=50, lambdas=1.0, tv_weight=0.1,
                  tv_iter_max=5, eps=2e-4, accelerate=True, gamma=0.01, gammas=None,
-                 use_graph=True, use_bits=True, tvm="tv_chambolle"):
+                 use_graph=True, use_bits=True, tvm="tv_chambolle", resid_norm=False):
         if projmeth not in ("gap", "admm"):
             raise ValueError("Unsupported projection method %s" % projmeth)
         self.op = op
@@ -58,6 +58,11 @@ class Solver:
         o.sqerr = None
         o.tv_steps = None
         o.use_graph = 1 if use_graph else 0
+        # FP64 ||r_k||^2 of every iteration's projection residual, on the
+        # device (see resid_norms)
+        self.resid_norm = (torch.zeros(self.iters, dtype=torch.float64, device=op.dev)
+                           if resid_norm else None)
+        o.resid_norm = self.resid_norm.data_ptr() if resid_norm else None
         n = ctypes.c_size_t()
         call("sci_solver_workspace_bytes", self.B, self.H, self.W, ctypes.byref(o),
              ctypes.byref(n))
@@ -96,6 +101,16 @@ class Solver:
              _dev.ptr(self.bits), ps.data_ptr(), x0.data_ptr(), x.data_ptr(), self.B, self.H,
              self.W, ctypes.byref(o), self.ws.data_ptr(), self.ws.numel(), _dev.stream_handle())
         return x
+
+    def resid_norms(self):
+        """||r_k||^2 per iteration of the last run (float64 numpy): the
+        squared L2 norm of the projection residual r = (y1 - A x) / Phi_sum
+        (GAP_acc), (y - A x) / Phi_sum (GAP) or (y - A(theta + b)) /
+        (Phi_sum + gamma) (ADMM), summed in FP64 on the GPU.  Needs
+        ``resid_norm=True`` at construction."""
+        if self.resid_norm is None:
+            raise ValueError("Solver(..., resid_norm=True) records the residual norms")
+        return self.resid_norm.cpu().numpy()
 
     def psnr_all(self):
         """Per-iteration PSNR of the last run with ``orig`` (utils.py:28-36)."""

@@ -193,4 +193,8 @@ def main(ref_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SCI_REFERENCE_ROOT", "/root/reference"))
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("SCI_REFERENCE_ROOT")
+    if not root:
+        sys.exit("usage: %s REFERENCE_ROOT  (or set SCI_REFERENCE_ROOT): the root of the "
+                 "reference checkout, the directory holding PnP_SCI/" % sys.argv[0])
+    main(root)

@@ -209,21 +209,68 @@ def test_run_host_many_pipelined():
 
 @pytest.mark.parametrize("eps", [2e-4, 0.05])
 @pytest.mark.parametrize("iters", [7, 8])
-def test_fused_projection_path_is_bitwise_equal(monkeypatch, eps, iters):
+@pytest.mark.parametrize("shape,cpl", [((64, 96, 8), None), ((40, 1040, 6), None),
+                                       ((70, 520, 12), "2"), ((33, 1032, 5), "4"),
+                                       ((64, 96, 8), "4")])
+def test_fused_projection_path_is_bitwise_equal(monkeypatch, eps, iters, shape, cpl):
     """The fused iteration (residual map + projection applied while the TV
     kernel loads x) against the two-kernel iteration, including early stops
-    of the TV inside the fused kernel (eps = 0.05)."""
-    orig, mask, meas = sci.datasets.video_config(64, 96, 8)
+    of the TV inside the fused kernel (eps = 0.05), on 2 and 4 columns per
+    lane of the lean TV pass."""
+    if cpl is not None:
+        monkeypatch.setenv("SCI_TV_CPL", cpl)
+    orig, mask, meas = sci.datasets.video_config(*shape)
     op = sci.MaskOperator(mask)
     y = _dev.plane(meas)
     monkeypatch.setenv("SCI_FUSED_PROJ", "1")
     fused = sci.Solver(op, "gap", iters, 1.0, 0.1, 5, eps=eps, use_graph=False)
     a = fused.run(y, tv_steps=True).clone()
     sa = fused.tv_steps.clone()
-    monkeypatch.delenv("SCI_FUSED_PROJ")
+    monkeypatch.setenv("SCI_FUSED_PROJ", "0")
     plain = sci.Solver(op, "gap", iters, 1.0, 0.1, 5, eps=eps, use_graph=False)
     b = plain.run(y, tv_steps=True).clone()
     assert torch.equal(a, b)
     assert torch.equal(sa, plain.tv_steps)
     if eps > 0.01:
         assert int((sa < 5).sum()) > 0  # the stop test fired somewhere
+
+
+@pytest.mark.parametrize("kind,acc,bits,fused", [
+    ("gap", True, True, False), ("gap", False, True, False), ("gap", True, False, False),
+    ("gap", True, True, True), ("gap", False, True, True), ("admm", True, True, False),
+    ("admm", True, False, False)])
+def test_projection_residual_norm_matches_oracle(monkeypatch, kind, acc, bits, fused):
+    """The FP64 ||r_k||^2 of every iteration's projection residual, summed by
+    the projection kernels (bulk-copy staged, per-thread, fused residual
+    pass; packed and float masks), against the float64 oracle's value of the
+    same residual map (pnp_sci_algo.py:640-645 for GAP, :808-809 for ADMM)
+    on its own trajectory: the two trajectories differ by float32 rounding,
+    so 1e-4 relative."""
+    monkeypatch.setenv("SCI_FUSED_PROJ", "1" if fused else "0")
+    H, W, B, iters = 64, 96, 8, 10
+    orig, mask, meas = sci.datasets.video_config(H, W, B, noise_rel=0.01)
+    msum = mask.sum(axis=2)
+    msum[msum == 0] = 1
+    op = sci.MaskOperator(mask)
+    y = _dev.plane(meas)
+    s = sci.Solver(op, kind, iters, 1.0, 0.1, 5, accelerate=acc, resid_norm=True,
+                   use_bits=bits)
+    s.run(y)
+    rn = s.resid_norms()
+    ref = []
+    A = lambda v: port.A_(v, mask)       # noqa: E731
+    At = lambda r: port.At_(r, mask)     # noqa: E731
+    if kind == "gap":
+        port.gap_denoise(meas, msum, A, At, _lambda=1, accelerate=acc, iter_max=iters,
+                         tv_weight=0.1, tv_iter_max=5, x0=At(meas), show_iqa=False, resid=ref)
+    else:
+        port.admm_denoise(meas, msum, A, At, _lambda=1, gamma=0.01, iter_max=iters,
+                          tv_weight=0.1, tv_iter_max=5, x0=At(meas), show_iqa=False,
+                          resid=ref)
+    assert len(ref) == iters
+    np.testing.assert_allclose(rn, ref, rtol=1e-4)
+    # without the option the solver records nothing and computes the same x
+    plain = sci.Solver(op, kind, iters, 1.0, 0.1, 5, accelerate=acc, use_bits=bits)
+    assert torch.equal(plain.run(y), s.x)
+    with pytest.raises(ValueError):
+        plain.resid_norms()

@@ -137,9 +137,11 @@ def _tv_env(monkeypatch, fp, weight, K, eps, slim, R=None):
     return u, steps.cpu().numpy(), energy.cpu().numpy()
 
 
-@pytest.mark.parametrize("H,W,F", SLIM_SHAPES)
+@pytest.mark.parametrize("H,W,F", SLIM_SHAPES + [(64, 256, 3), (37, 62, 2), (300, 500, 2)])
 @pytest.mark.parametrize("K", [2, 3, 4, 5])
-def test_tv_slim_bitwise_equals_generic(H, W, F, K, monkeypatch):
+@pytest.mark.parametrize("cpl", ["2", "4"])
+def test_tv_slim_bitwise_equals_generic(H, W, F, K, cpl, monkeypatch):
+    monkeypatch.setenv("SCI_TV_CPL", cpl)
     f = smooth_frames(H, W, F, seed=7 * H + W + K)
     fp = _dev.planar(f)
     u0, s0, e0 = _tv_env(monkeypatch, fp, 0.1, K, 2e-4, "0")
@@ -176,13 +178,18 @@ def test_tv_slim_row_chunks_and_early_stop(R, monkeypatch):
         assert np.max(np.abs(_dev.unplanar(u1, f) - ref)) < ATOL
 
 
-def test_tv_slim_occupancy_variants(monkeypatch):
-    # the 3- and 4-blocks-per-SM builds of the lean kernel agree bit for bit
+@pytest.mark.parametrize("cpl,minbs", [("4", ("3", "4")), ("2", ("5", "6", "7"))])
+def test_tv_slim_occupancy_variants(cpl, minbs, monkeypatch):
+    # the register budgets of the lean kernel agree bit for bit
+    monkeypatch.setenv("SCI_TV_CPL", cpl)
     f = smooth_frames(96, 2048, 3, seed=3)
     fp = _dev.planar(f)
-    monkeypatch.setenv("SCI_SLIM_MINB", "3")
-    u3, s3, _ = _tv_env(monkeypatch, fp, 0.1, 5, 2e-4, "1")
-    monkeypatch.setenv("SCI_SLIM_MINB", "4")
-    u4, s4, _ = _tv_env(monkeypatch, fp, 0.1, 5, 2e-4, "1")
-    assert torch.equal(u3, u4)
-    assert list(s3) == list(s4)
+    outs = []
+    for mb in minbs:
+        monkeypatch.setenv("SCI_SLIM_MINB", mb)
+        for form in ("0", "1"):  # the dual field as p or as 4 p
+            monkeypatch.setenv("SCI_TV_FORM", form)
+            outs.append(_tv_env(monkeypatch, fp, 0.1, 5, 2e-4, "1"))
+    for u, s, _ in outs[1:]:
+        assert torch.equal(outs[0][0], u)
+        assert list(outs[0][1]) == list(s)
