@@ -311,11 +311,12 @@ void build_table(const sci_batch_item *items, int n, int K, float eps, char *ws,
         for (int par = 0; par < 2; ++par) {
             tv::Pass &Q = I.tvq[par];
             Q = P;
+            // halos of 4 columns for either width, so that a lane pair's
+            // 16-byte copies (2 columns per lane) start on 16-byte columns
             const int cpl = s.cpl == 2 ? 2 : 4;
-            const int ru = (P.S + cpl - 1) / cpl * cpl;
             Q.cpl = cpl;
-            Q.hl = ru;
-            Q.own = 32 * cpl - 2 * ru;
+            Q.hl = 4;
+            Q.own = 32 * cpl - 8;
             Q.nbands = (int)((s.W + Q.own - 1) / Q.own);
             Q.energy = reinterpret_cast<double *>(ws + L.energy +
                                                   (par ? L.item_e1[i] : L.item_e[i]));
@@ -367,6 +368,10 @@ int enqueue(const Table &T, Table *dT, const Layout &L, char *ws, int n, int ite
     for (int i = 0; i < n; ++i)
         if (accelerate) SCI_CUDA(cudaMemsetAsync(T.it[i].y1, 0, 4 * T.it[i].hw, s));
     if (queue_enabled()) {
+        // the items' stop decisions and tickets: a ticket counts the TV
+        // tasks of an iteration and is reset by the last one, so it starts
+        // at zero once per solve
+        SCI_CUDA(cudaMemsetAsync(ws + L.stop, 0, L.queue - L.stop, s));
         Queue *dQ = reinterpret_cast<Queue *>(ws + L.queue);
         const int m = per_launch > 0 ? per_launch : std::max(1, iters);
         const int blocks = queue_blocks();

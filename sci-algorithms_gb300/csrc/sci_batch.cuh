@@ -69,7 +69,10 @@ __device__ __forceinline__ bool wait_count(Queue *Q, const unsigned *cnt, unsign
             if (ns < 1024) ns <<= 1;
         }
     }
-    return __shfl_sync(0xffffffffu, ok, 0) != 0;
+    ok = __shfl_sync(0xffffffffu, ok, 0);
+    // the lanes' loads after the wait are ordered after lane 0's acquire
+    __syncwarp();
+    return ok != 0;
 }
 
 __device__ __forceinline__ int find_item(const int *prefix, int n, int g) {

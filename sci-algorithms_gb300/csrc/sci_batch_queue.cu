@@ -47,9 +47,11 @@ __device__ __forceinline__ float bitf(uint32_t w, int b) { return ((w >> b) & 1u
 // GAP projection of one 128-pixel tile of item I (4 pixels per lane), the
 // arithmetic of k_proj_gap_tma: yb = sum_b phi_b x_b in frame order, ACC:
 // y1 += y - yb, r = (y1 - yb) / Phi_sum, else r = (y - yb) / Phi_sum;
-// xp_b = x_b + lam (r phi_b).  The second sweep over x reads the tile back
-// from L1.  Tile 0 also clears the energy sums the item's TV pass of this
-// iteration adds to.
+// xp_b = x_b + lam (r phi_b).  Tile 0 also clears the energy sums the
+// item's TV pass of this iteration adds to.
+// x and y1 were written earlier in this launch by warps on other SMs: they
+// are read at L2 (ld.global.cg), never through the non-coherent or L1
+// caches, which may still hold the lines of an earlier iteration.
 template <bool ACC>
 __device__ __forceinline__ void proj_task(const Item &I, const tv::Pass &P, int tile, int lane) {
     if (tile == 0) {
@@ -64,7 +66,7 @@ __device__ __forceinline__ void proj_task(const Item &I, const tv::Pass &P, int 
     float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll 8
     for (int b = 0; b < B; ++b) {
-        const float4 v = ldg4(I.x + b * hw + p);
+        const float4 v = __ldcg(reinterpret_cast<const float4 *>(I.x + b * hw + p));
         s.x = fmaf(v.x, bitf(w.x, b), s.x);
         s.y = fmaf(v.y, bitf(w.y, b), s.y);
         s.z = fmaf(v.z, bitf(w.z, b), s.z);
@@ -73,7 +75,7 @@ __device__ __forceinline__ void proj_task(const Item &I, const tv::Pass &P, int 
     const float4 yv = ldg4(I.y + p), ps = ldg4(I.phisum + p);
     float4 r;
     if (ACC) {
-        float4 tt = *reinterpret_cast<const float4 *>(I.y1 + p);
+        float4 tt = __ldcg(reinterpret_cast<const float4 *>(I.y1 + p));
         tt.x = tt.x + (yv.x - s.x);
         tt.y = tt.y + (yv.y - s.y);
         tt.z = tt.z + (yv.z - s.z);
@@ -88,7 +90,7 @@ __device__ __forceinline__ void proj_task(const Item &I, const tv::Pass &P, int 
     const float lam = I.lam;
 #pragma unroll 8
     for (int b = 0; b < B; ++b) {
-        const float4 v = ldg4(I.x + b * hw + p);
+        const float4 v = __ldcg(reinterpret_cast<const float4 *>(I.x + b * hw + p));
         float4 o;
         o.x = fmaf(lam, r.x * bitf(w.x, b), v.x);
         o.y = fmaf(lam, r.y * bitf(w.y, b), v.y);
@@ -106,27 +108,27 @@ __device__ __forceinline__ void tv_task(const tv::Pass &P, int frame, int chunk,
                                         const tv::slim::Rings &G2) {
     using namespace tv::slim;
     if (!FIX) {
-        if (P.cpl == 2) srun_mode<S, 2, true, 0>(P, frame, chunk, band, lane, G2);
-        else srun_mode<S, 4, true, 0>(P, frame, chunk, band, lane, G4);
+        if (P.cpl == 2) srun_mode<S, 2, true, 0, 0, 1>(P, frame, chunk, band, lane, G2);
+        else srun_mode<S, 4, true, 0, 0, 1>(P, frame, chunk, band, lane, G4);
         return;
     }
-    const int j = P.stopj[frame];
+    const int j = __ldcg(P.stopj + frame);  // decided by another warp of this launch
     if (j < 1 || j >= S) return;
     switch (j) {
         case 1:
-            if (P.cpl == 2) srun_mode<1, 2, false, 0>(P, frame, chunk, band, lane, G2);
-            else srun_mode<1, 4, false, 0>(P, frame, chunk, band, lane, G4);
+            if (P.cpl == 2) srun_mode<1, 2, false, 0, 0, 1>(P, frame, chunk, band, lane, G2);
+            else srun_mode<1, 4, false, 0, 0, 1>(P, frame, chunk, band, lane, G4);
             break;
         case 2:
             if constexpr (S > 2) {
-                if (P.cpl == 2) srun_mode<2, 2, false, 0>(P, frame, chunk, band, lane, G2);
-                else srun_mode<2, 4, false, 0>(P, frame, chunk, band, lane, G4);
+                if (P.cpl == 2) srun_mode<2, 2, false, 0, 0, 1>(P, frame, chunk, band, lane, G2);
+                else srun_mode<2, 4, false, 0, 0, 1>(P, frame, chunk, band, lane, G4);
             }
             break;
         default:
             if constexpr (S > 3) {
-                if (P.cpl == 2) srun_mode<3, 2, false, 0>(P, frame, chunk, band, lane, G2);
-                else srun_mode<3, 4, false, 0>(P, frame, chunk, band, lane, G4);
+                if (P.cpl == 2) srun_mode<3, 2, false, 0, 0, 1>(P, frame, chunk, band, lane, G2);
+                else srun_mode<3, 4, false, 0, 0, 1>(P, frame, chunk, band, lane, G4);
             }
             break;
     }

@@ -136,15 +136,29 @@ struct Rings {
 };
 
 // Copies input row `row` into ring slot `slot` of every ring of the lane.
-template <int CPL, int PROJ>
+// COH (coherent): the rows may have been written earlier in the same launch
+// by other SMs, so every copy goes through L2 only (cp.async.cg): with 2
+// columns per lane the even lane of each pair copies both lanes' 16 bytes
+// (ldb: the pair's bytes inside the frame) and sstep synchronises the warp.
+template <int CPL, int PROJ, int COH = 0>
 __device__ __forceinline__ void fetch(const Pass &P, const Rings &G, const float *fb, int slot,
                                       int row, int colc, uint32_t ldb) {
     const int64_t o = (int64_t)row * P.W + colc;
     const uint32_t so = (uint32_t)(slot & (RING - 1)) * Geo<CPL>::ROWB;
-    cp_row<CPL>(G.xs + so, fb + o, ldb);
-    if (PROJ) {
-        cp_row<CPL>(G.cs + so, P.cmap + o, ldb);
-        cp_row<CPL>(G.ms + so, P.bits + o, ldb);
+    if (COH && CPL == 2) {
+        if ((threadIdx.x & 1) == 0) {
+            cp_row<4>(G.xs + so, fb + o, ldb);
+            if (PROJ) {
+                cp_row<4>(G.cs + so, P.cmap + o, ldb);
+                cp_row<4>(G.ms + so, P.bits + o, ldb);
+            }
+        }
+    } else {
+        cp_row<CPL>(G.xs + so, fb + o, ldb);
+        if (PROJ) {
+            cp_row<CPL>(G.cs + so, P.cmap + o, ldb);
+            cp_row<CPL>(G.ms + so, P.bits + o, ldb);
+        }
     }
     cp_commit();
 }
@@ -272,22 +286,23 @@ __device__ __forceinline__ void stages(const Pass &P, const SS<S, CPL> &in, SS<S
 }
 
 // One pipeline step: input row r enters, stage k handles row r - k.
-template <int S, int CPL, bool ENERGY, int MODE, bool GEN, int PROJ, int FORM = 0>
+template <int S, int CPL, bool ENERGY, int MODE, bool GEN, int PROJ, int FORM = 0, int COH = 0>
 __device__ __forceinline__ void sstep(const Pass &P, const SS<S, CPL> &in, SS<S, CPL> &out,
                                       int r, int rs, int r0, int r1, const SLane<CPL> &L,
                                       const float *fb, float *ob, const Rings &G, uint32_t ldb,
                                       int frame, f2 (&ek)[S]) {
     // copy input row r + PF into its ring slots (clamped into the frame; a
     // clamped row is never read), then wait for row r
-    fetch<CPL, PROJ>(P, G, fb, r + PF, min(r + PF, P.H - 1), L.colc, ldb);
+    fetch<CPL, PROJ, COH>(P, G, fb, r + PF, min(r + PF, P.H - 1), L.colc, ldb);
     cp_wait<PF>();
+    if (COH && CPL == 2) __syncwarp();  // the pair's copy was the even lane's
     Row<CPL> ucur = (!GEN || r < P.H) ? stage0<CPL, PROJ>(P, G, r, frame) : zrow<CPL>();
     stages<S, 1, CPL, ENERGY, MODE, GEN, FORM>(P, in, out, ucur, r, rs, r0, r1, L, ob, G, ek);
 }
 
 // One work item: frame, row chunk, column band.  Requires rows aligned for
 // CPL-wide access (W % CPL == 0, base pointers aligned to 4 CPL bytes).
-template <int S, int CPL, bool ENERGY, int MODE, int PROJ, int FORM = 0>
+template <int S, int CPL, bool ENERGY, int MODE, int PROJ, int FORM = 0, int COH = 0>
 __device__ __forceinline__ void srun(const Pass &P, int frame, int chunk, int band, int lane,
                                      const Rings &G) {
     const int H = P.H, W = P.W;
@@ -308,15 +323,19 @@ __device__ __forceinline__ void srun(const Pass &P, int frame, int chunk, int ba
         }
     }
     // columns outside the frame read as zeros (W % CPL == 0: all or none)
-    const uint32_t ldb = (L.col >= 0 && L.col < W) ? 4u * CPL : 0u;
+    uint32_t ldb = (L.col >= 0 && L.col < W) ? 4u * CPL : 0u;
     L.colc = min(max(L.col, 0), W - CPL);
+    if (COH && CPL == 2) {  // a coherent pair copy: the pair's columns inside the frame
+        ldb = (L.col >= 0 && L.col < W) ? 4u * (uint32_t)min(4, W - L.col) : 0u;
+        L.colc = min(max(L.col, 0), W - 4);
+    }
     const float *fb = P.f + (int64_t)frame * P.fs;
     float *ob = P.u + (int64_t)frame * P.fs;
 
     // the first PF input rows
 #pragma unroll
     for (int q = 0; q < PF; ++q)
-        fetch<CPL, PROJ>(P, G, fb, rs + q, min(rs + q, H - 1), L.colc, ldb);
+        fetch<CPL, PROJ, COH>(P, G, fb, rs + q, min(rs + q, H - 1), L.colc, ldb);
 
     SS<S, CPL> A, B;
     zero_ss<S, CPL>(A);
@@ -332,14 +351,14 @@ __device__ __forceinline__ void srun(const Pass &P, int frame, int chunk, int ba
     while (r <= rlast) {
         if (r == rfb && r + 1 <= rfe) {
             for (; r + 1 <= rfe; r += 2) {
-                sstep<S, CPL, ENERGY, MODE, false, PROJ, FORM>(P, A, B, r, rs, r0, r1, L, fb, ob, G,
+                sstep<S, CPL, ENERGY, MODE, false, PROJ, FORM, COH>(P, A, B, r, rs, r0, r1, L, fb, ob, G,
                                                          ldb, frame, ek);
-                sstep<S, CPL, ENERGY, MODE, false, PROJ, FORM>(P, B, A, r + 1, rs, r0, r1, L, fb, ob,
+                sstep<S, CPL, ENERGY, MODE, false, PROJ, FORM, COH>(P, B, A, r + 1, rs, r0, r1, L, fb, ob,
                                                          G, ldb, frame, ek);
             }
             continue;
         }
-        sstep<S, CPL, ENERGY, MODE, true, PROJ, FORM>(P, A, B, r, rs, r0, r1, L, fb, ob, G, ldb, frame,
+        sstep<S, CPL, ENERGY, MODE, true, PROJ, FORM, COH>(P, A, B, r, rs, r0, r1, L, fb, ob, G, ldb, frame,
                                                 ek);
         A = B;
         ++r;
@@ -361,14 +380,14 @@ __device__ __forceinline__ void srun(const Pass &P, int frame, int chunk, int ba
     }
 }
 
-template <int S, int CPL, bool ENERGY, int PROJ, int FORM = 0>
+template <int S, int CPL, bool ENERGY, int PROJ, int FORM = 0, int COH = 0>
 __device__ __forceinline__ void srun_mode(const Pass &P, int frame, int chunk, int band, int lane,
                                           const Rings &G) {
     const int c0 = band * P.own - P.hl;
     if (c0 >= 0 && c0 + 32 * CPL - 1 <= P.W - 1)
-        srun<S, CPL, ENERGY, INTERIOR, PROJ, FORM>(P, frame, chunk, band, lane, G);
+        srun<S, CPL, ENERGY, INTERIOR, PROJ, FORM, COH>(P, frame, chunk, band, lane, G);
     else
-        srun<S, CPL, ENERGY, EDGE, PROJ, FORM>(P, frame, chunk, band, lane, G);
+        srun<S, CPL, ENERGY, EDGE, PROJ, FORM, COH>(P, frame, chunk, band, lane, G);
 }
 
 // Shared memory of a block: RING rows per warp per ring (one ring, three

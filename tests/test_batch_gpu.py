@@ -43,11 +43,13 @@ def test_batch_matches_single_solver(autotune):
 
 @pytest.mark.parametrize("accelerate", [True, False])
 def test_batch_bulk_copy_projection_is_bitwise_equal(monkeypatch, accelerate):
-    """The bulk-copy staged batch projection (the default) against the
-    per-thread shared-memory kernel: identical results after 6 iterations."""
+    """The per-phase launches' bulk-copy staged batch projection against
+    their per-thread shared-memory kernel: identical results after 6
+    iterations."""
     shapes = [(64, 64, 8, 0.5), (40, 48, 4, 0.7), (33, 200, 32, 0.45), (96, 256, 12, 0.6),
               (300, 260, 24, 0.5)]
     data = make_items(shapes, seed=5)
+    monkeypatch.setenv("SCI_BATCH_QUEUE", "0")
     runs = []
     for tma in ("1", "0"):
         monkeypatch.setenv("SCI_PROJ_TMA", tma)
