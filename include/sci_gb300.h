@@ -292,14 +292,15 @@ typedef struct sci_batch_item {
 int sci_batch_workspace_bytes(const sci_batch_item *items, int n, int tv_iter_max,
                               size_t *bytes);
 
-/* Autotuner of the batched solve.  (1) Per distinct (B, H, W), times the TV
- * pass on the item's own data for each column width (2 or 4 columns per
- * lane) and row-chunk height and writes the fastest into items[i].cpl and
- * items[i].R (cached per process).  (2) With a non-null iters_per_launch,
- * times a few iterations of the whole batch for several iterations per
- * persistent launch and writes the fastest (0: all in one launch); this
- * solves the batch from x0 = At(y / phisum), overwriting every item's x.
- * Synchronises the stream. */
+/* Autotuner of the batched solve: times candidate tilings on a few
+ * iterations of the batch's own solve (from x0 = At(y / phisum), overwriting
+ * every item's x) -- row-chunk heights of 1/2, 1 and 2 times the default for
+ * each item's height, and 4 columns per lane for every item or 2 for items
+ * at most 256 columns wide -- and writes the fastest into items[i].R and
+ * items[i].cpl; with a non-null iters_per_launch it then times 1, 2 or 3
+ * iterations per persistent launch against all of them and writes the
+ * fastest (0: all in one launch).  Cached per process for the list of
+ * shapes.  Synchronises the stream. */
 int sci_batch_autotune(sci_batch_item *items, int n, int iters, int tv_iter_max,
                        float eps, int accelerate, int *iters_per_launch,
                        void *workspace, size_t workspace_bytes, void *stream);

@@ -33,9 +33,6 @@ __device__ unsigned int g_batch_status;
 int tv_launch(const float *f, float *u, float *resid, int64_t nf, int64_t H, int64_t W,
               int64_t fs, float weight, float eps, int K, int *steps, double *energy_out,
               void *workspace, size_t ws_bytes, cudaStream_t s, int force_R);
-int tv_launch_flags(const float *f, float *u, float *resid, int64_t nf, int64_t H, int64_t W,
-                    int64_t fs, float weight, float eps, int K, int *steps, double *energy_out,
-                    void *workspace, size_t ws_bytes, cudaStream_t s, int force_R, int flags);
 size_t tv_workspace_bytes(int64_t nf, int64_t H, int64_t W, int K);
 
 namespace batch {
@@ -475,21 +472,51 @@ int sci_batch_autotune(sci_batch_item *items, int n, int iters, int tv_iter_max,
     const Layout L = layout(items, n, tv_iter_max);
     SCI_CHECK_ARG(workspace && workspace_bytes >= L.total, "batch: workspace too small");
     SCI_CHECK_ARG(iters >= 0, "batch: iters must be >= 0");
-    char *ws = static_cast<char *>(workspace);
     cudaStream_t s = as_stream(stream);
-    // 1. per distinct (B, H, W): the TV pass of the item's own x into its
-    // projection buffer, for each column width (2 or 4 per lane) and row
-    // chunk height; the fastest pair is cached per process
+    // Every candidate is timed on the batch itself -- a few iterations of its
+    // own solve from x0 = At(y / Phi_sum) (overwriting x), inside the
+    // persistent launch where all items share the GPU -- because a tiling
+    // timed on one item alone ranks differently there (measured on the
+    // 64-item uneven batch: per-shape single-item tuning 185 ms per solve,
+    // the default tiling 138 ms).  Candidates: row-chunk heights of
+    // 1/2, 1 and 2 times the default for each item's height (16..512 rows),
+    // 4 columns per lane for every item or 2 for items at most 256 columns
+    // wide; then, for the best tiling, 1, 2 or 3 iterations per launch
+    // against all of them.  The choice is cached per process for the batch's
+    // list of shapes.
+    const int probe = std::max(1, std::min(iters, 6));
+    std::string key;
+    key_append(key, n, tv_iter_max, probe, accelerate);
+    for (int i = 0; i < n; ++i) key_append(key, items[i].B, items[i].H, items[i].W);
     static std::mutex mu;
-    static std::map<std::tuple<int64_t, int64_t, int64_t, int>, std::pair<int, int>> tuned;
+    static std::map<std::string, std::tuple<int, int, int>> tuned;  // scale x 2, narrow, m
+    auto apply = [&](int scale2, int narrow) {
+        for (int i = 0; i < n; ++i) {
+            const int R = default_R(items[i].H, items[i].W, items[i].B) * scale2 / 2;
+            items[i].R = std::max(16, std::min(512, R));
+            items[i].cpl = (narrow && items[i].W <= 256) ? 2 : 4;
+        }
+    };
+    {
+        std::lock_guard<std::mutex> lk(mu);
+        auto f = tuned.find(key);
+        if (f != tuned.end()) {
+            apply(std::get<0>(f->second), std::get<1>(f->second));
+            if (iters_per_launch) *iters_per_launch = std::get<2>(f->second);
+            return SCI_OK;
+        }
+    }
     cudaEvent_t e0, e1;
     SCI_CUDA(cudaEventCreate(&e0));
     SCI_CUDA(cudaEventCreate(&e1));
-    auto timed = [&](auto &&fn, int reps) -> float {  // the first run warms up
+    int rc = SCI_OK;
+    auto timed = [&](int m) -> float {  // the first run warms up
         float ms = 0.f;
-        for (int rep = 0; rep <= reps; ++rep) {
+        for (int rep = 0; rep <= 2; ++rep) {
             cudaEventRecord(e0, s);
-            if (fn() != SCI_OK) return -1.f;
+            rc = solve(items, n, probe, tv_iter_max, eps, accelerate, 1, 0, m, workspace,
+                       workspace_bytes, s);
+            if (rc != SCI_OK) return -1.f;
             cudaEventRecord(e1, s);
             cudaEventSynchronize(e1);
             float t = 0.f;
@@ -498,78 +525,41 @@ int sci_batch_autotune(sci_batch_item *items, int n, int iters, int tv_iter_max,
         }
         return ms;
     };
-    int rc = SCI_OK;
-    for (int i = 0; i < n && rc == SCI_OK; ++i) {
-        sci_batch_item &it = items[i];
-        const auto key = std::make_tuple(it.B, it.H, it.W, tv_iter_max);
-        {
-            std::lock_guard<std::mutex> lk(mu);
-            auto f = tuned.find(key);
-            if (f != tuned.end()) {
-                it.R = f->second.first;
-                it.cpl = f->second.second;
-                continue;
-            }
-        }
-        float best = 1e30f;
-        int bestR = default_R(it.H, it.W, it.B), bestC = 4;
-        for (int cpl : {4, 2}) {
-            for (int R : {16, 32, 64, 128, 256, 512}) {
-                if (R > 2 * it.H && R != 16) break;
-                const float ms = timed(
-                    [&] {
-                        return tv_launch_flags(it.x, reinterpret_cast<float *>(ws + L.item_xp[i]),
-                                               nullptr, it.B, it.H, it.W, it.H * it.W,
-                                               it.tv_weight, eps, tv_iter_max, nullptr, nullptr,
-                                               ws + L.tvscratch, L.total - L.tvscratch, s, R,
-                                               cpl << 8);
-                    },
-                    2);
-                if (ms < 0.f) {
-                    rc = SCI_ERR_CUDA;
-                    break;
-                }
-                if (ms < best) {
-                    best = ms;
-                    bestR = R;
-                    bestC = cpl;
-                }
-            }
-        }
-        it.R = bestR;
-        it.cpl = bestC;
-        std::lock_guard<std::mutex> lk(mu);
-        tuned[key] = std::make_pair(bestR, bestC);
-    }
-    // 2. iterations per persistent launch of the work queue: the batch's own
-    // solve (from x0 = At(y / Phi_sum), overwriting every item's x) of a few
-    // iterations for each candidate
-    if (rc == SCI_OK && iters_per_launch) {
-        const int probe = std::max(1, std::min(iters, 6));
-        float best = 1e30f;
-        int bestM = 0;
-        for (int m : {0, 1, 2, 3}) {
-            if (m >= probe) continue;
-            const float ms = timed(
-                [&] {
-                    return solve(items, n, probe, tv_iter_max, eps, accelerate, 1, 0, m, ws,
-                                 workspace_bytes, s);
-                },
-                2);
-            if (ms < 0.f) {
-                rc = SCI_ERR_CUDA;
-                break;
-            }
+    float best = 1e30f;
+    int bs = 2, bn = 0, bm = 0;
+    for (int scale2 : {2, 1, 4}) {
+        for (int narrow : {0, 1}) {
+            apply(scale2, narrow);
+            const float ms = timed(0);
+            if (ms < 0.f) break;
             if (ms < best) {
                 best = ms;
-                bestM = m;
+                bs = scale2;
+                bn = narrow;
+            }
+        }
+        if (rc != SCI_OK) break;
+    }
+    apply(bs, bn);
+    if (rc == SCI_OK && iters_per_launch) {
+        for (int m : {1, 2, 3}) {
+            if (m >= probe) continue;
+            const float ms = timed(m);
+            if (ms < 0.f) break;
+            if (ms < best) {
+                best = ms;
+                bm = m;
             }
         }
         // a launch of all `probe` iterations stands for one of all iterations
-        *iters_per_launch = bestM;
+        *iters_per_launch = bm;
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    if (rc == SCI_OK) {
+        std::lock_guard<std::mutex> lk(mu);
+        tuned[key] = std::make_tuple(bs, bn, bm);
+    }
     return rc;
 }
 

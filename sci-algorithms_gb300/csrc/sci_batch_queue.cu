@@ -108,27 +108,27 @@ __device__ __forceinline__ void tv_task(const tv::Pass &P, int frame, int chunk,
                                         const tv::slim::Rings &G2) {
     using namespace tv::slim;
     if (!FIX) {
-        if (P.cpl == 2) srun_mode<S, 2, true, 0, 0, 1>(P, frame, chunk, band, lane, G2);
-        else srun_mode<S, 4, true, 0, 0, 1>(P, frame, chunk, band, lane, G4);
+        if (P.cpl == 2) srun_mode<S, 2, true, 0, 1, 1>(P, frame, chunk, band, lane, G2);
+        else srun_mode<S, 4, true, 0, 1, 1>(P, frame, chunk, band, lane, G4);
         return;
     }
     const int j = __ldcg(P.stopj + frame);  // decided by another warp of this launch
     if (j < 1 || j >= S) return;
     switch (j) {
         case 1:
-            if (P.cpl == 2) srun_mode<1, 2, false, 0, 0, 1>(P, frame, chunk, band, lane, G2);
-            else srun_mode<1, 4, false, 0, 0, 1>(P, frame, chunk, band, lane, G4);
+            if (P.cpl == 2) srun_mode<1, 2, false, 0, 1, 1>(P, frame, chunk, band, lane, G2);
+            else srun_mode<1, 4, false, 0, 1, 1>(P, frame, chunk, band, lane, G4);
             break;
         case 2:
             if constexpr (S > 2) {
-                if (P.cpl == 2) srun_mode<2, 2, false, 0, 0, 1>(P, frame, chunk, band, lane, G2);
-                else srun_mode<2, 4, false, 0, 0, 1>(P, frame, chunk, band, lane, G4);
+                if (P.cpl == 2) srun_mode<2, 2, false, 0, 1, 1>(P, frame, chunk, band, lane, G2);
+                else srun_mode<2, 4, false, 0, 1, 1>(P, frame, chunk, band, lane, G4);
             }
             break;
         default:
             if constexpr (S > 3) {
-                if (P.cpl == 2) srun_mode<3, 2, false, 0, 0, 1>(P, frame, chunk, band, lane, G2);
-                else srun_mode<3, 4, false, 0, 0, 1>(P, frame, chunk, band, lane, G4);
+                if (P.cpl == 2) srun_mode<3, 2, false, 0, 1, 1>(P, frame, chunk, band, lane, G2);
+                else srun_mode<3, 4, false, 0, 1, 1>(P, frame, chunk, band, lane, G4);
             }
             break;
     }

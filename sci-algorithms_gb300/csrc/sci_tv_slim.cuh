@@ -189,11 +189,12 @@ __device__ __forceinline__ Row<CPL> stage0(const Pass &P, const Rings &G, int r,
 // ucur becomes u_k(i).  GEN: rows may lie outside [r0, r1) or touch the
 // frame's last row.
 //
-// FORM 1 holds the dual field as 4 p (a power-of-two scaling, so every
-// rounding is that of FORM 0 scaled): p' = (4p - g) / den needs no tau
-// product, u = f - d / 4 takes it once per pixel instead, and the energy
-// sums are accumulated 16-fold (their w |grad u| term with 16 w).
-template <int S, int K, int CPL, bool ENERGY, int MODE, bool GEN, int FORM = 0>
+// FORM 1 (the default) holds the dual field as 4 p (a power-of-two scaling,
+// so every rounding is that of FORM 0 scaled): p' = (4p - g) / den needs no
+// tau product, u = f - d / 4 takes it once per pixel instead, and the energy
+// sums are accumulated 16-fold (their w |grad u| term with 16 w).  FORM 0
+// holds p itself.
+template <int S, int K, int CPL, bool ENERGY, int MODE, bool GEN, int FORM = 1>
 __device__ __forceinline__ void stage(const Pass &P, const SS<S, CPL> &in, SS<S, CPL> &out,
                                       Row<CPL> &ucur, int r, int rs, int r0, int r1,
                                       const SLane<CPL> &L, float *ob, const Rings &G,
@@ -286,7 +287,7 @@ __device__ __forceinline__ void stages(const Pass &P, const SS<S, CPL> &in, SS<S
 }
 
 // One pipeline step: input row r enters, stage k handles row r - k.
-template <int S, int CPL, bool ENERGY, int MODE, bool GEN, int PROJ, int FORM = 0, int COH = 0>
+template <int S, int CPL, bool ENERGY, int MODE, bool GEN, int PROJ, int FORM = 1, int COH = 0>
 __device__ __forceinline__ void sstep(const Pass &P, const SS<S, CPL> &in, SS<S, CPL> &out,
                                       int r, int rs, int r0, int r1, const SLane<CPL> &L,
                                       const float *fb, float *ob, const Rings &G, uint32_t ldb,
@@ -302,7 +303,7 @@ __device__ __forceinline__ void sstep(const Pass &P, const SS<S, CPL> &in, SS<S,
 
 // One work item: frame, row chunk, column band.  Requires rows aligned for
 // CPL-wide access (W % CPL == 0, base pointers aligned to 4 CPL bytes).
-template <int S, int CPL, bool ENERGY, int MODE, int PROJ, int FORM = 0, int COH = 0>
+template <int S, int CPL, bool ENERGY, int MODE, int PROJ, int FORM = 1, int COH = 0>
 __device__ __forceinline__ void srun(const Pass &P, int frame, int chunk, int band, int lane,
                                      const Rings &G) {
     const int H = P.H, W = P.W;
@@ -380,7 +381,7 @@ __device__ __forceinline__ void srun(const Pass &P, int frame, int chunk, int ba
     }
 }
 
-template <int S, int CPL, bool ENERGY, int PROJ, int FORM = 0, int COH = 0>
+template <int S, int CPL, bool ENERGY, int PROJ, int FORM = 1, int COH = 0>
 __device__ __forceinline__ void srun_mode(const Pass &P, int frame, int chunk, int band, int lane,
                                           const Rings &G) {
     const int c0 = band * P.own - P.hl;
@@ -419,7 +420,7 @@ __device__ __forceinline__ Rings lane_rings(unsigned char *smem, int lane, int w
 // all S dual updates of every frame, and (with a ticket) the stop decision
 // by the last work item, as k_tv_main.  MINB: resident blocks per SM the
 // registers are sized for.
-template <int S, int CPL, int MINB, int PROJ, int FORM = 0>
+template <int S, int CPL, int MINB, int PROJ, int FORM = 1>
 __global__ void __launch_bounds__(WPB * 32, MINB) k_tv_slim(Pass P) {
     __shared__ __align__(16) unsigned char smem[Smem<CPL, PROJ>::bytes];
     int frame, chunk, band;

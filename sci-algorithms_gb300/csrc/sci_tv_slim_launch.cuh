@@ -28,7 +28,7 @@ const void *main_kernel(int SG) {
 }
 
 template <int CPL, int MINB, int PROJ>
-void launch_main(const Pass &P, int SG, cudaStream_t s, int form = 0) {
+void launch_main(const Pass &P, int SG, cudaStream_t s, int form = 1) {
     const unsigned g = pass_blocks(P);
     constexpr int D = MinB<CPL>::def;
     switch (SG) {
