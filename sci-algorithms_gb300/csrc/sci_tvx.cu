@@ -19,13 +19,15 @@
 // update from the forward differences of u), so kinds 1, 2, 3 and 5 run on
 // the temporally blocked TV pipeline (sci_tv.cuh, RULE_CLIP /
 // RULE_CHAM_ATV / RULE_CHAM_ITV): the stack crosses HBM once per 4 dual
-// updates.  The FGP files (two dual fields and a momentum) and ITV3D_cham
-// (a norm summed over all frames of a pixel) run one kernel per iteration
-// over the stack, one thread per pixel (kinds 7 and 8: per pixel position,
-// looping over the frames); a thread recomputes the few primal values its
-// dual update needs from the neighbouring duals (served by L1).  The last
-// dual update of the FGP loop does not reach the returned value and is not
-// computed.
+// updates.  ITV3D_cham (a norm summed over all frames of a pixel) runs its
+// own row pipeline with the frames of a pixel spread over the warps of a
+// block: up to 5 updates and the output per pass, so the stack crosses HBM
+// once per call.  The FGP files (two dual fields and a momentum) run one
+// kernel per iteration over the stack, one thread per pixel (kind 8: per
+// pixel position, looping over the frames); a thread recomputes the few
+// primal values its dual update needs from the neighbouring duals (served
+// by L1).  The last dual update of the FGP loop does not reach the
+// returned value and is not computed.
 #include <cmath>
 #include <utility>
 
@@ -52,15 +54,6 @@ struct Geo {
 };
 
 // -------------------------------------------------------- Chambolle family
-// divp = p1 - p1(:,il) + p2 - p2(iu,:): no p at the first column / row.
-__device__ __forceinline__ float cham_divp(const float *p1, const float *p2, const Geo &g, int i,
-                                           int j) {
-    const int64_t p = (int64_t)i * g.W + j;
-    const float a = p1[p], l = j > 0 ? p1[p - 1] : a;
-    const float b = p2[p], t = i > 0 ? p2[p - g.W] : b;
-    return ((a - l) + b) - t;
-}
-
 // Frame-coupled kernels (ITV3D): a block covers 32 pixels of one row with
 // FL frame lanes (threadIdx.y); lane l handles frames l, l+FL, ... (at most
 // FMAX per lane, kept in registers), the per-pixel sum over frames is
@@ -78,152 +71,180 @@ __device__ __forceinline__ float lane_reduce(float v, float (*red)[32]) {
     return s;
 }
 
-// ITV3D: denom = 1 + dt sqrt(sum over frames of z1^2 + z2^2).  A block
-// owns a strip of 32 columns and RB rows and walks down it: per row it
-// loads p1, p2 and f of the next row once (the left neighbour of p1 and
-// the right neighbour of z come by shuffle; lanes 0 and 31 load the strip's
-// halo columns), reduces the norm over the frames in shared memory and
-// writes the updated duals of the row.
-#ifndef SCI_ITV3D_RB
-#define SCI_ITV3D_RB 16
-#endif
-constexpr int RB = SCI_ITV3D_RB;  // rows per block
+// ITV3D Chambolle (tvdenoise_cham_ITV3D.m:74-91), up to 5 updates and the
+// output u = f - div p / lambda in one pass over the stack.  Per update,
+//   z  = div p - lambda f          (div p = p1 - p1(:,il) + p2 - p2(iu,:))
+//   z1 = z(:, ir) - z, z2 = z(ir, :) - z   (zero at the last column / row)
+//   q  = (p + dt z) / (1 + dt sqrt(sum over frames of z1^2 + z2^2)).
+// q at (i, j) reads p at (i, j-1 .. j+1) and (i-1 .. i+1, j): radius one,
+// so S updates chain as a row pipeline (the lean scikit-image TV pass's
+// scheme): when input row r arrives, update k produces row r - k from the
+// rows of update k - 1 it keeps in registers, and the output stage forms
+// u at row r - S.  A block is 32 columns (lanes) x FL frame lanes (warps);
+// warp w holds frames w, w + FL, ... (NT slots); the norm over the frames
+// of a pixel is reduced in shared memory, one barrier per update and row
+// (the sums of consecutive rows in alternate buffers, so a warp that runs
+// ahead never overwrites sums another warp still reads).
+// Each update narrows the valid columns by one on either side, so a strip
+// owns 32 - 2S - 1 columns; a chunk of rows starts S + 1 rows early.  f
+// rows come through a per-thread cp.async ring (each lane reads back only
+// the values it copied).  The first pass starts from p = 0; a run of more
+// than 5 updates carries p through the workspace between passes (pin: load
+// p of the input rows, out == 0: store p^S instead of u).
+constexpr int IT3_RING = 8;  // f rows in the ring (>= S + 1 + prefetch distance 2)
 
-__global__ void __launch_bounds__(32 * FL) k_cham_update_coupled(
-    const float *__restrict__ f, const float *__restrict__ p1, const float *__restrict__ p2,
-    float *__restrict__ q1, float *__restrict__ q2, Geo g, int nf, float lam, float dt,
-    int first) {
-    __shared__ float red[FL][32];
-    const int lane = threadIdx.x;
-    const int x0 = blockIdx.x * 32, j = x0 + lane;
-    const int i0 = blockIdx.y * RB, i1 = min(i0 + RB, g.H);
-    const bool in = j < g.W;
-    const int jc = in ? j : g.W - 1;           // a valid column for the loads
-    const bool right = x0 + 32 < g.W;          // the strip has a right halo column
-    const int jr = right ? x0 + 32 : jc;
-    // z at (i, col) from p1(i, col), p1(i, col-1), p2(i, col), p2(i-1, col), f
-    auto zval = [&](float a, float al, float b, float bu, float fv) {
-        return (((a - al) + b) - bu) - fv * lam;
-    };
-    float zc[FMAX], zr[FMAX], p1c[FMAX], p2c[FMAX], p2r[FMAX];
-#pragma unroll
-    for (int t = 0; t < FMAX; ++t) {  // row i0
-        const int b = threadIdx.y + t * FL;
-        zc[t] = zr[t] = p1c[t] = p2c[t] = p2r[t] = 0.f;
-        if (b >= nf) continue;
-        const int64_t fo = (int64_t)b * g.hw;
-        const int64_t o = fo + (int64_t)i0 * g.W;
-        if (first) {
-            zc[t] = -f[o + jc] * lam;
-            if (lane == 31 && right) zr[t] = -f[o + jr] * lam;
-            continue;
-        }
-        const float a = p1[o + jc], bb = p2[o + jc];
-        const float al = (jc > 0) ? p1[o + jc - 1] : a;
-        const float bu = (i0 > 0) ? p2[o - g.W + jc] : bb;
-        zc[t] = zval(a, al, bb, bu, f[o + jc]);
-        p1c[t] = a;
-        p2c[t] = bb;
-        if (lane == 31 && right) {
-            const float ar = p1[o + jr], br = p2[o + jr];
-            const float bur = (i0 > 0) ? p2[o - g.W + jr] : br;
-            zr[t] = zval(ar, p1[o + jr - 1], br, bur, f[o + jr]);
-            p2r[t] = br;
-        }
-    }
-    for (int i = i0; i < i1; ++i) {
-        const bool lastrow = i + 1 >= g.H;
-        float z1[FMAX], z2[FMAX], zn[FMAX], p1n[FMAX], p2n[FMAX], zrn[FMAX], p2rn[FMAX];
-        float s = 0.f;
-        // every load of row i + 1 first, by all lanes alike (lanes that are
-        // not at the strip's edge load their own column for the halo
-        // values, an L1 hit), so that one memory latency covers the row
-        const int jl = (lane == 0 && x0 > 0) ? x0 - 1 : jc;  // left p1
-        const int jh = (lane == 31) ? jr : jc;               // right halo column
-        float la[FMAX], lb[FMAX], lf[FMAX], ll[FMAX], ra[FMAX], rb[FMAX], rf[FMAX];
-#pragma unroll
-        for (int t = 0; t < FMAX; ++t) {
-            const int b = threadIdx.y + t * FL;
-            la[t] = lb[t] = lf[t] = ll[t] = ra[t] = rb[t] = rf[t] = 0.f;
-            if (b >= nf || lastrow) continue;
-            const int64_t o = (int64_t)b * g.hw + (int64_t)(i + 1) * g.W;
-            lf[t] = f[o + jc];
-            rf[t] = f[o + jh];
-            if (!first) {
-                la[t] = p1[o + jc];
-                lb[t] = p2[o + jc];
-                ll[t] = p1[o + jl];
-                ra[t] = p1[o + jh];
-                rb[t] = p2[o + jh];
-            }
-        }
-#pragma unroll
-        for (int t = 0; t < FMAX; ++t) {
-            const int b = threadIdx.y + t * FL;
-            // right neighbour of z in this row (all lanes shuffle)
-            float zright = __shfl_down_sync(0xffffffffu, zc[t], 1);
-            if (lane == 31) zright = zr[t];
-            const float a = la[t];
-            float al = __shfl_up_sync(0xffffffffu, a, 1);
-            zn[t] = p1n[t] = p2n[t] = zrn[t] = p2rn[t] = 0.f;
-            z1[t] = z2[t] = 0.f;
-            if (b >= nf) continue;
-            if (!lastrow) {  // row i + 1
-                if (first) {
-                    zn[t] = -lf[t] * lam;
-                    if (lane == 31 && right) zrn[t] = -rf[t] * lam;
-                } else {
-                    const float bb = lb[t];
-                    if (lane == 0) al = (x0 > 0) ? ll[t] : a;
-                    if (jc == 0) al = a;  // MATLAB: no p1 at the first column
-                    zn[t] = zval(a, al, bb, p2c[t], lf[t]);
-                    p1n[t] = a;
-                    p2n[t] = bb;
-                    if (lane == 31 && right) {
-                        zrn[t] = zval(ra[t], a, rb[t], p2r[t], rf[t]);
-                        p2rn[t] = rb[t];
-                    }
-                }
-            }
-            z1[t] = (j < g.W - 1) ? zright - zc[t] : 0.f;
-            z2[t] = lastrow ? 0.f : zn[t] - zc[t];
-            s += z1[t] * z1[t] + z2[t] * z2[t];
-        }
-        red[threadIdx.y][lane] = s;
-        __syncthreads();
-        float tot = 0.f;
-#pragma unroll
-        for (int l = 0; l < FL; ++l) tot += red[l][lane];
-        __syncthreads();
-        const float denom = 1.f + dt * sqrtf(tot);
-#pragma unroll
-        for (int t = 0; t < FMAX; ++t) {
-            const int b = threadIdx.y + t * FL;
-            if (b < nf && in) {
-                const int64_t q = (int64_t)b * g.hw + (int64_t)i * g.W + j;
-                q1[q] = (p1c[t] + dt * z1[t]) / denom;
-                q2[q] = (p2c[t] + dt * z2[t]) / denom;
-            }
-            zc[t] = zn[t];
-            p1c[t] = p1n[t];
-            p2c[t] = p2n[t];
-            zr[t] = zrn[t];
-            p2r[t] = p2rn[t];
-        }
-    }
+__device__ __forceinline__ void cp4(uint32_t dst, const float *src) {
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 4;\n" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp4_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp4_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-__global__ void k_cham_out(const float *__restrict__ f, const float *__restrict__ p1,
-                           const float *__restrict__ p2, float *__restrict__ u,
-                           float *__restrict__ resid, Geo g, float lam) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    const int i = blockIdx.y * blockDim.y + threadIdx.y;
-    if (i >= g.H || j >= g.W) return;
-    const int64_t fo = (int64_t)blockIdx.z * g.hw;
-    const int64_t p = (int64_t)i * g.W + j;
-    const float x = f[fo + p] - cham_divp(p1 + fo, p2 + fo, g, i, j) / lam;
-    u[fo + p] = x;
-    if (resid) resid[fo + p] = x - f[fo + p];
+template <int S, int NT>
+__global__ void __launch_bounds__(32 * FL, 2) k_itv3d_cham(
+    const float *__restrict__ f, const float *__restrict__ pin1, const float *__restrict__ pin2,
+    float *__restrict__ u, float *__restrict__ resid, float *__restrict__ pout1,
+    float *__restrict__ pout2, Geo g, int nf, float lam, float dt, int R, int own, int pin,
+    int out) {
+    constexpr int PF = IT3_RING - S - 1;  // rows prefetched ahead
+    static_assert(S >= 1 && S <= 5 && PF >= 2, "ITV3D pass: 1..5 updates");
+    __shared__ float ring[IT3_RING][NT * FL][32];
+    __shared__ float red[2][S][FL][32];  // by row parity: one barrier per use
+    const int lane = threadIdx.x, w = threadIdx.y;
+    const int H = g.H, W = g.W;
+    const int col = blockIdx.x * own - (S + 1) + lane;
+    const int colc = min(max(col, 0), W - 1);
+    const bool owned = lane >= S + 1 && lane < S + 1 + own && col < W;
+    const bool first_col = col <= 0, last_col = col >= W - 1;
+    const int r0 = blockIdx.y * R, r1 = min(r0 + R, H);
+    const int rs = max(0, r0 - S - 1), re = r1 - 1 + S;  // input rows rs.., last step re
+    bool fv[NT];
+    int64_t fo[NT];
+#pragma unroll
+    for (int t = 0; t < NT; ++t) {
+        const int b = w + t * FL;
+        fv[t] = b < nf;
+        fo[t] = (int64_t)min(b, nf - 1) * g.hw + colc;
+    }
+    auto fetch = [&](int r) {  // f row r into its ring slot
+        if (r < H && r <= re) {
+#pragma unroll
+            for (int t = 0; t < NT; ++t)
+                cp4((uint32_t)__cvta_generic_to_shared(&ring[r % IT3_RING][w + t * FL][lane]),
+                    f + fo[t] + (int64_t)r * W);
+        }
+        cp4_commit();
+    };
+    // kept per update k: p^{k-1} and z^{k-1} of the row before its input row
+    float zc[S][NT], p1c[S][NT], p2c[S][NT], p2o[NT];
+#pragma unroll
+    for (int k = 0; k < S; ++k)
+#pragma unroll
+        for (int t = 0; t < NT; ++t) zc[k][t] = p1c[k][t] = p2c[k][t] = 0.f;
+#pragma unroll
+    for (int t = 0; t < NT; ++t) p2o[t] = 0.f;
+#pragma unroll
+    for (int q = 0; q < PF; ++q) fetch(rs + q);
+    for (int r = rs; r <= re; ++r) {
+        fetch(r + PF);
+        cp4_wait<PF>();
+        // p^0 of input row r
+        float in1[NT], in2[NT];
+#pragma unroll
+        for (int t = 0; t < NT; ++t) {
+            in1[t] = in2[t] = 0.f;
+            if (pin && r < H) {
+                in1[t] = __ldg(pin1 + fo[t] + (int64_t)r * W);
+                in2[t] = __ldg(pin2 + fo[t] + (int64_t)r * W);
+            }
+        }
+#pragma unroll
+        for (int k = 0; k < S; ++k) {  // update k + 1: input row a, output row a - 1
+            const int a = r - k, b = a - 1;
+            const bool vin = a < H && a >= rs, vout = b >= rs && b < H;
+            float zin[NT];
+#pragma unroll
+            for (int t = 0; t < NT; ++t) zin[t] = 0.f;
+            if (vin) {
+#pragma unroll
+                for (int t = 0; t < NT; ++t) {
+                    float l = __shfl_up_sync(0xffffffffu, in1[t], 1);
+                    if (first_col) l = in1[t];
+                    const float up = (a == 0) ? in2[t] : p2c[k][t];
+                    const float fa = ring[a % IT3_RING][w + t * FL][lane];
+                    zin[t] = (((in1[t] - l) + in2[t]) - up) - fa * lam;
+                }
+            }
+            if (vout) {
+                float z1[NT], z2[NT], s = 0.f;
+#pragma unroll
+                for (int t = 0; t < NT; ++t) {
+                    const float zr = __shfl_down_sync(0xffffffffu, zc[k][t], 1);
+                    z1[t] = last_col ? 0.f : zr - zc[k][t];
+                    z2[t] = (b < H - 1) ? zin[t] - zc[k][t] : 0.f;
+                    if (fv[t]) s += z1[t] * z1[t] + z2[t] * z2[t];
+                }
+                red[r & 1][k][w][lane] = s;
+                __syncthreads();
+                float tot = 0.f;
+#pragma unroll
+                for (int l = 0; l < FL; ++l) tot += red[r & 1][k][l][lane];
+                const float rd = __frcp_rn(1.f + dt * sqrtf(tot));
+                // p^{k+1} of row b becomes the next update's input row
+#pragma unroll
+                for (int t = 0; t < NT; ++t) {
+                    const float q1 = (p1c[k][t] + dt * z1[t]) * rd;
+                    const float q2 = (p2c[k][t] + dt * z2[t]) * rd;
+                    if (vin) {
+                        zc[k][t] = zin[t];
+                        p1c[k][t] = in1[t];
+                        p2c[k][t] = in2[t];
+                    }
+                    in1[t] = q1;
+                    in2[t] = q2;
+                }
+            } else {
+#pragma unroll
+                for (int t = 0; t < NT; ++t) {
+                    if (vin) {
+                        zc[k][t] = zin[t];
+                        p1c[k][t] = in1[t];
+                        p2c[k][t] = in2[t];
+                    }
+                    in1[t] = in2[t] = 0.f;
+                }
+            }
+        }
+        // p^S of row a = r - S
+        const int a = r - S;
+        if (a < rs || a >= H) continue;
+        const bool keep = owned && a >= r0 && a < r1;
+        if (!out) {
+#pragma unroll
+            for (int t = 0; t < NT; ++t)
+                if (keep && fv[t]) {
+                    pout1[fo[t] + (int64_t)a * W] = in1[t];
+                    pout2[fo[t] + (int64_t)a * W] = in2[t];
+                }
+            continue;
+        }
+#pragma unroll
+        for (int t = 0; t < NT; ++t) {
+            float l = __shfl_up_sync(0xffffffffu, in1[t], 1);
+            if (first_col) l = in1[t];
+            const float up = (a == 0) ? in2[t] : p2o[t];
+            p2o[t] = in2[t];
+            const float fa = ring[a % IT3_RING][w + t * FL][lane];
+            const float x = fa - (((in1[t] - l) + in2[t]) - up) / lam;
+            if (keep && fv[t]) {
+                u[fo[t] + (int64_t)a * W] = x;
+                if (resid) resid[fo[t] + (int64_t)a * W] = x - fa;
+            }
+        }
+    }
+    asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
 
 // ------------------------------------------------------------ FGP family
@@ -335,6 +356,59 @@ __global__ void k_fill(int *a, int v, int n) {
     if (i < n) a[i] = v;
 }
 
+// One pass of S ITV3D updates (p_in null: p = 0; p_out null: store u).
+// Row chunks are sized so the blocks fill whole waves of the resident
+// blocks, counting the 2S + 1 rows every chunk recomputes.
+int itv3d_pass(int S, const float *f, const float *p_in1, const float *p_in2, float *u,
+               float *resid, float *p_out1, float *p_out2, const Geo &g, int nf, float lam,
+               float dt, cudaStream_t s) {
+    const int nt = (nf + FL - 1) / FL;
+    const int own = 32 - 2 * S - 1;
+    const int strips = (g.W + own - 1) / own;
+    static int resident[6][5] = {};
+    const void *kp = nullptr;
+#define SCI_IT3_PTR(SV, NV) if (S == SV && nt == NV) kp = reinterpret_cast<const void *>(&k_itv3d_cham<SV, NV>);
+#define SCI_IT3_ROW(SV) SCI_IT3_PTR(SV, 1) SCI_IT3_PTR(SV, 2) SCI_IT3_PTR(SV, 3) SCI_IT3_PTR(SV, 4)
+    SCI_IT3_ROW(1) SCI_IT3_ROW(2) SCI_IT3_ROW(3) SCI_IT3_ROW(4) SCI_IT3_ROW(5)
+#undef SCI_IT3_ROW
+#undef SCI_IT3_PTR
+    SCI_CHECK_ARG(kp != nullptr, "tv_matlab: ITV3D pass of %d updates, %d frames", S, nf);
+    if (resident[S][nt - 1] == 0) {
+        int per_sm = 0;
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kp, 32 * FL, 0) !=
+                cudaSuccess || per_sm <= 0) {
+            cudaGetLastError();
+            per_sm = 1;
+        }
+        resident[S][nt - 1] = per_sm * kSMs;
+    }
+    const int64_t slots = resident[S][nt - 1];
+    int best_n = 1;
+    double best = 1e300;
+    for (int n = 1; n <= std::min(g.H, 256); ++n) {
+        const int R = (g.H + n - 1) / n;
+        const int64_t blocks = (int64_t)strips * ((g.H + R - 1) / R);
+        const double t = (double)((blocks + slots - 1) / slots) * (R + 2 * S + 1);
+        if (t < best - 1e-9) {
+            best = t;
+            best_n = n;
+        }
+    }
+    const int R = (g.H + best_n - 1) / best_n;
+    const dim3 grd((unsigned)strips, (unsigned)((g.H + R - 1) / R)), blk(32, FL);
+    const int pin = p_in1 != nullptr, out = p_out1 == nullptr;
+#define SCI_IT3_CASE(SV, NV)                                                                  \
+    if (S == SV && nt == NV)                                                                  \
+        k_itv3d_cham<SV, NV><<<grd, blk, 0, s>>>(f, p_in1, p_in2, u, resid, p_out1, p_out2, g, \
+                                                 nf, lam, dt, R, own, pin, out);
+#define SCI_IT3_ROW(SV) SCI_IT3_CASE(SV, 1) SCI_IT3_CASE(SV, 2) SCI_IT3_CASE(SV, 3) SCI_IT3_CASE(SV, 4)
+    SCI_IT3_ROW(1) SCI_IT3_ROW(2) SCI_IT3_ROW(3) SCI_IT3_ROW(4) SCI_IT3_ROW(5)
+#undef SCI_IT3_ROW
+#undef SCI_IT3_CASE
+    SCI_LAUNCHED("k_itv3d_cham");
+    return SCI_OK;
+}
+
 // Kinds run on the TV pipeline, and its update rule.
 bool on_pipeline(int kind) {
     return kind == CLIP_A || kind == CLIP_B || kind == CHAM_ATV || kind == CHAM_ITV2D;
@@ -375,11 +449,9 @@ int tvx_launch(int kind, const float *f, float *u, float *resid, int64_t nf, int
     Geo g{(int)H, (int)W, hw};
     const dim3 blk(32, 8);
     const dim3 grd((unsigned)((W + 31) / 32), (unsigned)((H + 7) / 8), (unsigned)nf);
-    // frame-coupled kernels: 32 pixels x FL frame lanes per block; FGP one
-    // row per block, Chambolle RB rows per block
+    // frame-coupled FGP: 32 pixels x FL frame lanes per block, one row
     const dim3 blkc(32, FL);
     const dim3 grdc((unsigned)((W + 31) / 32), (unsigned)H, 1);
-    const dim3 grds((unsigned)((W + 31) / 32), (unsigned)((H + RB - 1) / RB), 1);
     float *w0 = static_cast<float *>(ws);
     float *a1 = w0, *a2 = w0 + n, *b1 = w0 + 2 * n, *b2 = w0 + 3 * n;
     if (steps) {
@@ -403,18 +475,23 @@ int tvx_launch(int kind, const float *f, float *u, float *resid, int64_t nf, int
             return tv_launch_rule(tv::RULE_CHAM_ATV, f, u, resid, nf, H, W, iters, 0.125f, 0.f,
                                   lam, 0.f, nullptr, ws, ws_bytes, s);
         case CHAM_ITV3D: {
-            // tvdenoise_cham_ITV3D.m:74-91
+            // tvdenoise_cham_ITV3D.m:74-91: passes of up to 5 updates, the
+            // last one forming u
             const float dt = 0.25f;
-            float *p1 = a1, *p2 = a2, *q1 = b1, *q2 = b2;
-            for (int it = 0; it < iters; ++it) {
-                k_cham_update_coupled<<<grds, blkc, 0, s>>>(f, p1, p2, q1, q2, g, (int)nf, lam,
-                                                            dt, it == 0);
-                SCI_LAUNCHED("k_cham_update_coupled");
-                std::swap(p1, q1);
-                std::swap(p2, q2);
+            const int npass = (iters + 4) / 5;
+            const float *p_in1 = nullptr, *p_in2 = nullptr;
+            float *q1 = a1, *q2 = a2;
+            for (int ps = 0; ps < npass; ++ps) {
+                const bool last = ps + 1 == npass;
+                const int S = last ? iters - 5 * (npass - 1) : 5;
+                const int e = itv3d_pass(S, f, p_in1, p_in2, u, resid, last ? nullptr : q1,
+                                         last ? nullptr : q2, g, (int)nf, lam, dt, s);
+                if (e) return e;
+                p_in1 = q1;
+                p_in2 = q2;
+                std::swap(q1, b1);
+                std::swap(q2, b2);
             }
-            k_cham_out<<<grd, blk, 0, s>>>(f, p1, p2, u, resid, g, lam);
-            SCI_LAUNCHED("k_cham_out");
             return SCI_OK;
         }
         default: {

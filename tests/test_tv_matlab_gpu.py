@@ -43,10 +43,12 @@ def test_denoiser_matches_oracle(tvm, H, W, B):
 
 @pytest.mark.parametrize("tvm,lam", [("ITV3D_FGP", 0.004), ("ITV2D_FGP", 0.004),
                                      ("ATV_FGP", 0.004), ("ITV3D_cham", 2.0)])
-@pytest.mark.parametrize("iters", [1, 2, 4])
+@pytest.mark.parametrize("iters", [1, 2, 4, 6, 11])
 def test_projection_active_and_iteration_counts(tvm, lam, iters):
     """Small FGP lambdas make the dual projection bind (and couple the
-    frames for ITV3D); other iteration counts than gapdenoise's."""
+    frames for ITV3D); other iteration counts than gapdenoise's (ITV3D
+    Chambolle runs passes of up to 5 updates: 6 and 11 carry the dual field
+    through the workspace between passes)."""
     f = frames(48, 40, 3, seed=iters)
     kind = sci.TVM[tvm][0]
     fn = tm._FN[tm.TVM[tvm][0]]
@@ -67,6 +69,19 @@ def test_itv3d_frame_counts(B, H, W):
     ref = tm.tv_by_name(f, "ITV3D_cham", 0.1)
     out = sci.denoise_tv_matlab(f, "ITV3D_cham", 0.1)
     assert np.max(np.abs(out - ref)) < ATOL
+
+
+@pytest.mark.parametrize("H,W,B,iters", [(300, 260, 24, 5), (129, 517, 32, 5), (64, 1000, 16, 2),
+                                         (97, 45, 12, 7)])
+def test_itv3d_row_chunks_and_strips(H, W, B, iters):
+    """ITV3D Chambolle at sizes with many row chunks (each recomputes the
+    2 S + 1 rows around its edges) and column strips (each owns 32 - 2 S - 1
+    columns of its 32 lanes)."""
+    f = frames(H, W, B, seed=H + W + B)
+    ref = tm.tvdenoise_cham_itv3d(f, 10.0, iters)
+    u = sci.tv_matlab_frames(_dev.planar(f), sci.TVM["ITV3D_cham"][0], 10.0, iters)
+    torch.cuda.synchronize()
+    assert np.max(np.abs(_dev.unplanar(u, f) - ref)) < ATOL
 
 
 def test_one_frame_takes_matlabs_2d_branch():
