@@ -29,6 +29,7 @@
 // by L1).  The last dual update of the FGP loop does not reach the
 // returned value and is not computed.
 #include <cmath>
+#include <type_traits>
 #include <utility>
 
 #include "sci_common.cuh"
@@ -110,14 +111,22 @@ __global__ void __launch_bounds__(32 * FL, 2) k_itv3d_cham(
     int out) {
     constexpr int PF = IT3_RING - S - 1;  // rows prefetched ahead
     static_assert(S >= 1 && S <= 5 && PF >= 2, "ITV3D pass: 1..5 updates");
+    static_assert((IT3_RING & (IT3_RING - 1)) == 0 && FL == 8, "ring slots by mask");
     __shared__ float ring[IT3_RING][NT * FL][32];
-    __shared__ float red[2][S][FL][32];  // by row parity: one barrier per use
+    // per-pixel sums of the frame lanes, [row parity][update][column][lane
+    // slot]: a column's FL sums are one 32-byte row, read with two vector
+    // loads; the slot is the frame lane XOR (column / 4) % FL, so the FL
+    // lanes' stores of one warp hit distinct banks.  Every warp adds a
+    // column's slots in the same (slot) order, so all frames of a pixel see
+    // the same total.
+    __shared__ __align__(16) float red[2][S][32][FL];
     const int lane = threadIdx.x, w = threadIdx.y;
     const int H = g.H, W = g.W;
     const int col = blockIdx.x * own - (S + 1) + lane;
     const int colc = min(max(col, 0), W - 1);
     const bool owned = lane >= S + 1 && lane < S + 1 + own && col < W;
     const bool first_col = col <= 0, last_col = col >= W - 1;
+    const int slot = w ^ ((lane >> 2) & (FL - 1));
     const int r0 = blockIdx.y * R, r1 = min(r0 + R, H);
     const int rs = max(0, r0 - S - 1), re = r1 - 1 + S;  // input rows rs.., last step re
     bool fv[NT];
@@ -132,7 +141,8 @@ __global__ void __launch_bounds__(32 * FL, 2) k_itv3d_cham(
         if (r < H && r <= re) {
 #pragma unroll
             for (int t = 0; t < NT; ++t)
-                cp4((uint32_t)__cvta_generic_to_shared(&ring[r % IT3_RING][w + t * FL][lane]),
+                cp4((uint32_t)__cvta_generic_to_shared(
+                        &ring[r & (IT3_RING - 1)][w + t * FL][lane]),
                     f + fo[t] + (int64_t)r * W);
         }
         cp4_commit();
@@ -145,17 +155,19 @@ __global__ void __launch_bounds__(32 * FL, 2) k_itv3d_cham(
         for (int t = 0; t < NT; ++t) zc[k][t] = p1c[k][t] = p2c[k][t] = 0.f;
 #pragma unroll
     for (int t = 0; t < NT; ++t) p2o[t] = 0.f;
-#pragma unroll
-    for (int q = 0; q < PF; ++q) fetch(rs + q);
-    for (int r = rs; r <= re; ++r) {
+
+    // One step: input row r enters, update k + 1 produces row r - k - 1,
+    // the output stage row r - S.  FAST: every stage has its input and
+    // output rows inside [rs, H - 1) and none is row 0 (no tests needed).
+    auto step = [&](int r, auto fast) {
+        constexpr bool FAST = decltype(fast)::value;
         fetch(r + PF);
         cp4_wait<PF>();
-        // p^0 of input row r
-        float in1[NT], in2[NT];
+        float in1[NT], in2[NT];  // p^0 of input row r
 #pragma unroll
         for (int t = 0; t < NT; ++t) {
             in1[t] = in2[t] = 0.f;
-            if (pin && r < H) {
+            if (pin && (FAST || r < H)) {
                 in1[t] = __ldg(pin1 + fo[t] + (int64_t)r * W);
                 in2[t] = __ldg(pin2 + fo[t] + (int64_t)r * W);
             }
@@ -163,7 +175,7 @@ __global__ void __launch_bounds__(32 * FL, 2) k_itv3d_cham(
 #pragma unroll
         for (int k = 0; k < S; ++k) {  // update k + 1: input row a, output row a - 1
             const int a = r - k, b = a - 1;
-            const bool vin = a < H && a >= rs, vout = b >= rs && b < H;
+            const bool vin = FAST || (a < H && a >= rs), vout = FAST || (b >= rs && b < H);
             float zin[NT];
 #pragma unroll
             for (int t = 0; t < NT; ++t) zin[t] = 0.f;
@@ -172,8 +184,8 @@ __global__ void __launch_bounds__(32 * FL, 2) k_itv3d_cham(
                 for (int t = 0; t < NT; ++t) {
                     float l = __shfl_up_sync(0xffffffffu, in1[t], 1);
                     if (first_col) l = in1[t];
-                    const float up = (a == 0) ? in2[t] : p2c[k][t];
-                    const float fa = ring[a % IT3_RING][w + t * FL][lane];
+                    const float up = (!FAST && a == 0) ? in2[t] : p2c[k][t];
+                    const float fa = ring[a & (IT3_RING - 1)][w + t * FL][lane];
                     zin[t] = (((in1[t] - l) + in2[t]) - up) - fa * lam;
                 }
             }
@@ -183,14 +195,15 @@ __global__ void __launch_bounds__(32 * FL, 2) k_itv3d_cham(
                 for (int t = 0; t < NT; ++t) {
                     const float zr = __shfl_down_sync(0xffffffffu, zc[k][t], 1);
                     z1[t] = last_col ? 0.f : zr - zc[k][t];
-                    z2[t] = (b < H - 1) ? zin[t] - zc[k][t] : 0.f;
+                    z2[t] = (FAST || b < H - 1) ? zin[t] - zc[k][t] : 0.f;
                     if (fv[t]) s += z1[t] * z1[t] + z2[t] * z2[t];
                 }
-                red[r & 1][k][w][lane] = s;
+                float(&rs_)[FL] = red[r & 1][k][lane];
+                rs_[slot] = s;
                 __syncthreads();
-                float tot = 0.f;
-#pragma unroll
-                for (int l = 0; l < FL; ++l) tot += red[r & 1][k][l][lane];
+                const float4 v0 = *reinterpret_cast<const float4 *>(&rs_[0]);
+                const float4 v1 = *reinterpret_cast<const float4 *>(&rs_[4]);
+                const float tot = ((((((v0.x + v0.y) + v0.z) + v0.w) + v1.x) + v1.y) + v1.z) + v1.w;
                 const float rd = __frcp_rn(1.f + dt * sqrtf(tot));
                 // p^{k+1} of row b becomes the next update's input row
 #pragma unroll
@@ -219,7 +232,7 @@ __global__ void __launch_bounds__(32 * FL, 2) k_itv3d_cham(
         }
         // p^S of row a = r - S
         const int a = r - S;
-        if (a < rs || a >= H) continue;
+        if (!FAST && (a < rs || a >= H)) return;
         const bool keep = owned && a >= r0 && a < r1;
         if (!out) {
 #pragma unroll
@@ -228,22 +241,31 @@ __global__ void __launch_bounds__(32 * FL, 2) k_itv3d_cham(
                     pout1[fo[t] + (int64_t)a * W] = in1[t];
                     pout2[fo[t] + (int64_t)a * W] = in2[t];
                 }
-            continue;
+            return;
         }
 #pragma unroll
         for (int t = 0; t < NT; ++t) {
             float l = __shfl_up_sync(0xffffffffu, in1[t], 1);
             if (first_col) l = in1[t];
-            const float up = (a == 0) ? in2[t] : p2o[t];
+            const float up = (!FAST && a == 0) ? in2[t] : p2o[t];
             p2o[t] = in2[t];
-            const float fa = ring[a % IT3_RING][w + t * FL][lane];
+            const float fa = ring[a & (IT3_RING - 1)][w + t * FL][lane];
             const float x = fa - (((in1[t] - l) + in2[t]) - up) / lam;
             if (keep && fv[t]) {
                 u[fo[t] + (int64_t)a * W] = x;
                 if (resid) resid[fo[t] + (int64_t)a * W] = x - fa;
             }
         }
-    }
+    };
+
+#pragma unroll
+    for (int q = 0; q < PF; ++q) fetch(rs + q);
+    // steady rows: r in [rs + S + 1, min(H - 1, re)]
+    const int fb = rs + S + 1, fe = min(H - 1, re);
+    int r = rs;
+    for (; r <= re && r < fb; ++r) step(r, std::false_type{});
+    for (; r <= fe; ++r) step(r, std::true_type{});
+    for (; r <= re; ++r) step(r, std::false_type{});
     asm volatile("cp.async.wait_all;\n" ::: "memory");
 }
 
