@@ -293,9 +293,10 @@ void build_table(const sci_batch_item *items, int n, int K, float eps, char *ws,
         P.cpl = 4;
         P.S = K - 1;
         P.hl = 4;
+        P.hr = 4;
         P.own = 128 - 4 - 4;
         P.ht = K - 1;
-        P.nbands = (int)((s.W + P.own - 1) / P.own);
+        P.nbands = tv::band_count((int)s.W, 128, P.hl, P.hr);
         P.R = s.R > 0 ? s.R : default_R(s.H, s.W, s.B);
         P.nchunks = (int)((s.H + P.R - 1) / P.R);
         P.vec = 1;
@@ -308,13 +309,15 @@ void build_table(const sci_batch_item *items, int n, int K, float eps, char *ws,
         for (int par = 0; par < 2; ++par) {
             tv::Pass &Q = I.tvq[par];
             Q = P;
-            // halos of 4 columns for either width, so that a lane pair's
-            // 16-byte copies (2 columns per lane) start on 16-byte columns
+            // halos of 4 columns for either width: with W % 4 == 0 every
+            // band window starts on a multiple of 4 columns, so that a lane
+            // pair's 16-byte copies (2 columns per lane) are aligned
             const int cpl = s.cpl == 2 ? 2 : 4;
             Q.cpl = cpl;
             Q.hl = 4;
+            Q.hr = 4;
             Q.own = 32 * cpl - 8;
-            Q.nbands = (int)((s.W + Q.own - 1) / Q.own);
+            Q.nbands = tv::band_count((int)s.W, 32 * cpl, Q.hl, Q.hr);
             Q.energy = reinterpret_cast<double *>(ws + L.energy +
                                                   (par ? L.item_e1[i] : L.item_e[i]));
             Q.stopj = reinterpret_cast<int *>(ws + L.item_stop[i]);

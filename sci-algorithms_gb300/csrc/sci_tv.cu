@@ -271,7 +271,8 @@ static int tv_launch_core(const float *f, float *u, float *resid, int64_t nf, in
         P.eps = eps;
         P.cpl = cpl;
         P.hl = round_up(SG + (PIN ? 1 : 0), cpl);
-        P.own = 32 * cpl - P.hl - round_up(SG, cpl);
+        P.hr = round_up(SG, cpl);
+        P.own = 32 * cpl - P.hl - P.hr;
         P.ht = SG + (PIN ? 1 : 0);
         P.lag = lag;
         P.proj = proj ? 1 : 0;
@@ -279,7 +280,7 @@ static int tv_launch_core(const float *f, float *u, float *resid, int64_t nf, in
         P.cmap = proj_c;
         P.lam = proj_lam;
         P.frame_fast = frame_fast_order(proj);
-        P.nbands = (int)((W + P.own - 1) / P.own);
+        P.nbands = band_count((int)W, 32 * cpl, P.hl, P.hr);
         if (force_R > 0) P.R = force_R;
         else if (slim)
             P.R = choose_R_slim(nf, P.nbands, (int)H, SG,

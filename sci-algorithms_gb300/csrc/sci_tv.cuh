@@ -68,7 +68,11 @@ struct Pass {
     int a;                // this pass starts from p_a (p_in) and computes p_{a+1..a+S}
     float tau, tw;        // tau, tau / weight
     float weight, eps;
-    int nbands, nchunks, R, own, hl, ht;
+    // Column bands (band_window): a band is a window of 32 CPL columns; the
+    // middle bands own `own` columns after hl columns of left halo and
+    // before hr of right halo; the first band starts at column 0 and the
+    // last ends at column W - 1, so no lane works outside the frame.
+    int nbands, nchunks, R, own, hl, hr, ht;
     int S;                // dual updates of this pass (geometry of the window)
     int vec;              // 1: rows are aligned for CPL-wide vector loads
     int cpl;              // columns per lane (2 or 4)
@@ -428,15 +432,56 @@ __device__ __forceinline__ void step(const Pass &P, const St<S, CPL> &in, St<S, 
     }
 }
 
+// Number of column bands of a W-wide frame for windows of `width` columns
+// (band_window): one window when it covers the frame, else a first and a
+// last band flush with the frame's edges and as many middle bands as the
+// columns between them need.
+inline int band_count(int W, int width, int hl, int hr) {
+    if (W <= width) return 1;
+    const int own = width - hl - hr;
+    const int mid = W - 2 * width + hl + hr;
+    return 2 + (mid > 0 ? (mid + own - 1) / own : 0);
+}
+
+// Band `band`'s window [c0, c0 + width) and owned columns [lo, hi).  The
+// first band starts at column 0 and owns up to its right halo; middle
+// bands own P.own columns each; the last band ends at column W - 1 (its
+// window may reach further left than hl columns before lo, which only
+// adds halo).  A frame that fits one window is band 0 alone.
+__device__ __forceinline__ void band_window(const Pass &P, int band, int width, int &c0, int &lo,
+                                            int &hi) {
+    if (band == 0) {
+        c0 = 0;
+        lo = 0;
+        hi = P.nbands == 1 ? P.W : width - P.hr;
+    } else {
+        lo = width - P.hr + (band - 1) * P.own;
+        if (band == P.nbands - 1) {
+            c0 = P.W - width;
+            hi = P.W;
+        } else {
+            c0 = lo - P.hl;
+            hi = lo + P.own;
+        }
+    }
+}
+
+// A window with frame columns on both sides: no frame edge, no column
+// outside the frame.
+__device__ __forceinline__ bool band_interior(const Pass &P, int c0, int width) {
+    return c0 > 0 && c0 + width < P.W;
+}
+
 template <int S, int CPL, bool PIN, bool OUT_U, bool ENERGY, int MODE, int PROJ,
           int RULE = RULE_SKIMAGE, bool TAPE = false, bool RES = true>
 __device__ __forceinline__ void run(const Pass &P, int frame, int chunk, int band, int lane) {
     const int H = P.H, W = P.W;
     Lane<CPL> L;
-    L.col = band * P.own - P.hl + lane * CPL;
+    int c0, own_lo, own_hi;
+    band_window(P, band, 32 * CPL, c0, own_lo, own_hi);
+    L.col = c0 + lane * CPL;
     const int r0 = chunk * P.R, r1 = min(r0 + P.R, H);
     const int rs = max(0, r0 - P.ht);
-    const int own_lo = band * P.own, own_hi = min(own_lo + P.own, W);
     L.lane_own = (L.col >= own_lo) && (L.col + CPL <= own_hi);
     L.first_col = (MODE != INTERIOR) && (L.col == 0);
 #pragma unroll
@@ -675,10 +720,11 @@ template <int S, int CPL, bool PIN, bool OUT_U, bool ENERGY, int MODE>
 __device__ __forceinline__ void run2(const Pass &P, int frame, int chunk, int band, int lane) {
     const int H = P.H, W = P.W;
     Lane<CPL> L;
-    L.col = band * P.own - P.hl + lane * CPL;
+    int c0, own_lo, own_hi;
+    band_window(P, band, 32 * CPL, c0, own_lo, own_hi);
+    L.col = c0 + lane * CPL;
     const int r0 = chunk * P.R, r1 = min(r0 + P.R, H);
     const int rs = max(0, r0 - P.ht);
-    const int own_lo = band * P.own, own_hi = min(own_lo + P.own, W);
     L.lane_own = (L.col >= own_lo) && (L.col + CPL <= own_hi);
     L.first_col = (MODE != INTERIOR) && (L.col == 0);
 #pragma unroll
@@ -744,8 +790,9 @@ __device__ __forceinline__ void run2(const Pass &P, int frame, int chunk, int ba
 template <int S, int CPL, bool PIN, bool OUT_U, bool ENERGY, int LAG = 1, int PROJ = 0,
           int RULE = RULE_SKIMAGE, bool TAPE = false, bool RES = true>
 __device__ __forceinline__ void run_mode(const Pass &P, int frame, int chunk, int band, int lane) {
-    const int c0 = band * P.own - P.hl;
-    const bool interior = P.vec && c0 >= 0 && c0 + 32 * CPL - 1 <= P.W - 1;
+    int c0, lo, hi;
+    band_window(P, band, 32 * CPL, c0, lo, hi);
+    const bool interior = P.vec && band_interior(P, c0, 32 * CPL);
     static_assert(!(TAPE && LAG == 2), "the tape is written by the lag-1 pipeline");
     if (LAG == 2) {
         if (interior) run2<S, CPL, PIN, OUT_U, ENERGY, INTERIOR>(P, frame, chunk, band, lane);

@@ -308,10 +308,11 @@ __device__ __forceinline__ void srun(const Pass &P, int frame, int chunk, int ba
                                      const Rings &G) {
     const int H = P.H, W = P.W;
     SLane<CPL> L;
-    L.col = band * P.own - P.hl + lane * CPL;
+    int c0, own_lo, own_hi;
+    band_window(P, band, 32 * CPL, c0, own_lo, own_hi);
+    L.col = c0 + lane * CPL;
     const int r0 = chunk * P.R, r1 = min(r0 + P.R, H);
     const int rs = max(0, r0 - P.ht);
-    const int own_lo = band * P.own, own_hi = min(own_lo + P.own, W);
     L.lane_own = (L.col >= own_lo) && (L.col + CPL <= own_hi);
     L.first_col = (MODE != INTERIOR) && (L.col == 0);
     if (MODE != INTERIOR) {
@@ -384,8 +385,9 @@ __device__ __forceinline__ void srun(const Pass &P, int frame, int chunk, int ba
 template <int S, int CPL, bool ENERGY, int PROJ, int FORM = 1, int COH = 0>
 __device__ __forceinline__ void srun_mode(const Pass &P, int frame, int chunk, int band, int lane,
                                           const Rings &G) {
-    const int c0 = band * P.own - P.hl;
-    if (c0 >= 0 && c0 + 32 * CPL - 1 <= P.W - 1)
+    int c0, lo, hi;
+    band_window(P, band, 32 * CPL, c0, lo, hi);
+    if (band_interior(P, c0, 32 * CPL))
         srun<S, CPL, ENERGY, INTERIOR, PROJ, FORM, COH>(P, frame, chunk, band, lane, G);
     else
         srun<S, CPL, ENERGY, EDGE, PROJ, FORM, COH>(P, frame, chunk, band, lane, G);
