@@ -24,7 +24,13 @@
 //    must be ordered by the caller;
 //  * the first call on each device looks up the array's device address
 //    (cudaGetSymbolAddress, with that device current) and caches it; make
-//    that first call before any stream capture on the device.
+//    that first call before any stream capture on the device.  Later calls
+//    read the cached address without taking a lock.  The cache does not
+//    survive a reset of the device's primary context (cudaDeviceReset, or a
+//    host framework that resets the device): the library's device image is
+//    unloaded with the context, so do not call this entry point again in a
+//    process that has reset the device.
+#include <atomic>
 #include <mutex>
 
 #include "sci_common.cuh"
@@ -46,23 +52,27 @@ constexpr int kMaxDevices = 64;
 // cudaGetSymbolAddress below.
 static __device__ __align__(256) unsigned char g_tv_scratch[kScratchBytes];
 
-std::mutex g_mu;
-void *g_addr[kMaxDevices] = {};
+std::mutex g_mu;  // serialises the first lookup on a device
+std::atomic<void *> g_addr[kMaxDevices] = {};
 
-// Device address of the scratch on the current device (looked up once).
+// Device address of the scratch on the current device (looked up once; a
+// cached address is read without the lock).
 int scratch_address(void **out) {
     int dev = 0;
     SCI_CUDA(cudaGetDevice(&dev));
     SCI_CHECK_ARG(dev >= 0 && dev < kMaxDevices, "no-alloc TV: device ordinal %d out of range",
                   dev);
-    std::lock_guard<std::mutex> lk(g_mu);
-    if (!g_addr[dev]) {
-        void *p = nullptr;
-        const cudaError_t e = cudaGetSymbolAddress(&p, g_tv_scratch);
-        if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(g_tv_scratch)");
-        g_addr[dev] = p;
+    void *p = g_addr[dev].load(std::memory_order_acquire);
+    if (!p) {
+        std::lock_guard<std::mutex> lk(g_mu);
+        p = g_addr[dev].load(std::memory_order_relaxed);
+        if (!p) {
+            const cudaError_t e = cudaGetSymbolAddress(&p, g_tv_scratch);
+            if (e != cudaSuccess) return cuda_status(e, "cudaGetSymbolAddress(g_tv_scratch)");
+            g_addr[dev].store(p, std::memory_order_release);
+        }
     }
-    *out = g_addr[dev];
+    *out = p;
     return SCI_OK;
 }
 

@@ -67,6 +67,28 @@ def test_noalloc_matches_workspace_variant_twice():
         assert torch.equal(steps, ref_steps)
 
 
+def test_noalloc_edge_of_its_scratch():
+    """742 frames at n_iter_max 5 fill the 64 KiB scratch exactly and run
+    (matching the workspace variant); 743 are refused."""
+    n = ctypes.c_size_t()
+    _lib.call("sci_tv_workspace_bytes", 742, 32, 32, 5, ctypes.byref(n))
+    assert n.value <= 64 * 1024
+    _lib.call("sci_tv_workspace_bytes", 743, 32, 32, 5, ctypes.byref(n))
+    assert n.value > 64 * 1024
+    f = _frames(742, 32, 32, seed=3)
+    ref, ref_steps = _regular(f, 0.15, 5, eps=0.02)
+    u, steps = _noalloc(f, 0.15, 5, eps=0.02)
+    torch.cuda.synchronize()
+    assert float((u - ref).abs().max()) < ATOL
+    assert torch.equal(steps, ref_steps)
+    L = _lib.load()
+    g = torch.zeros((743, 32, 32), dtype=torch.float32, device=f.device)
+    v = torch.empty_like(g)
+    assert L.sci_tv_chambolle_noalloc(g.data_ptr(), v.data_ptr(), None, 743, 32, 32, 0.15, 0.02,
+                                      5, None, _dev.stream_handle()) == -1
+    assert "scratch" in _lib.last_error()
+
+
 def test_noalloc_rejects_requests_beyond_its_scratch():
     L = _lib.load()
     f = _frames(1, 16, 16, seed=1)
