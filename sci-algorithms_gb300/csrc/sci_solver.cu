@@ -35,6 +35,10 @@ int proj_gap_rn(const float *x, const float *phi, const uint32_t *mask_bits, con
 int gap_residual_rn(const float *x, const float *phi, const uint32_t *mask_bits,
                     const float *y, float *y1, const float *phisum, float *c,
                     int accelerate, int64_t B, int64_t H, int64_t W, void *stream, double *rn);
+int admm_residual_rn(const float *theta, const float *theta_old, const float *r_old,
+                     float lambda_old, const uint32_t *mask_bits, const float *y,
+                     const float *phisum, float *r_new, float *x_out, float lambda, float gamma,
+                     int first, int64_t B, int64_t H, int64_t W, void *stream, double *rn);
 int proj_admm_rn(const float *theta, const float *b, const float *phi,
                  const uint32_t *mask_bits, const float *y, const float *phisum, float *v,
                  float *x_out, float lambda, float gamma, int64_t B, int64_t H, int64_t W,
@@ -210,6 +214,37 @@ int enqueue(const Args &a, cudaStream_t s) {
     }
     // admm_denoise: theta = x0, b = 0  (pnp_sci_algo.py:800-802)
     SCI_CUDA(cudaMemcpyAsync(w.theta, a.x0, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
+    const char *af = getenv("SCI_ADMM_FUSED");
+    if (!o.tvm && a.bits && aligned && hw % 4 == 0 && tv_proj_supported(B, W, K) &&
+        !(af && af[0] == '0')) {
+        // Fused iteration: a read-only pass forms the residual map r_k from
+        // theta_k and the previous iteration's TV input (re-formed from
+        // theta_{k-1} and r_{k-1}, see k_admm_resid_vec); the TV kernel
+        // applies theta_k + lambda_k (r_k phi_b) = x - b while it loads
+        // theta_k.  theta ping-pongs between w.theta and w.b0 (theta_{k+1}
+        // overwrites theta_{k-1}), the residual maps between w.v and w.b1.
+        float *T[2] = {w.theta, w.b0};
+        float *R[2] = {w.v, w.b1};
+        for (int it = 0; it < o.iters; ++it) {
+            const bool want_x = (it == o.iters - 1) || (o.orig && o.sqerr);
+            const float gamma = o.gammas ? o.gammas[it] : o.gamma;
+            float *cur = T[it & 1], *old = T[(it + 1) & 1];
+            int e = admm_residual_rn(cur, it ? old : nullptr, it ? R[(it + 1) & 1] : nullptr,
+                                     it ? o.lambdas[it - 1] : 0.f, a.bits, a.y, a.phisum,
+                                     R[it & 1], want_x ? a.x_out : nullptr, o.lambdas[it], gamma,
+                                     it == 0, B, H, W, s, rn(it));
+            if (e) return e;
+            e = tv_launch_impl(cur, old, nullptr, B, H, W, hw, o.weights[it], o.eps, K,
+                               o.tv_steps ? o.tv_steps + (int64_t)it * B : nullptr, nullptr, w.tv,
+                               w.tv_bytes, s, 0, 0, a.bits, R[it & 1], o.lambdas[it]);
+            if (e) return e;
+            if (o.orig && o.sqerr) {
+                e = sci_sqerr_accum(o.orig, a.x_out, n, o.sqerr + it, s);
+                if (e) return e;
+            }
+        }
+        return SCI_OK;
+    }
     const char *bv = getenv("SCI_ADMM_B_FROM_V");
     if (a.bits && aligned && hw % 4 == 0 && B <= 32 && !(bv && bv[0] == '0')) {
         // b = b - (x - theta) = theta - v (pnp_sci_algo.py:836) is the TV's

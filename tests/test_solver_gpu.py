@@ -144,7 +144,11 @@ def test_graph_replay_is_bitwise_stable():
     assert torch.equal(a, b) and torch.equal(a, c)
 
 
-def test_float_mask_and_packed_mask_agree():
+def test_float_mask_and_packed_mask_agree(monkeypatch):
+    """The ADMM projection kernels on a float mask and on the packed mask
+    give the same bits (the packed mask's default fused iteration is
+    checked against this loop in test_fused_admm_iteration)."""
+    monkeypatch.setenv("SCI_ADMM_FUSED", "0")
     orig, mask, meas = sci.datasets.video_config(40, 56, 8)
     op = sci.MaskOperator(mask)
     y = _dev.plane(meas)
@@ -169,6 +173,7 @@ def test_run_host_end_to_end():
 def test_admm_multiplier_from_tv_input_is_bitwise_equal(monkeypatch, tvm, with_orig):
     """ADMM forming b = theta - v in the projection (no residual written by
     the TV) against the stored-residual loop (SCI_ADMM_B_FROM_V=0)."""
+    monkeypatch.setenv("SCI_ADMM_FUSED", "0")
     orig, mask, meas = sci.datasets.video_config(64, 96, 8, noise_rel=0.01)
     op = sci.MaskOperator(mask)
     y = _dev.plane(meas)
@@ -238,7 +243,7 @@ def test_fused_projection_path_is_bitwise_equal(monkeypatch, eps, iters, shape, 
 @pytest.mark.parametrize("kind,acc,bits,fused", [
     ("gap", True, True, False), ("gap", False, True, False), ("gap", True, False, False),
     ("gap", True, True, True), ("gap", False, True, True), ("admm", True, True, False),
-    ("admm", True, False, False)])
+    ("admm", True, False, False), ("admm", True, True, True)])
 def test_projection_residual_norm_matches_oracle(monkeypatch, kind, acc, bits, fused):
     """The FP64 ||r_k||^2 of every iteration's projection residual, summed by
     the projection kernels (bulk-copy staged, per-thread, fused residual
@@ -274,3 +279,37 @@ def test_projection_residual_norm_matches_oracle(monkeypatch, kind, acc, bits, f
     assert torch.equal(plain.run(y), s.x)
     with pytest.raises(ValueError):
         plain.resid_norms()
+
+
+@pytest.mark.parametrize("shape,cpl", [((64, 96, 8), None), ((72, 1040, 24), None),
+                                       ((40, 128, 12), "2"), ((33, 1032, 5), "4")])
+@pytest.mark.parametrize("with_orig", [False, True])
+def test_fused_admm_iteration(monkeypatch, shape, cpl, with_orig):
+    """ADMM as residual pass + TV pass with the projection applied on load
+    (the default with a packed mask) against the projection-kernel loop
+    (SCI_ADMM_FUSED=0): the same iteration re-associated (the TV input
+    formed as theta + lambda (r phi) instead of x - b), so equal to float32
+    rounding -- 1e-5 relative L2 after 12 iterations with gammas and an
+    annealed weight -- and the same per-iteration PSNR and residual norms to
+    1e-4 relative."""
+    if cpl is not None:
+        monkeypatch.setenv("SCI_TV_CPL", cpl)
+    orig, mask, meas = sci.datasets.video_config(*shape, noise_rel=0.01)
+    op = sci.MaskOperator(mask)
+    y = _dev.plane(meas)
+    o = _dev.planar(orig) if with_orig else None
+    iters = 12
+    gam = np.linspace(0.01, 0.02, iters).astype(np.float32)
+    w = np.array([0.2 * 0.25 ** (k / (iters - 1)) for k in range(iters)], np.float32)
+    runs = []
+    for fused in ("1", "0"):
+        monkeypatch.setenv("SCI_ADMM_FUSED", fused)
+        s = sci.Solver(op, "admm", iters, 1.0, w, 5, gammas=gam, resid_norm=True)
+        x = s.run(y, orig=o).clone()
+        runs.append((x, s.resid_norms(), s.psnr_all() if with_orig else None))
+    (xa, ra, pa), (xb, rb, pb) = runs
+    rel = float(torch.linalg.vector_norm(xa - xb) / torch.linalg.vector_norm(xb))
+    assert rel < 1e-5, rel
+    assert np.allclose(ra, rb, rtol=1e-4, atol=0)
+    if with_orig:
+        assert np.allclose(pa, pb, rtol=0, atol=1e-3)
