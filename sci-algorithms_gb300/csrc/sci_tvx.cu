@@ -103,29 +103,26 @@ __device__ __forceinline__ void cp4_wait() {
     asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory");
 }
 
-template <int S, int NT>
-__global__ void __launch_bounds__(32 * FL, 2) k_itv3d_cham(
+// EDGE: the strip holds column 0 or W - 1 (or columns outside the frame);
+// interior strips compile without the edge selects.  The square root and
+// reciprocal of the dual update are the approximate MUFU forms, and the
+// output divides by lambda as a product with its reciprocal.
+template <int S, int NT, bool EDGE>
+__device__ __forceinline__ void itv3d_body(
     const float *__restrict__ f, const float *__restrict__ pin1, const float *__restrict__ pin2,
     float *__restrict__ u, float *__restrict__ resid, float *__restrict__ pout1,
-    float *__restrict__ pout2, Geo g, int nf, float lam, float dt, int R, int own, int pin,
-    int out) {
+    float *__restrict__ pout2, const Geo &g, int nf, float lam, float dt, int R, int own, int pin,
+    int out, float (&ring)[IT3_RING][NT * FL][32], float (&red)[2][S][32][FL]) {
     constexpr int PF = IT3_RING - S - 1;  // rows prefetched ahead
     static_assert(S >= 1 && S <= 5 && PF >= 2, "ITV3D pass: 1..5 updates");
     static_assert((IT3_RING & (IT3_RING - 1)) == 0 && FL == 8, "ring slots by mask");
-    __shared__ float ring[IT3_RING][NT * FL][32];
-    // per-pixel sums of the frame lanes, [row parity][update][column][lane
-    // slot]: a column's FL sums are one 32-byte row, read with two vector
-    // loads; the slot is the frame lane XOR (column / 4) % FL, so the FL
-    // lanes' stores of one warp hit distinct banks.  Every warp adds a
-    // column's slots in the same (slot) order, so all frames of a pixel see
-    // the same total.
-    __shared__ __align__(16) float red[2][S][32][FL];
     const int lane = threadIdx.x, w = threadIdx.y;
     const int H = g.H, W = g.W;
     const int col = blockIdx.x * own - (S + 1) + lane;
-    const int colc = min(max(col, 0), W - 1);
+    const int colc = EDGE ? min(max(col, 0), W - 1) : col;
     const bool owned = lane >= S + 1 && lane < S + 1 + own && col < W;
-    const bool first_col = col <= 0, last_col = col >= W - 1;
+    const bool first_col = EDGE && col <= 0, last_col = EDGE && col >= W - 1;
+    const float ilam = 1.f / lam;
     const int slot = w ^ ((lane >> 2) & (FL - 1));
     const int r0 = blockIdx.y * R, r1 = min(r0 + R, H);
     const int rs = max(0, r0 - S - 1), re = r1 - 1 + S;  // input rows rs.., last step re
@@ -204,7 +201,7 @@ __global__ void __launch_bounds__(32 * FL, 2) k_itv3d_cham(
                 const float4 v0 = *reinterpret_cast<const float4 *>(&rs_[0]);
                 const float4 v1 = *reinterpret_cast<const float4 *>(&rs_[4]);
                 const float tot = ((((((v0.x + v0.y) + v0.z) + v0.w) + v1.x) + v1.y) + v1.z) + v1.w;
-                const float rd = __frcp_rn(1.f + dt * sqrtf(tot));
+                const float rd = rcp_approx(fmaf(dt, sqrt_approx(tot), 1.f));
                 // p^{k+1} of row b becomes the next update's input row
 #pragma unroll
                 for (int t = 0; t < NT; ++t) {
@@ -250,7 +247,7 @@ __global__ void __launch_bounds__(32 * FL, 2) k_itv3d_cham(
             const float up = (!FAST && a == 0) ? in2[t] : p2o[t];
             p2o[t] = in2[t];
             const float fa = ring[a & (IT3_RING - 1)][w + t * FL][lane];
-            const float x = fa - (((in1[t] - l) + in2[t]) - up) / lam;
+            const float x = fa - (((in1[t] - l) + in2[t]) - up) * ilam;
             if (keep && fv[t]) {
                 u[fo[t] + (int64_t)a * W] = x;
                 if (resid) resid[fo[t] + (int64_t)a * W] = x - fa;
@@ -267,6 +264,29 @@ __global__ void __launch_bounds__(32 * FL, 2) k_itv3d_cham(
     for (; r <= fe; ++r) step(r, std::true_type{});
     for (; r <= re; ++r) step(r, std::false_type{});
     asm volatile("cp.async.wait_all;\n" ::: "memory");
+}
+
+template <int S, int NT>
+__global__ void __launch_bounds__(32 * FL, 2) k_itv3d_cham(
+    const float *__restrict__ f, const float *__restrict__ pin1, const float *__restrict__ pin2,
+    float *__restrict__ u, float *__restrict__ resid, float *__restrict__ pout1,
+    float *__restrict__ pout2, Geo g, int nf, float lam, float dt, int R, int own, int pin,
+    int out) {
+    __shared__ float ring[IT3_RING][NT * FL][32];
+    // per-pixel sums of the frame lanes, [row parity][update][column][lane
+    // slot]: a column's FL sums are one 32-byte row, read with two vector
+    // loads; the slot is the frame lane XOR (column / 4) % FL, so the FL
+    // lanes' stores of one warp hit distinct banks.  Every warp adds a
+    // column's slots in the same (slot) order, so all frames of a pixel see
+    // the same total.
+    __shared__ __align__(16) float red[2][S][32][FL];
+    const int c0 = blockIdx.x * own - (S + 1);  // the strip's first column
+    if (c0 >= 1 && c0 + 31 <= g.W - 2)
+        itv3d_body<S, NT, false>(f, pin1, pin2, u, resid, pout1, pout2, g, nf, lam, dt, R, own,
+                                 pin, out, ring, red);
+    else
+        itv3d_body<S, NT, true>(f, pin1, pin2, u, resid, pout1, pout2, g, nf, lam, dt, R, own,
+                                pin, out, ring, red);
 }
 
 // ------------------------------------------------------------ FGP family
