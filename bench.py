@@ -689,12 +689,12 @@ def run_kernel(args):
              y1.data_ptr(), op.phisum.data_ptr(), cmap.data_ptr(), 1, F, H, W, s.cuda_stream)
 
     gap = None
-    if args.kernel == "gap":
+    if args.kernel in ("gap", "admm"):
         # whole solves (residual pass, TV pass with the projection applied
         # on load, stop test), 60 iterations, annealed weight
         weights = np.array([0.2 * 0.25 ** (k / (ITERS - 1)) for k in range(ITERS)], np.float32)
-        gap = sci.Solver(op, "gap", ITERS, 1.0, weights, TV_ITERS, accelerate=True,
-                         use_graph=False)
+        kw = {"accelerate": True} if args.kernel == "gap" else {"gamma": 0.01}
+        gap = sci.Solver(op, args.kernel, ITERS, 1.0, weights, TV_ITERS, use_graph=False, **kw)
     sums = torch.zeros((2, F), dtype=torch.float64, device=dev)
     if args.kernel == "metrics":
         out.copy_(x * 0.9)
@@ -709,7 +709,8 @@ def run_kernel(args):
         sci.tv_matlab_frames(x, 7, 1.0 / 0.07, 5, u=out, workspace=wsm)
 
     fn = {"tv": tv_once, "proj": proj_once, "proj_admm": proj_admm_once, "resid": resid_once,
-          "gap": (lambda: gap.run(y)), "metrics": metrics_once, "itv3d": itv3d_once}[args.kernel]
+          "gap": (lambda: gap.run(y)), "admm": (lambda: gap.run(y)), "metrics": metrics_once,
+          "itv3d": itv3d_once}[args.kernel]
     fn()
     torch.cuda.synchronize()
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -1018,8 +1019,8 @@ def main():
                     help="skip the per-configuration comparison with the float64 oracle")
     ap.add_argument("--parity-size", type=int, default=H,
                     help="H = W of the 60-iteration video parity solves (2048: the timed workload)")
-    ap.add_argument("--kernel", choices=["tv", "proj", "proj_admm", "resid", "gap", "metrics",
-                                         "itv3d", "batch", "unrolled", "cnn", "cassi"],
+    ap.add_argument("--kernel", choices=["tv", "proj", "proj_admm", "resid", "gap", "admm",
+                                         "metrics", "itv3d", "batch", "unrolled", "cnn", "cassi"],
                     default=None,
                     help="profiling mode: time one kernel on a 2048x2048xFRAMES stack")
     ap.add_argument("--frames", type=int, default=8)
