@@ -1,7 +1,13 @@
 // Host driver of the Chambolle TV (all passes of one call) and its C ABI.
 // The kernels are in sci_tv.cuh (instantiated in sci_tv_k4.cu,
 // sci_tv_k123.cu and sci_tv_fix.cu).
+#include <algorithm>
 #include <cstdlib>
+#include <map>
+#include <mutex>
+#include <queue>
+#include <tuple>
+#include <vector>
 
 #include "sci_tv.cuh"
 
@@ -79,28 +85,65 @@ static int choose_R(int64_t nf, int nbands, int H) {
     return R;
 }
 
-// Rows per chunk for the register-lean pass: the grid runs in waves of
-// `resident` warps, each work item of R rows costs about R + S + 4 pipeline
-// steps, so the chunking that minimises waves x (R + S + 4) is taken (a
-// last wave that is half empty costs a whole wave).
-static int choose_R_slim(int64_t nf, int nbands, int H, int S, int64_t resident) {
+// Finish time of a grid whose blocks (WPB consecutive work items each, in
+// launch order) are taken by `slots` resident block slots, each slot taking
+// the next block as soon as it is free; a block costs its longest item.
+static double grid_makespan(const std::vector<int> &item_cost, int slots) {
+    std::priority_queue<double, std::vector<double>, std::greater<double>> free_at;
+    for (int i = 0; i < slots; ++i) free_at.push(0.0);
+    double end = 0.0;
+    for (size_t b = 0; b < item_cost.size(); b += WPB) {
+        int c = 0;
+        for (size_t i = b; i < std::min(item_cost.size(), b + WPB); ++i)
+            c = std::max(c, item_cost[i]);
+        const double t = free_at.top() + c;
+        free_at.pop();
+        free_at.push(t);
+        end = std::max(end, t);
+    }
+    return end;
+}
+
+// Rows per chunk for the register-lean pass: a work item of R rows costs
+// about R + S + 4 pipeline steps, and the chunk count whose grid finishes
+// first in the slot model of grid_makespan is taken (a last wave that is
+// half empty costs a whole wave there).  Results are cached per shape.
+// Measured: this choice 2311 iter/s on the 2048 x 2048 x 24 GAP-TV solve
+// against 2294 for the wave-count formula it replaced; tall chunks followed
+// by short ones for the grid's tail (1 % shorter in the model) measured no
+// faster (a partly empty last wave costs less than the model says: the
+// SMs that run fewer blocks run them faster).
+static int choose_R_slim(int64_t nf, int nbands, int H, int S, int slots) {
     if (const char *e = getenv("SCI_TV_R")) {
         const int v = atoi(e);
         if (v >= 8) return v;
     }
+    static std::mutex mu;
+    static std::map<std::tuple<int64_t, int, int, int, int>, int> cache;
+    const auto key = std::make_tuple(nf, nbands, H, S, slots);
+    {
+        std::lock_guard<std::mutex> lock(mu);
+        auto it = cache.find(key);
+        if (it != cache.end()) return it->second;
+    }
+    const int64_t cols = nf * (int64_t)nbands;  // items per chunk row
+    std::vector<int> cost;
     int best_R = H;
-    double best = -1.0;
+    double best_t = -1.0;
     const int max_chunks = std::max(1, H / 16);
     for (int nc = 1; nc <= max_chunks; ++nc) {
         const int R = (H + nc - 1) / nc;
-        const int64_t items = nf * nbands * (int64_t)((H + R - 1) / R);
-        const int64_t waves = (items + resident - 1) / resident;
-        const double cost = (double)waves * (R + S + 4);
-        if (best < 0.0 || cost < best - 1e-9) {
-            best = cost;
+        cost.clear();
+        for (int r0 = 0; r0 < H; r0 += R)
+            cost.insert(cost.end(), (size_t)cols, std::min(R, H - r0) + S + 4);
+        const double t = grid_makespan(cost, slots);
+        if (best_t < 0.0 || t < best_t - 1e-9) {
+            best_t = t;
             best_R = R;
         }
     }
+    std::lock_guard<std::mutex> lock(mu);
+    cache[key] = best_R;
     return best_R;
 }
 
@@ -284,7 +327,7 @@ static int tv_launch_core(const float *f, float *u, float *resid, int64_t nf, in
         if (force_R > 0) P.R = force_R;
         else if (slim)
             P.R = choose_R_slim(nf, P.nbands, (int)H, SG,
-                                (int64_t)kSMs * slim_resident_blocks(cpl, SG, minb, proj) * WPB);
+                                kSMs * slim_resident_blocks(cpl, SG, minb, proj));
         else P.R = choose_R(nf, P.nbands, (int)H);
         P.nchunks = (int)((H + P.R - 1) / P.R);
         P.S = SG;
