@@ -353,9 +353,10 @@ int sci_unrolled_fwd(const float *logits, const float *lambdas,
 
 /* Reverse pass of the preceding sci_unrolled_fwd on the same workspace and
  * arguments: grad_logits (B x H x W) and grad_lambdas (device double[K])
- * of grad_loss * loss.  Reads the TV tape the forward kept (when the tapes
- * of all K iterations fit in 48 GiB of workspace; sci_unrolled_workspace_bytes
- * includes them) or recomputes each TV call from its checkpoint. */
+ * of grad_loss * loss.  Recomputes each TV call from its checkpoint, or,
+ * with SCI_UNROLLED_TAPE=1 set for the forward and the workspace query,
+ * reads the TV tape the forward kept (when the tapes of all K iterations
+ * fit in 48 GiB of workspace; sci_unrolled_workspace_bytes includes them). */
 int sci_unrolled_bwd(const float *logits, const float *lambdas,
                      const float *x_true, int64_t N, int64_t B, int64_t H,
                      int64_t W, int K, int tv_iters, float tv_weight,

@@ -9,9 +9,10 @@
 //     v^k = x^k + lambda_k At(q);   x^{k+1} = TV(v^k)   (fixed T Chambolle
 //     steps, no stop test: the stop rule is not differentiable)
 //   loss = mean (x^K - x_true)^2.
-// The forward keeps x^k and y1^k and, when they fit (up to 48 GiB), v^k and
-// the tape (u_k, p_{k+1}) its TV pipeline writes as it runs; otherwise the
-// reverse pass recomputes each TV call from v^k step by step.  The reverse
+// The forward keeps x^k and y1^k and the reverse pass recomputes v^k and
+// each TV call from v^k step by step; with SCI_UNROLLED_TAPE=1 the forward
+// also keeps, when they fit (up to 48 GiB), v^k and the tape (u_k, p_{k+1})
+// its TV pipeline writes as it runs, and the reverse pass reads them.  The reverse
 // pass runs the adjoint of every TV step:
 //   p_{k+1} = (p_k - tau g_k) r_k,  r_k = 1 / (1 + (tau/w) n_k),  n_k = |g_k|,
 //   gbar_k = -tau r_k pbar_{k+1} - (tau/w) r_k (g_k / n_k) <pbar_{k+1}, p_{k+1}>
@@ -464,11 +465,13 @@ struct Ws {
 };
 
 // Whether the forward keeps v^k and the TV tape of every outer iteration
-// (3 (T-1) planes per iteration) for the reverse pass: up to 48 GiB, unless
-// SCI_UNROLLED_TAPE=0 (then the reverse pass recomputes them).
+// (3 (T-1) planes per iteration) for the reverse pass.  By default it keeps
+// only the outer iterates and the reverse pass recomputes each inner TV
+// loop (the checkpoint-only form); SCI_UNROLLED_TAPE=1 stores the tapes
+// instead when they fit in 48 GiB.
 bool stored_tape(int64_t N, int64_t B, int64_t H, int64_t W, int K, int T) {
     const char *e = getenv("SCI_UNROLLED_TAPE");
-    if (e && e[0] == '0') return false;
+    if (!(e && e[0] == '1')) return false;
     const double bytes = 4.0 * (double)(N * B * H * W) * 3.0 * (T - 1) * K;
     return bytes <= 48.0 * (1ull << 30);
 }

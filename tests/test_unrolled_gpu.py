@@ -61,14 +61,14 @@ def test_unrolled_matches_fp64_autograd(N, B, H, W, K, T):
 
 @pytest.mark.parametrize("T", [5, 3])
 def test_stored_tape_and_recompute_agree(monkeypatch, T):
-    """The reverse pass on the tape the forward TV kept against the one that
-    recomputes it (SCI_UNROLLED_TAPE=0): the same adjoint of (almost) the
-    same tape."""
+    """The reverse pass on the tape the forward TV kept (SCI_UNROLLED_TAPE=1)
+    against the default that recomputes it: the same adjoint of (almost)
+    the same tape."""
     N, B, H, W, K = 2, 8, 48, 72, 5
     logits, lambdas, x_true = problem(N, B, H, W, K, seed=5)
-    l1, g1, m1 = ours(logits, lambdas, x_true, K, T)
-    monkeypatch.setenv("SCI_UNROLLED_TAPE", "0")
     l2, g2, m2 = ours(logits, lambdas, x_true, K, T)
+    monkeypatch.setenv("SCI_UNROLLED_TAPE", "1")
+    l1, g1, m1 = ours(logits, lambdas, x_true, K, T)
     assert abs(float(l1) - float(l2)) <= 1e-6 * abs(float(l2))
     assert rel(g1, g2) < 1e-5
     assert rel(m1, m2) < 1e-5
