@@ -141,8 +141,11 @@ template <bool ACC>
 __global__ void __launch_bounds__(1024) k_cassi_proj_rows(
     const float *__restrict__ x, const float *__restrict__ phi, const float *__restrict__ y,
     float *__restrict__ y1, const float *__restrict__ ps, float *__restrict__ xo, float lam,
-    int L, int H, int W, int step) {
+    int L, int H, int W, int step, double *__restrict__ zero, int nzero) {
     extern __shared__ float rs[];
+    grid_dep_wait();
+    if (blockIdx.x == 0)  // the next TV pass's stop-test sums
+        for (int i = threadIdx.x; i < nzero; i += blockDim.x) zero[i] = 0.0;
     const int Wd = W + step * (L - 1);
     const int64_t hw = (int64_t)H * W;
     for (int h = blockIdx.x; h < H; h += gridDim.x) {
@@ -205,9 +208,10 @@ int check(int64_t L, int64_t H, int64_t W, int step) {
 
 }  // namespace
 
-int tv_launch(const float *f, float *u, float *resid, int64_t nf, int64_t H, int64_t W,
-              int64_t fs, float weight, float eps, int K, int *steps, double *energy_out,
-              void *workspace, size_t ws_bytes, cudaStream_t s, int force_R);
+int tv_launch_flags(const float *f, float *u, float *resid, int64_t nf, int64_t H, int64_t W,
+                    int64_t fs, float weight, float eps, int K, int *steps, double *energy_out,
+                    void *workspace, size_t ws_bytes, cudaStream_t s, int force_R, int flags);
+double *tv_clear_region(int64_t nf, int64_t H, int64_t W, int K, void *workspace, int *words);
 size_t tv_workspace_bytes(int64_t nf, int64_t H, int64_t W, int K);
 
 static size_t r256(size_t b) { return (b + 255) & ~size_t(255); }
@@ -294,6 +298,10 @@ int sci_cassi_gap_tv(const float *y, const float *phi, const float *phisum, cons
     const size_t row_smem = sizeof(float) * (size_t)(W + step * (L - 1));
     const bool rows = row_smem <= kRowSmemMax && rows_enabled();
     const int rt = row_threads();
+    // the row-fused projection also clears the TV pass's stop-test sums, so
+    // that the TV kernel follows it directly (flags 4)
+    int nzero = 0;
+    double *zero = rows ? tv_clear_region(L, H, W, o->tv_iter_max, tv, &nzero) : nullptr;
     auto enqueue = [&](cudaStream_t s) -> int {
         if (x0 != x_out) SCI_CUDA(cudaMemcpyAsync(x_out, x0, 4 * n, cudaMemcpyDeviceToDevice, s));
         if (o->accelerate) SCI_CUDA(cudaMemsetAsync(y1, 0, 4 * nd, s));
@@ -303,13 +311,13 @@ int sci_cassi_gap_tv(const float *y, const float *phi, const float *phisum, cons
             if (rows) {
                 const unsigned g = (unsigned)std::min<int64_t>(H, (int64_t)kSMs * 8);
                 if (o->accelerate)
-                    k_cassi_proj_rows<true><<<g, rt, row_smem, s>>>(
-                        x_out, phi, y, y1, phisum, xp, o->lambdas[it], (int)L, (int)H, (int)W,
-                        step);
+                    SCI_CUDA(launch_dep(k_cassi_proj_rows<true>, dim3(g), dim3(rt), row_smem, s,
+                                        x_out, phi, y, y1, phisum, xp, o->lambdas[it], (int)L,
+                                        (int)H, (int)W, step, zero, nzero));
                 else
-                    k_cassi_proj_rows<false><<<g, rt, row_smem, s>>>(
-                        x_out, phi, y, y1, phisum, xp, o->lambdas[it], (int)L, (int)H, (int)W,
-                        step);
+                    SCI_CUDA(launch_dep(k_cassi_proj_rows<false>, dim3(g), dim3(rt), row_smem, s,
+                                        x_out, phi, y, y1, phisum, xp, o->lambdas[it], (int)L,
+                                        (int)H, (int)W, step, zero, nzero));
                 SCI_LAUNCHED("k_cassi_proj_rows");
             } else {
                 if (o->accelerate)
@@ -323,10 +331,10 @@ int sci_cassi_gap_tv(const float *y, const float *phi, const float *phisum, cons
                                                              (int)L, (int)H, (int)W, step);
                 SCI_LAUNCHED("k_cassi_update");
             }
-            int e = tv_launch(xp, x_out, nullptr, L, H, W, H * W, o->weights[it], o->eps,
-                              o->tv_iter_max,
-                              o->tv_steps ? o->tv_steps + (int64_t)it * L : nullptr, nullptr, tv,
-                              tvb, s, 0);
+            int e = tv_launch_flags(xp, x_out, nullptr, L, H, W, H * W, o->weights[it], o->eps,
+                                    o->tv_iter_max,
+                                    o->tv_steps ? o->tv_steps + (int64_t)it * L : nullptr,
+                                    nullptr, tv, tvb, s, 0, rows ? 4 : 0);
             if (e) return e;
             if (o->orig && o->sqerr) {
                 e = sci_sqerr_accum(o->orig, x_out, n, o->sqerr + it, s);

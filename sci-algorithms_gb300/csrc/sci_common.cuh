@@ -6,6 +6,7 @@
 #include <cstdint>
 #include <cstdio>
 #include <string>
+#include <utility>
 
 #include "sci_gb300.h"
 
@@ -36,6 +37,36 @@ inline cudaStream_t as_stream(void *s) { return reinterpret_cast<cudaStream_t>(s
 inline bool aligned16(const void *p) { return (reinterpret_cast<uintptr_t>(p) & 15u) == 0; }
 
 constexpr int kSMs = 152;  // GB300: 2 dies x 76 SMs
+
+// ------------------------------------------- programmatic dependent launch
+// The iteration kernels of the solvers (residual passes, TV passes, their
+// stop-test launches, the spectral projection) are launched so that a
+// kernel's blocks may be scheduled while its predecessor in the stream
+// drains; each of them calls grid_dep_wait() before it touches memory, which
+// returns once the predecessor grid has completed and its writes are
+// visible (a no-op for a normal launch).  This hides the launch gap between
+// consecutive kernels.  SCI_PDL=0 launches them normally.
+bool pdl_enabled();
+
+template <typename... K, typename... A>
+cudaError_t launch_dep(void (*kernel)(K...), dim3 grid, dim3 block, size_t smem,
+                       cudaStream_t s, A &&...args) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = grid;
+    cfg.blockDim = block;
+    cfg.dynamicSmemBytes = smem;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+    at[0].val.programmaticStreamSerializationAllowed = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = pdl_enabled() ? 1 : 0;
+    return cudaLaunchKernelEx(&cfg, kernel, std::forward<A>(args)...);
+}
+
+__device__ __forceinline__ void grid_dep_wait() {
+    asm volatile("griddepcontrol.wait;" ::: "memory");
+}
 
 // ------------------------------------------------------------- device side
 __device__ __forceinline__ float4 ldg4(const float *p) {

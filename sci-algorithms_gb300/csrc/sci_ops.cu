@@ -32,6 +32,11 @@ int cuda_status(cudaError_t e, const char *what) {
     return SCI_ERR_CUDA;
 }
 
+bool pdl_enabled() {
+    const char *e = getenv("SCI_PDL");
+    return !(e && atoi(e) == 0);
+}
+
 int launch_proj_gap_tma(const float *x, const uint32_t *bits, const float *y, float *y1,
                         const float *phisum, float *xo, float lam, bool acc, int B, int64_t hw,
                         cudaStream_t s, double *rn);
@@ -345,7 +350,10 @@ template <int MODE, bool ACC>
 __global__ void __launch_bounds__(256) k_gap_resid_vec(
     const float *__restrict__ x, Mask<MODE> M, const float *__restrict__ y,
     float *__restrict__ y1, const float *__restrict__ phisum, float *__restrict__ c, int B,
-    int64_t hw, double *__restrict__ rn) {
+    int64_t hw, double *__restrict__ rn, double *__restrict__ zero, int nzero) {
+    grid_dep_wait();
+    if (blockIdx.x == 0)  // the next TV pass's stop-test sums
+        for (int i = threadIdx.x; i < nzero; i += blockDim.x) zero[i] = 0.0;
     const int64_t n4 = hw >> 2;
     double racc = 0.0;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n4;
@@ -409,7 +417,10 @@ __global__ void __launch_bounds__(256) k_admm_resid_vec(
     const float *__restrict__ th, const float *__restrict__ tho, const float *__restrict__ rold,
     float lam_old, Mask<1> M, const float *__restrict__ y, const float *__restrict__ phisum,
     float *__restrict__ rnew, float *__restrict__ xo, float lam, float gamma, int B, int64_t hw,
-    double *__restrict__ rn) {
+    double *__restrict__ rn, double *__restrict__ zero, int nzero) {
+    grid_dep_wait();
+    if (blockIdx.x == 0)  // the next TV pass's stop-test sums
+        for (int i = threadIdx.x; i < nzero; i += blockDim.x) zero[i] = 0.0;
     const int64_t n4 = hw >> 2;
     double racc = 0.0;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n4;
@@ -612,7 +623,8 @@ int proj_gap_rn(const float *x, const float *phi, const uint32_t *mask_bits, con
 
 int gap_residual_rn(const float *x, const float *phi, const uint32_t *mask_bits,
                      const float *y, float *y1, const float *phisum, float *c,
-                     int accelerate, int64_t B, int64_t H, int64_t W, void *stream, double *rn) {
+                     int accelerate, int64_t B, int64_t H, int64_t W, void *stream, double *rn,
+                     double *zero, int nzero) {
     if (int e = check_dims(B, H, W)) return e;
     SCI_CHECK_ARG(x && y && phisum && c && (phi || mask_bits), "sci_gap_residual: null pointer");
     SCI_CHECK_ARG(!accelerate || y1, "sci_gap_residual: accelerate needs y1");
@@ -624,12 +636,16 @@ int gap_residual_rn(const float *x, const float *phi, const uint32_t *mask_bits,
     const dim3 g = grid_for(hw / 4, 256);
     if (mask_bits) {
         Mask<1> M{mask_bits, hw};
-        if (accelerate) k_gap_resid_vec<1, true><<<g, 256, 0, s>>>(x, M, y, y1, phisum, c, (int)B, hw, rn);
-        else k_gap_resid_vec<1, false><<<g, 256, 0, s>>>(x, M, y, y1, phisum, c, (int)B, hw, rn);
+        if (accelerate) SCI_CUDA(launch_dep(k_gap_resid_vec<1, true>, g, dim3(256), 0, s, x, M, y, y1,
+                                        phisum, c, (int)B, hw, rn, zero, nzero));
+        else SCI_CUDA(launch_dep(k_gap_resid_vec<1, false>, g, dim3(256), 0, s, x, M, y, y1,
+                                        phisum, c, (int)B, hw, rn, zero, nzero));
     } else {
         Mask<0> M{phi, hw};
-        if (accelerate) k_gap_resid_vec<0, true><<<g, 256, 0, s>>>(x, M, y, y1, phisum, c, (int)B, hw, rn);
-        else k_gap_resid_vec<0, false><<<g, 256, 0, s>>>(x, M, y, y1, phisum, c, (int)B, hw, rn);
+        if (accelerate) SCI_CUDA(launch_dep(k_gap_resid_vec<0, true>, g, dim3(256), 0, s, x, M, y, y1,
+                                        phisum, c, (int)B, hw, rn, zero, nzero));
+        else SCI_CUDA(launch_dep(k_gap_resid_vec<0, false>, g, dim3(256), 0, s, x, M, y, y1,
+                                        phisum, c, (int)B, hw, rn, zero, nzero));
     }
     SCI_LAUNCHED("k_gap_resid");
     return SCI_OK;
@@ -641,7 +657,8 @@ int gap_residual_rn(const float *x, const float *phi, const uint32_t *mask_bits,
 int admm_residual_rn(const float *theta, const float *theta_old, const float *r_old,
                      float lambda_old, const uint32_t *mask_bits, const float *y,
                      const float *phisum, float *r_new, float *x_out, float lambda, float gamma,
-                     int first, int64_t B, int64_t H, int64_t W, void *stream, double *rn) {
+                     int first, int64_t B, int64_t H, int64_t W, void *stream, double *rn,
+                     double *zero, int nzero) {
     if (int e = check_dims(B, H, W)) return e;
     SCI_CHECK_ARG(theta && y && phisum && r_new && mask_bits && (first || (theta_old && r_old)),
                   "admm residual: null pointer");
@@ -653,8 +670,9 @@ int admm_residual_rn(const float *theta, const float *theta_old, const float *r_
     const dim3 g = grid_for(hw / 4, 256);
     Mask<1> M{mask_bits, hw};
 #define SCI_ADMM_RESID(F, X)                                                                    \
-    k_admm_resid_vec<F, X><<<g, 256, 0, s>>>(theta, theta_old, r_old, lambda_old, M, y, phisum, \
-                                             r_new, x_out, lambda, gamma, (int)B, hw, rn)
+    SCI_CUDA(launch_dep(k_admm_resid_vec<F, X>, g, dim3(256), 0, s, theta, theta_old, r_old,    \
+                        lambda_old, M, y, phisum, r_new, x_out, lambda, gamma, (int)B, hw, rn, \
+                        zero, nzero))
     if (first) {
         if (x_out) SCI_ADMM_RESID(true, true);
         else SCI_ADMM_RESID(true, false);
@@ -785,7 +803,7 @@ int sci_gap_residual(const float *x, const float *phi, const uint32_t *mask_bits
                      const float *y, float *y1, const float *phisum, float *c,
                      int accelerate, int64_t B, int64_t H, int64_t W, void *stream) {
     return sci::gap_residual_rn(x, phi, mask_bits, y, y1, phisum, c, accelerate, B, H, W,
-                                stream, nullptr);
+                                stream, nullptr, nullptr, 0);
 }
 
 int sci_proj_admm(const float *theta, const float *b, const float *phi,

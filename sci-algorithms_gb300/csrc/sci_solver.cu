@@ -34,11 +34,14 @@ int proj_gap_rn(const float *x, const float *phi, const uint32_t *mask_bits, con
                 int64_t B, int64_t H, int64_t W, void *stream, double *rn);
 int gap_residual_rn(const float *x, const float *phi, const uint32_t *mask_bits,
                     const float *y, float *y1, const float *phisum, float *c,
-                    int accelerate, int64_t B, int64_t H, int64_t W, void *stream, double *rn);
+                    int accelerate, int64_t B, int64_t H, int64_t W, void *stream, double *rn,
+                    double *zero, int nzero);
+double *tv_clear_region(int64_t nf, int64_t H, int64_t W, int K, void *workspace, int *words);
 int admm_residual_rn(const float *theta, const float *theta_old, const float *r_old,
                      float lambda_old, const uint32_t *mask_bits, const float *y,
                      const float *phisum, float *r_new, float *x_out, float lambda, float gamma,
-                     int first, int64_t B, int64_t H, int64_t W, void *stream, double *rn);
+                     int first, int64_t B, int64_t H, int64_t W, void *stream, double *rn,
+                     double *zero, int nzero);
 int proj_admm_rn(const float *theta, const float *b, const float *phi,
                  const uint32_t *mask_bits, const float *y, const float *phisum, float *v,
                  float *x_out, float lambda, float gamma, int64_t B, int64_t H, int64_t W,
@@ -177,15 +180,19 @@ int enqueue(const Args &a, cudaStream_t s) {
         if (a.x0 != X[start])
             SCI_CUDA(cudaMemcpyAsync(X[start], a.x0, sizeof(float) * n, cudaMemcpyDeviceToDevice, s));
         if (o.accelerate) SCI_CUDA(cudaMemsetAsync(w.y1, 0, sizeof(float) * hw, s));
+        // the residual pass also clears the TV pass's stop-test sums, so
+        // that the TV kernel follows it directly (flags 4)
+        int nzero = 0;
+        double *zero = tv_clear_region(B, H, W, K, w.tv, &nzero);
         for (int it = 0; it < o.iters; ++it) {
             const float *cur = X[(start + it) & 1];
             float *nxt = X[(start + it + 1) & 1];
             int e = gap_residual_rn(cur, nullptr, a.bits, a.y, w.y1, a.phisum, w.c,
-                                    o.accelerate, B, H, W, s, rn(it));
+                                    o.accelerate, B, H, W, s, rn(it), zero, nzero);
             if (e) return e;
             e = tv_launch_impl(cur, nxt, nullptr, B, H, W, hw, o.weights[it], o.eps, K,
                                o.tv_steps ? o.tv_steps + (int64_t)it * B : nullptr, nullptr, w.tv,
-                               w.tv_bytes, s, 0, 0, a.bits, w.c, o.lambdas[it]);
+                               w.tv_bytes, s, 0, 4, a.bits, w.c, o.lambdas[it]);
             if (e) return e;
             if (o.orig && o.sqerr) {
                 e = sci_sqerr_accum(o.orig, nxt, n, o.sqerr + it, s);
@@ -225,6 +232,8 @@ int enqueue(const Args &a, cudaStream_t s) {
         // overwrites theta_{k-1}), the residual maps between w.v and w.b1.
         float *T[2] = {w.theta, w.b0};
         float *R[2] = {w.v, w.b1};
+        int nzero = 0;
+        double *zero = tv_clear_region(B, H, W, K, w.tv, &nzero);
         for (int it = 0; it < o.iters; ++it) {
             const bool want_x = (it == o.iters - 1) || (o.orig && o.sqerr);
             const float gamma = o.gammas ? o.gammas[it] : o.gamma;
@@ -232,11 +241,11 @@ int enqueue(const Args &a, cudaStream_t s) {
             int e = admm_residual_rn(cur, it ? old : nullptr, it ? R[(it + 1) & 1] : nullptr,
                                      it ? o.lambdas[it - 1] : 0.f, a.bits, a.y, a.phisum,
                                      R[it & 1], want_x ? a.x_out : nullptr, o.lambdas[it], gamma,
-                                     it == 0, B, H, W, s, rn(it));
+                                     it == 0, B, H, W, s, rn(it), zero, nzero);
             if (e) return e;
             e = tv_launch_impl(cur, old, nullptr, B, H, W, hw, o.weights[it], o.eps, K,
                                o.tv_steps ? o.tv_steps + (int64_t)it * B : nullptr, nullptr, w.tv,
-                               w.tv_bytes, s, 0, 0, a.bits, R[it & 1], o.lambdas[it]);
+                               w.tv_bytes, s, 0, 4, a.bits, R[it & 1], o.lambdas[it]);
             if (e) return e;
             if (o.orig && o.sqerr) {
                 e = sci_sqerr_accum(o.orig, a.x_out, n, o.sqerr + it, s);

@@ -246,7 +246,14 @@ static int tv_launch_core(const float *f, float *u, float *resid, int64_t nf, in
     ws_layout(nf, H, W, K, &w, static_cast<char *>(workspace));
     double *energy = energy_out ? energy_out : w.energy;
     const size_t ne = sizeof(double) * (size_t)(nf * K * 2);
-    if (energy == w.energy) {
+    // flags & 4: the caller's preceding kernel cleared the energy sums and
+    // the ticket (tv_clear_region), so that this launch follows it directly
+    // (a memset node between two kernels of the solver graphs cost about
+    // 6 us per iteration); runs without a stop test read neither
+    SCI_CHECK_ARG(!(flags & 4) || energy == w.energy,
+                  "tv: pre-cleared sums need the workspace's own energy buffer");
+    if ((flags & 4) || (no_stop && !energy_out)) {
+    } else if (energy == w.energy) {
         SCI_CUDA(cudaMemsetAsync(energy, 0, ne + sizeof(unsigned), s));  // and the ticket
     } else {
         SCI_CUDA(cudaMemsetAsync(energy, 0, ne, s));
@@ -443,6 +450,15 @@ bool tv_proj_supported(int64_t nf, int64_t W, int K) {
 
 size_t tv_workspace_bytes(int64_t nf, int64_t H, int64_t W, int K) {
     return tv::ws_layout(nf, H, W, K, nullptr, nullptr);
+}
+
+// The stop-test sums and ticket of a TV workspace, as 8-byte words to clear
+// (see flags & 4 of tv_launch_core).
+double *tv_clear_region(int64_t nf, int64_t H, int64_t W, int K, void *workspace, int *words) {
+    tv::Workspace w;
+    tv::ws_layout(nf, H, W, K, &w, static_cast<char *>(workspace));
+    *words = (int)(nf * K * 2) + 1;
+    return w.energy;
 }
 
 }  // namespace sci

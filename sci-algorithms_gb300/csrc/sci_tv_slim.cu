@@ -32,8 +32,8 @@ void launch_slim_fix(const Pass &P, bool proj, cudaStream_t s) {
     using namespace slim;
     if (P.cpl == 2) return launch_slim2_fix(P, proj, s);
     constexpr int D = MinB<4>::def;
-    if (proj) k_tv_slim_fix<4, D, 1><<<pass_blocks(P), WPB * 32, 0, s>>>(P);
-    else k_tv_slim_fix<4, D, 0><<<pass_blocks(P), WPB * 32, 0, s>>>(P);
+    if (proj) (void)launch_dep(k_tv_slim_fix<4, D, 1>, dim3(pass_blocks(P)), dim3(WPB * 32), 0, s, P);
+    else (void)launch_dep(k_tv_slim_fix<4, D, 0>, dim3(pass_blocks(P)), dim3(WPB * 32), 0, s, P);
 }
 
 int slim_resident_blocks(int cpl, int SG, int minb, bool proj) {

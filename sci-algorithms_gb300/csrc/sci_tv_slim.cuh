@@ -425,6 +425,7 @@ __device__ __forceinline__ Rings lane_rings(unsigned char *smem, int lane, int w
 template <int S, int CPL, int MINB, int PROJ, int FORM = 1>
 __global__ void __launch_bounds__(WPB * 32, MINB) k_tv_slim(Pass P) {
     __shared__ __align__(16) unsigned char smem[Smem<CPL, PROJ>::bytes];
+    grid_dep_wait();
     int frame, chunk, band;
     if (!decode_item(P, frame, chunk, band)) return;
     const int lane = threadIdx.x & 31;
@@ -438,6 +439,7 @@ __global__ void __launch_bounds__(WPB * 32, MINB) k_tv_slim(Pass P) {
 template <int CPL, int MINB, int PROJ>
 __global__ void __launch_bounds__(WPB * 32, MINB) k_tv_slim_fix(Pass P) {
     __shared__ __align__(16) unsigned char smem[Smem<CPL, PROJ>::bytes];
+    grid_dep_wait();
     int frame, chunk, band;
     if (!decode_item(P, frame, chunk, band)) return;
     const int j = P.stopj[frame];

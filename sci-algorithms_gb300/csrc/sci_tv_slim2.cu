@@ -25,8 +25,8 @@ void launch_slim2(const Pass &P, int SG, int minb, bool proj, cudaStream_t s) {
 void launch_slim2_fix(const Pass &P, bool proj, cudaStream_t s) {
     using namespace slim;
     constexpr int D = MinB<2>::def;
-    if (proj) k_tv_slim_fix<2, D, 1><<<pass_blocks(P), WPB * 32, 0, s>>>(P);
-    else k_tv_slim_fix<2, D, 0><<<pass_blocks(P), WPB * 32, 0, s>>>(P);
+    if (proj) (void)launch_dep(k_tv_slim_fix<2, D, 1>, dim3(pass_blocks(P)), dim3(WPB * 32), 0, s, P);
+    else (void)launch_dep(k_tv_slim_fix<2, D, 0>, dim3(pass_blocks(P)), dim3(WPB * 32), 0, s, P);
 }
 
 int slim2_resident_blocks(int SG, int minb, bool proj) {

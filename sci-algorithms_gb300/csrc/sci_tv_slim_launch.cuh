@@ -31,15 +31,18 @@ template <int CPL, int MINB, int PROJ>
 void launch_main(const Pass &P, int SG, cudaStream_t s, int form = 1) {
     const unsigned g = pass_blocks(P);
     constexpr int D = MinB<CPL>::def;
+    const dim3 b(WPB * 32);
+    cudaError_t e;
     switch (SG) {
-        case 1: k_tv_slim<1, CPL, D, PROJ><<<g, WPB * 32, 0, s>>>(P); break;
-        case 2: k_tv_slim<2, CPL, D, PROJ><<<g, WPB * 32, 0, s>>>(P); break;
-        case 3: k_tv_slim<3, CPL, D, PROJ><<<g, WPB * 32, 0, s>>>(P); break;
+        case 1: e = launch_dep(k_tv_slim<1, CPL, D, PROJ>, dim3(g), b, 0, s, P); break;
+        case 2: e = launch_dep(k_tv_slim<2, CPL, D, PROJ>, dim3(g), b, 0, s, P); break;
+        case 3: e = launch_dep(k_tv_slim<3, CPL, D, PROJ>, dim3(g), b, 0, s, P); break;
         default:
-            if (form) k_tv_slim<4, CPL, MINB, PROJ, 1><<<g, WPB * 32, 0, s>>>(P);
-            else k_tv_slim<4, CPL, MINB, PROJ, 0><<<g, WPB * 32, 0, s>>>(P);
+            if (form) e = launch_dep(k_tv_slim<4, CPL, MINB, PROJ, 1>, dim3(g), b, 0, s, P);
+            else e = launch_dep(k_tv_slim<4, CPL, MINB, PROJ, 0>, dim3(g), b, 0, s, P);
             break;
     }
+    (void)e;  // reported by the caller's cudaGetLastError
 }
 
 // Resident blocks per SM of a kernel, queried once; minb if the query fails.
