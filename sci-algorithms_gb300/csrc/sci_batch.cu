@@ -38,16 +38,23 @@ size_t tv_workspace_bytes(int64_t nf, int64_t H, int64_t W, int K);
 namespace batch {
 
 // x0 = At(y / Phi_sum) for every item (the start point of the GAP loop).
-__global__ void __launch_bounds__(PROJ_T) k_batch_x0(const Table *__restrict__ T) {
+// Start of a solve, one pass over every item's pixels: X0, x = At(y /
+// Phi_sum); Y1, the accelerated GAP's y1 = 0 (one launch instead of a
+// memset node per item).
+template <bool X0, bool Y1>
+__global__ void __launch_bounds__(PROJ_T) k_batch_init(const Table *__restrict__ T) {
     const int g = blockIdx.x;
     if (g >= T->proj_prefix[T->n]) return;
     const int i = find_item(T->proj_prefix, T->n, g);
     const Item &I = T->it[i];
     const int64_t p = (int64_t)(g - T->proj_prefix[i]) * PROJ_T + threadIdx.x;
     if (p >= I.hw) return;
-    const uint32_t w = I.bits[p];
-    const float s0 = I.y[p] / I.phisum[p];
-    for (int b = 0; b < I.B; ++b) I.x[b * I.hw + p] = ((w >> b) & 1u) ? s0 : 0.f * s0;
+    if (Y1) I.y1[p] = 0.f;
+    if (X0) {
+        const uint32_t w = I.bits[p];
+        const float s0 = I.y[p] / I.phisum[p];
+        for (int b = 0; b < I.B; ++b) I.x[b * I.hw + p] = ((w >> b) & 1u) ? s0 : 0.f * s0;
+    }
 }
 
 // GAP projection (acc: y1 += y - A x, x_p = x + lam At((y1 - A x)/Phi_sum)).
@@ -361,12 +368,12 @@ bool queue_enabled() {
 int enqueue(const Table &T, Table *dT, const Layout &L, char *ws, int n, int iters, int K,
             int accelerate, int init_x0, int per_launch, cudaStream_t s) {
     const int pb = T.proj_prefix[n], tb = (T.tv_prefix[n] + tv::WPB - 1) / tv::WPB;
-    if (init_x0) {
-        k_batch_x0<<<pb, PROJ_T, 0, s>>>(dT);
-        SCI_LAUNCHED("k_batch_x0");
+    if (init_x0 || accelerate) {
+        if (init_x0 && accelerate) k_batch_init<true, true><<<pb, PROJ_T, 0, s>>>(dT);
+        else if (init_x0) k_batch_init<true, false><<<pb, PROJ_T, 0, s>>>(dT);
+        else k_batch_init<false, true><<<pb, PROJ_T, 0, s>>>(dT);
+        SCI_LAUNCHED("k_batch_init");
     }
-    for (int i = 0; i < n; ++i)
-        if (accelerate) SCI_CUDA(cudaMemsetAsync(T.it[i].y1, 0, 4 * T.it[i].hw, s));
     if (queue_enabled()) {
         // the items' stop decisions and tickets: a ticket counts the TV
         // tasks of an iteration and is reset by the last one, so it starts
