@@ -394,45 +394,35 @@ __global__ void __launch_bounds__(256) k_gap_resid_vec(
 // The ADMM iteration (pnp_sci_algo.py:808-836) with the projection applied
 // by the TV kernel while it loads theta: the TV input of iteration k is
 // v_k = theta_k + lambda_k (r_k phi_b) (= x - b), its output theta_{k+1},
-// and b_{k+1} = b_k - (x_k - theta_{k+1}) = theta_{k+1} - v_k.  This pass
-// re-forms v_k from theta_k and r_k exactly as the TV kernel rounded it,
-// then t = theta_{k+1} + b_{k+1} (t = theta_0 + 0 at the first iteration),
+// and b_{k+1} = b_k - (x_k - theta_{k+1}) = theta_{k+1} - v_k; the TV pass
+// also stores t = theta_{k+1} + b_{k+1} (PROJ 3 of the lean pass).  This
+// pass reads t (t = theta_0 + 0 at the first iteration), forms
 // yb = sum_b phi_b t_b and r_{k+1} = (y - yb) / (phisum + gamma).  With xo
 // it also writes x = t + lambda (r phi_b) of every frame (a second sweep).
-template <bool FIRST>
-__device__ __forceinline__ float4 admm_t(const float *__restrict__ th,
-                                         const float *__restrict__ tho, float4 rp, float4 m,
-                                         float lam_old, int64_t o) {
-    const float4 a = ldg4(th + o);
-    if (FIRST) return make_float4(a.x + 0.f, a.y + 0.f, a.z + 0.f, a.w + 0.f);
-    const float4 q = ldg4(tho + o);
-    const float4 v = make_float4(fmaf(lam_old, rp.x * m.x, q.x), fmaf(lam_old, rp.y * m.y, q.y),
-                                 fmaf(lam_old, rp.z * m.z, q.z), fmaf(lam_old, rp.w * m.w, q.w));
-    const float4 bb = make_float4(a.x - v.x, a.y - v.y, a.z - v.z, a.w - v.w);
-    return make_float4(a.x + bb.x, a.y + bb.y, a.z + bb.z, a.w + bb.w);
-}
-
 template <bool FIRST, bool WANT_X>
 __global__ void __launch_bounds__(256) k_admm_resid_vec(
-    const float *__restrict__ th, const float *__restrict__ tho, const float *__restrict__ rold,
-    float lam_old, Mask<1> M, const float *__restrict__ y, const float *__restrict__ phisum,
-    float *__restrict__ rnew, float *__restrict__ xo, float lam, float gamma, int B, int64_t hw,
-    double *__restrict__ rn, double *__restrict__ zero, int nzero) {
+    const float *__restrict__ tp, Mask<1> M, const float *__restrict__ y,
+    const float *__restrict__ phisum, float *__restrict__ rnew, float *__restrict__ xo, float lam,
+    float gamma, int B, int64_t hw, double *__restrict__ rn, double *__restrict__ zero,
+    int nzero) {
     grid_dep_wait();
     if (blockIdx.x == 0)  // the next TV pass's stop-test sums
         for (int i = threadIdx.x; i < nzero; i += blockDim.x) zero[i] = 0.0;
+    auto tload = [&](int64_t o) {
+        const float4 a = ldg4(tp + o);
+        return FIRST ? make_float4(a.x + 0.f, a.y + 0.f, a.z + 0.f, a.w + 0.f) : a;
+    };
     const int64_t n4 = hw >> 2;
     double racc = 0.0;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n4;
          q += (int64_t)gridDim.x * blockDim.x) {
         const int64_t p = q << 2;
         const uint4 w = M.word4(p);
-        const float4 rp = FIRST ? make_float4(0.f, 0.f, 0.f, 0.f) : ldg4(rold + p);
         float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll 4
         for (int b = 0; b < B; ++b) {
             const float4 m = M.at4(b, p, w);
-            const float4 t = admm_t<FIRST>(th, tho, rp, m, lam_old, b * hw + p);
+            const float4 t = tload(b * hw + p);
             s.x = fmaf(t.x, m.x, s.x);
             s.y = fmaf(t.y, m.y, s.y);
             s.z = fmaf(t.z, m.z, s.z);
@@ -449,7 +439,7 @@ __global__ void __launch_bounds__(256) k_admm_resid_vec(
 #pragma unroll 4
             for (int b = 0; b < B; ++b) {
                 const float4 m = M.at4(b, p, w);
-                const float4 t = admm_t<FIRST>(th, tho, rp, m, lam_old, b * hw + p);
+                const float4 t = tload(b * hw + p);
                 st4(xo + b * hw + p,
                     make_float4(fmaf(lam, r.x * m.x, t.x), fmaf(lam, r.y * m.y, t.y),
                                 fmaf(lam, r.z * m.z, t.z), fmaf(lam, r.w * m.w, t.w)));
@@ -652,27 +642,24 @@ int gap_residual_rn(const float *x, const float *phi, const uint32_t *mask_bits,
 }
 
 // The fused ADMM iteration's residual pass (k_admm_resid_vec): packed
-// mask, H*W % 4 == 0, 16-byte aligned planes.  first: theta_old and r_old
-// are not read (b_0 = 0).
-int admm_residual_rn(const float *theta, const float *theta_old, const float *r_old,
-                     float lambda_old, const uint32_t *mask_bits, const float *y,
+// mask, H*W % 4 == 0, 16-byte aligned planes.  t: theta + b of every frame
+// (theta_0 at the first iteration, `first`).
+int admm_residual_rn(const float *t, const uint32_t *mask_bits, const float *y,
                      const float *phisum, float *r_new, float *x_out, float lambda, float gamma,
                      int first, int64_t B, int64_t H, int64_t W, void *stream, double *rn,
                      double *zero, int nzero) {
     if (int e = check_dims(B, H, W)) return e;
-    SCI_CHECK_ARG(theta && y && phisum && r_new && mask_bits && (first || (theta_old && r_old)),
-                  "admm residual: null pointer");
+    SCI_CHECK_ARG(t && y && phisum && r_new && mask_bits, "admm residual: null pointer");
     SCI_CHECK_ARG(B <= 32, "admm residual: packed mask needs B <= 32");
     const int64_t hw = H * W;
-    SCI_CHECK_ARG(vec_ok(hw, {theta, theta_old, r_old, mask_bits, y, phisum, r_new, x_out}),
+    SCI_CHECK_ARG(vec_ok(hw, {t, mask_bits, y, phisum, r_new, x_out}),
                   "admm residual: needs H*W %% 4 == 0 and 16-byte aligned buffers");
     cudaStream_t s = as_stream(stream);
     const dim3 g = grid_for(hw / 4, 256);
     Mask<1> M{mask_bits, hw};
-#define SCI_ADMM_RESID(F, X)                                                                    \
-    SCI_CUDA(launch_dep(k_admm_resid_vec<F, X>, g, dim3(256), 0, s, theta, theta_old, r_old,    \
-                        lambda_old, M, y, phisum, r_new, x_out, lambda, gamma, (int)B, hw, rn, \
-                        zero, nzero))
+#define SCI_ADMM_RESID(F, X)                                                                  \
+    SCI_CUDA(launch_dep(k_admm_resid_vec<F, X>, g, dim3(256), 0, s, t, M, y, phisum, r_new,   \
+                        x_out, lambda, gamma, (int)B, hw, rn, zero, nzero))
     if (first) {
         if (x_out) SCI_ADMM_RESID(true, true);
         else SCI_ADMM_RESID(true, false);

@@ -37,11 +37,14 @@ int gap_residual_rn(const float *x, const float *phi, const uint32_t *mask_bits,
                     int accelerate, int64_t B, int64_t H, int64_t W, void *stream, double *rn,
                     double *zero, int nzero);
 double *tv_clear_region(int64_t nf, int64_t H, int64_t W, int K, void *workspace, int *words);
-int admm_residual_rn(const float *theta, const float *theta_old, const float *r_old,
-                     float lambda_old, const uint32_t *mask_bits, const float *y,
+int admm_residual_rn(const float *t, const uint32_t *mask_bits, const float *y,
                      const float *phisum, float *r_new, float *x_out, float lambda, float gamma,
                      int first, int64_t B, int64_t H, int64_t W, void *stream, double *rn,
                      double *zero, int nzero);
+int tv_launch_tout(const float *f, float *u, int64_t nf, int64_t H, int64_t W, int64_t fs,
+                   float weight, float eps, int K, int *steps, void *workspace, size_t ws_bytes,
+                   cudaStream_t s, int flags, const uint32_t *proj_bits, const float *proj_c,
+                   float proj_lam, float *tout);
 int proj_admm_rn(const float *theta, const float *b, const float *phi,
                  const uint32_t *mask_bits, const float *y, const float *phisum, float *v,
                  float *x_out, float lambda, float gamma, int64_t B, int64_t H, int64_t W,
@@ -225,27 +228,25 @@ int enqueue(const Args &a, cudaStream_t s) {
     if (!o.tvm && a.bits && aligned && hw % 4 == 0 && tv_proj_supported(B, W, K) &&
         !(af && af[0] == '0')) {
         // Fused iteration: a read-only pass forms the residual map r_k from
-        // theta_k and the previous iteration's TV input (re-formed from
-        // theta_{k-1} and r_{k-1}, see k_admm_resid_vec); the TV kernel
-        // applies theta_k + lambda_k (r_k phi_b) = x - b while it loads
-        // theta_k.  theta ping-pongs between w.theta and w.b0 (theta_{k+1}
-        // overwrites theta_{k-1}), the residual maps between w.v and w.b1.
+        // t_k = theta_k + b_k; the TV kernel applies theta_k + lambda_k
+        // (r_k phi_b) = x - b while it loads theta_k and stores theta_{k+1}
+        // and t_{k+1} = theta_{k+1} + (theta_{k+1} - v_k).  theta ping-pongs
+        // between w.theta and w.b0; t lives in w.v, the map in w.b1.
         float *T[2] = {w.theta, w.b0};
-        float *R[2] = {w.v, w.b1};
+        float *tb = w.v, *R = w.b1;
         int nzero = 0;
         double *zero = tv_clear_region(B, H, W, K, w.tv, &nzero);
         for (int it = 0; it < o.iters; ++it) {
             const bool want_x = (it == o.iters - 1) || (o.orig && o.sqerr);
             const float gamma = o.gammas ? o.gammas[it] : o.gamma;
-            float *cur = T[it & 1], *old = T[(it + 1) & 1];
-            int e = admm_residual_rn(cur, it ? old : nullptr, it ? R[(it + 1) & 1] : nullptr,
-                                     it ? o.lambdas[it - 1] : 0.f, a.bits, a.y, a.phisum,
-                                     R[it & 1], want_x ? a.x_out : nullptr, o.lambdas[it], gamma,
-                                     it == 0, B, H, W, s, rn(it), zero, nzero);
+            float *cur = T[it & 1], *nxt = T[(it + 1) & 1];
+            int e = admm_residual_rn(it ? tb : cur, a.bits, a.y, a.phisum, R,
+                                     want_x ? a.x_out : nullptr, o.lambdas[it], gamma, it == 0, B,
+                                     H, W, s, rn(it), zero, nzero);
             if (e) return e;
-            e = tv_launch_impl(cur, old, nullptr, B, H, W, hw, o.weights[it], o.eps, K,
-                               o.tv_steps ? o.tv_steps + (int64_t)it * B : nullptr, nullptr, w.tv,
-                               w.tv_bytes, s, 0, 4, a.bits, R[it & 1], o.lambdas[it]);
+            e = tv_launch_tout(cur, nxt, B, H, W, hw, o.weights[it], o.eps, K,
+                               o.tv_steps ? o.tv_steps + (int64_t)it * B : nullptr, w.tv,
+                               w.tv_bytes, s, 4, a.bits, R, o.lambdas[it], tb);
             if (e) return e;
             if (o.orig && o.sqerr) {
                 e = sci_sqerr_accum(o.orig, a.x_out, n, o.sqerr + it, s);

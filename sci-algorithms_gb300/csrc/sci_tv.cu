@@ -209,6 +209,9 @@ struct RuleArgs {
     int rule = tv::RULE_SKIMAGE;
     float tau = 0.f, tw = 0.f, c1 = 0.f, c2 = 0.f;
     float *tape_p = nullptr, *tape_u = nullptr;  // single-pass tape (sci_tv_tape.cu)
+    // with the on-load projection: also store t = u + (u - f) (the lean
+    // pass only, PROJ 3; the fused ADMM iteration's next t = theta + b)
+    float *tout = nullptr;
 };
 
 static int tv_launch_core(const float *f, float *u, float *resid, int64_t nf, int64_t H,
@@ -281,7 +284,11 @@ static int tv_launch_core(const float *f, float *u, float *resid, int64_t nf, in
     // flags bits 8-11: columns per lane forced by the caller (2 or 4)
     const int fcpl = (flags >> 8) & 0xf;
     const int cpl_pick = (fcpl == 2 || fcpl == 4) ? fcpl : choose_cpl(W);
-    const bool slim = slim_ok && aligned_for(cpl_pick);
+    const bool slim = slim_ok && aligned_for(cpl_pick) &&
+                      (!ra.tout || (reinterpret_cast<uintptr_t>(ra.tout) % (4 * cpl_pick)) == 0);
+    SCI_CHECK_ARG(!ra.tout || (proj && slim), "tv: the t output needs the lean pass with the "
+                                              "on-load projection (aligned frames)");
+    const int pmode = proj ? (ra.tout ? 3 : 1) : 0;  // the lean pass's PROJ
     const int cpl = slim ? cpl_pick : ((proj || ra.rule != RULE_SKIMAGE) ? 4 : cpl_pick);
     const bool vec = (W % cpl == 0) && (fs % cpl == 0) &&
                      ((reinterpret_cast<uintptr_t>(f) | reinterpret_cast<uintptr_t>(u) |
@@ -326,6 +333,7 @@ static int tv_launch_core(const float *f, float *u, float *resid, int64_t nf, in
         P.ht = SG + (PIN ? 1 : 0);
         P.lag = lag;
         P.proj = proj ? 1 : 0;
+        P.tout = ra.tout;
         P.bits = proj_bits;
         P.cmap = proj_c;
         P.lam = proj_lam;
@@ -334,7 +342,7 @@ static int tv_launch_core(const float *f, float *u, float *resid, int64_t nf, in
         if (force_R > 0) P.R = force_R;
         else if (slim)
             P.R = choose_R_slim(nf, P.nbands, (int)H, SG,
-                                kSMs * slim_resident_blocks(cpl, SG, minb, proj));
+                                kSMs * slim_resident_blocks(cpl, SG, minb, pmode));
         else P.R = choose_R(nf, P.nbands, (int)H);
         P.nchunks = (int)((H + P.R - 1) / P.R);
         P.S = SG;
@@ -350,7 +358,7 @@ static int tv_launch_core(const float *f, float *u, float *resid, int64_t nf, in
         const int per_frame_blocks = (P.nbands * P.nchunks + WPB - 1) / WPB;
         P.gpf = std::max(1, std::min(per_frame_blocks, 16));
         if (slim) {
-            launch_slim(P, SG, minb, proj, s);
+            launch_slim(P, SG, minb, pmode, s);
         } else if (tape) {
             launch_tape(P, SG, s);
         } else if (ra.rule == RULE_CHAM_ITV) {
@@ -370,7 +378,7 @@ static int tv_launch_core(const float *f, float *u, float *resid, int64_t nf, in
         }
         SCI_LAUNCHED("k_tv_main");
         if (stop_test) {
-            if (slim) launch_slim_fix(P, proj, s);
+            if (slim) launch_slim_fix(P, pmode, s);
             else if (proj) launch_fixup_proj(P, s);
             else launch_fixup(P, PIN, s);
             SCI_LAUNCHED("k_tv_fixup");
@@ -388,6 +396,18 @@ int tv_launch_impl(const float *f, float *u, float *resid, int64_t nf, int64_t H
     return tv_launch_core(f, u, resid, nf, H, W, fs, weight, eps, K, steps, energy_out,
                           workspace, ws_bytes, s, force_R, flags, proj_bits, proj_c, proj_lam,
                           RuleArgs{});
+}
+
+// tv_launch_impl with the on-load projection that also stores t = u + (u -
+// f) into tout (the lean pass; see RuleArgs::tout).
+int tv_launch_tout(const float *f, float *u, int64_t nf, int64_t H, int64_t W, int64_t fs,
+                   float weight, float eps, int K, int *steps, void *workspace, size_t ws_bytes,
+                   cudaStream_t s, int flags, const uint32_t *proj_bits, const float *proj_c,
+                   float proj_lam, float *tout) {
+    RuleArgs ra;
+    ra.tout = tout;
+    return tv_launch_core(f, u, nullptr, nf, H, W, fs, weight, eps, K, steps, nullptr,
+                          workspace, ws_bytes, s, 0, flags, proj_bits, proj_c, proj_lam, ra);
 }
 
 // A MATLAB-rule run of `updates` dual updates (rule, tau, tw, c1, c2 as in

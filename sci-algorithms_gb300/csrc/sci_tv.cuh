@@ -101,6 +101,9 @@ struct Pass {
     // (zero when it starts; the last block resets it).
     int *stopj;
     unsigned *ticket;
+    // Lean pass with the projection on load and the t output (PROJ 3):
+    // t = u + (u - f) of every frame, same layout as u (nullable otherwise).
+    float *tout;
 };
 
 // Dual update rules of the pipeline (the dual p is held as p / lambda for
@@ -970,9 +973,9 @@ void launch_fixup(const Pass &P, bool pin, cudaStream_t s);
 // Register-lean single-pass kernels (sci_tv_slim.cu, P.cpl = 2 or 4); minb:
 // the resident blocks per SM their registers are sized for (0: default);
 // proj: the GAP projection applied on load.
-void launch_slim(const Pass &P, int SG, int minb, bool proj, cudaStream_t s);
-void launch_slim_fix(const Pass &P, bool proj, cudaStream_t s);
-int slim_resident_blocks(int cpl, int SG, int minb, bool proj);  // of the main kernel
+void launch_slim(const Pass &P, int SG, int minb, int proj, cudaStream_t s);
+void launch_slim_fix(const Pass &P, int proj, cudaStream_t s);
+int slim_resident_blocks(int cpl, int SG, int minb, int proj);  // of the main kernel
 
 inline unsigned pass_blocks(const Pass &P) {
     const int64_t items = (int64_t)P.nbands * P.nchunks * P.nf;

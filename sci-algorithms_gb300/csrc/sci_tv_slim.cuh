@@ -23,7 +23,10 @@
 // stored stack holds x, and f = x + lam (c phi_b) with c the per-pixel
 // residual map and phi_b bit `frame` of the packed mask word; the map and
 // mask rows come through two more rings, and stage 0 writes f back into the
-// input ring for the later stages.
+// input ring for the later stages.  PROJ 3 is PROJ 1 that also stores
+// t = u + (u - f) beside u (P.tout): in the ADMM iteration f is the TV
+// input v = x - b and u the new theta, so t = theta + b of the next
+// projection.
 //
 // Rounding is identical to the generic pipeline (same operations in the same
 // order), so the two produce bit-identical frames.
@@ -194,7 +197,7 @@ __device__ __forceinline__ Row<CPL> stage0(const Pass &P, const Rings &G, int r,
 // tau product, u = f - d / 4 takes it once per pixel instead, and the energy
 // sums are accumulated 16-fold (their w |grad u| term with 16 w).  FORM 0
 // holds p itself.
-template <int S, int K, int CPL, bool ENERGY, int MODE, bool GEN, int FORM = 1>
+template <int S, int K, int CPL, bool ENERGY, int MODE, bool GEN, int FORM = 1, bool TOUT = false>
 __device__ __forceinline__ void stage(const Pass &P, const SS<S, CPL> &in, SS<S, CPL> &out,
                                       Row<CPL> &ucur, int r, int rs, int r0, int r1,
                                       const SLane<CPL> &L, float *ob, const Rings &G,
@@ -268,20 +271,28 @@ __device__ __forceinline__ void stage(const Pass &P, const SS<S, CPL> &in, SS<S,
             }
         }
     }
-    if (K == S && (!GEN || (i >= r0 && i < r1)) && L.lane_own)
+    if (K == S && (!GEN || (i >= r0 && i < r1)) && L.lane_own) {
         vstore<CPL>(ob + (int64_t)i * W + L.col, uk);
+        if (TOUT) {  // t = u + (u - f), the ADMM iterate theta + b of the next residual
+            Row<CPL> t;
+#pragma unroll
+            for (int j = 0; j < NQ; ++j) t.q[j] = add2(uk.q[j], sub2(uk.q[j], fi.q[j]));
+            vstore<CPL>(P.tout + (ob - P.u) + (int64_t)i * W + L.col, t);
+        }
+    }
     ucur = uk;
 }
 
 // Stages K..S of one step, in order.
-template <int S, int K, int CPL, bool ENERGY, int MODE, bool GEN, int FORM>
+template <int S, int K, int CPL, bool ENERGY, int MODE, bool GEN, int FORM, bool TOUT = false>
 __device__ __forceinline__ void stages(const Pass &P, const SS<S, CPL> &in, SS<S, CPL> &out,
                                        Row<CPL> &ucur, int r, int rs, int r0, int r1,
                                        const SLane<CPL> &L, float *ob, const Rings &G,
                                        f2 (&ek)[S]) {
     if constexpr (K <= S) {
-        stage<S, K, CPL, ENERGY, MODE, GEN, FORM>(P, in, out, ucur, r, rs, r0, r1, L, ob, G, ek);
-        stages<S, K + 1, CPL, ENERGY, MODE, GEN, FORM>(P, in, out, ucur, r, rs, r0, r1, L, ob, G,
+        stage<S, K, CPL, ENERGY, MODE, GEN, FORM, TOUT>(P, in, out, ucur, r, rs, r0, r1, L, ob, G,
+                                                        ek);
+        stages<S, K + 1, CPL, ENERGY, MODE, GEN, FORM, TOUT>(P, in, out, ucur, r, rs, r0, r1, L, ob, G,
                                                        ek);
     }
 }
@@ -298,7 +309,8 @@ __device__ __forceinline__ void sstep(const Pass &P, const SS<S, CPL> &in, SS<S,
     cp_wait<PF>();
     if (COH && CPL == 2) __syncwarp();  // the pair's copy was the even lane's
     Row<CPL> ucur = (!GEN || r < P.H) ? stage0<CPL, PROJ>(P, G, r, frame) : zrow<CPL>();
-    stages<S, 1, CPL, ENERGY, MODE, GEN, FORM>(P, in, out, ucur, r, rs, r0, r1, L, ob, G, ek);
+    stages<S, 1, CPL, ENERGY, MODE, GEN, FORM, PROJ == 3>(P, in, out, ucur, r, rs, r0, r1, L, ob, G,
+                                                        ek);
 }
 
 // One work item: frame, row chunk, column band.  Requires rows aligned for

@@ -4,8 +4,9 @@
 namespace sci {
 namespace tv {
 
-void launch_slim2(const Pass &P, int SG, int minb, bool proj, cudaStream_t s) {
+void launch_slim2(const Pass &P, int SG, int minb, int proj, cudaStream_t s) {
     using namespace slim;
+    if (proj == 3) return launch_main<2, 6, 3>(P, SG, s);
     switch (minb) {
         case 5:
             if (proj) launch_main<2, 5, 1>(P, SG, s);
@@ -22,24 +23,26 @@ void launch_slim2(const Pass &P, int SG, int minb, bool proj, cudaStream_t s) {
     }
 }
 
-void launch_slim2_fix(const Pass &P, bool proj, cudaStream_t s) {
+void launch_slim2_fix(const Pass &P, int proj, cudaStream_t s) {
     using namespace slim;
     constexpr int D = MinB<2>::def;
-    if (proj) (void)launch_dep(k_tv_slim_fix<2, D, 1>, dim3(pass_blocks(P)), dim3(WPB * 32), 0, s, P);
+    if (proj == 3) (void)launch_dep(k_tv_slim_fix<2, D, 3>, dim3(pass_blocks(P)), dim3(WPB * 32), 0, s, P);
+    else if (proj) (void)launch_dep(k_tv_slim_fix<2, D, 1>, dim3(pass_blocks(P)), dim3(WPB * 32), 0, s, P);
     else (void)launch_dep(k_tv_slim_fix<2, D, 0>, dim3(pass_blocks(P)), dim3(WPB * 32), 0, s, P);
 }
 
-int slim2_resident_blocks(int SG, int minb, bool proj) {
+int slim2_resident_blocks(int SG, int minb, int proj) {
     using namespace slim;
     static std::mutex mu;
-    static int cache[3][2][5] = {};
+    static int cache[3][4][5] = {};
     SG = SG < 1 ? 1 : (SG > 4 ? 4 : SG);
-    const int mi = minb == 5 ? 0 : (minb == 7 ? 2 : 1);
+    const int mi = proj == 3 ? 1 : (minb == 5 ? 0 : (minb == 7 ? 2 : 1));
     std::lock_guard<std::mutex> lock(mu);
-    int &v = cache[mi][proj ? 1 : 0][SG];
+    int &v = cache[mi][proj & 3][SG];
     if (v == 0) {
         const void *k;
-        if (mi == 0) k = proj ? main_kernel<2, 5, 1>(SG) : main_kernel<2, 5, 0>(SG);
+        if (proj == 3) k = main_kernel<2, 6, 3>(SG);
+        else if (mi == 0) k = proj ? main_kernel<2, 5, 1>(SG) : main_kernel<2, 5, 0>(SG);
         else if (mi == 2) k = proj ? main_kernel<2, 7, 1>(SG) : main_kernel<2, 7, 0>(SG);
         else k = proj ? main_kernel<2, 6, 1>(SG) : main_kernel<2, 6, 0>(SG);
         v = resident(k, mi == 0 ? 5 : (mi == 2 ? 7 : 6));
