@@ -200,7 +200,7 @@ size_t r256(size_t b) { return (b + 255) & ~size_t(255); }
 
 struct Layout {
     size_t table, xp, y1, energy, stop, queue, tvscratch, total;
-    std::vector<size_t> item_xp, item_y1, item_e, item_e1, item_stop;
+    std::vector<size_t> item_xp, item_y1, item_c, item_e, item_e1, item_stop;
 };
 
 Layout layout(const sci_batch_item *items, int n, int K) {
@@ -213,6 +213,8 @@ Layout layout(const sci_batch_item *items, int n, int K) {
         L.item_xp.push_back(off);
         off += r256(4 * (size_t)nn);
         L.item_y1.push_back(off);
+        off += r256(4 * (size_t)hw);
+        L.item_c.push_back(off);
         off += r256(4 * (size_t)hw);
     }
     // per item the energy sums of even and odd iterations (the per-phase
@@ -280,6 +282,7 @@ void build_table(const sci_batch_item *items, int n, int K, float eps, char *ws,
         I.x = s.x;
         I.xp = reinterpret_cast<float *>(ws + L.item_xp[i]);
         I.y1 = reinterpret_cast<float *>(ws + L.item_y1[i]);
+        I.c = reinterpret_cast<float *>(ws + L.item_c[i]);
         I.B = (int)s.B;
         I.hw = s.H * s.W;
         I.lam = s.lambda;
@@ -329,12 +332,32 @@ void build_table(const sci_batch_item *items, int n, int K, float eps, char *ws,
                                                   (par ? L.item_e1[i] : L.item_e[i]));
             Q.stopj = reinterpret_cast<int *>(ws + L.item_stop[i]);
             Q.ticket = reinterpret_cast<unsigned *>(ws + L.item_stop[i] + sizeof(int) * s.B);
+            // the fused iteration: the TV pass loads x_k and applies
+            // x_k + lam (c phi_b) (the projection's rounding), writing x_{k+1}
+            Q.f = par ? I.xp : I.x;
+            Q.u = par ? I.x : I.xp;
+            Q.proj = 1;
+            Q.bits = I.bits;
+            Q.cmap = I.c;
+            Q.lam = I.lam;
         }
         T.tv_prefix[i + 1] = T.tv_prefix[i] + P.nbands * P.nchunks * P.nf;
         // both parities have the same geometry
         T.tq_prefix[i + 1] =
             T.tq_prefix[i] + I.tvq[0].nbands * I.tvq[0].nchunks * I.tvq[0].nf;
     }
+}
+
+// After an odd number of work-queue iterations the last x is in xp: copy
+// it into every item's x.
+__global__ void __launch_bounds__(PROJ_T) k_batch_copy_x(const Table *__restrict__ T) {
+    const int g = blockIdx.x;
+    if (g >= T->proj_prefix[T->n]) return;
+    const int i = find_item(T->proj_prefix, T->n, g);
+    const Item &I = T->it[i];
+    const int64_t p = (int64_t)(g - T->proj_prefix[i]) * PROJ_T + threadIdx.x;
+    if (p >= I.hw) return;
+    for (int b = 0; b < I.B; ++b) I.x[b * I.hw + p] = I.xp[b * I.hw + p];
 }
 
 // bit 1 of the batch status: a bounded wait of a work-queue launch gave up
@@ -389,6 +412,10 @@ int enqueue(const Table &T, Table *dT, const Layout &L, char *ws, int n, int ite
                 return e;
             k_batch_fold<<<1, 32, 0, s>>>(dQ);
             SCI_LAUNCHED("k_batch_fold");
+        }
+        if (iters & 1) {  // the last TV pass wrote xp
+            k_batch_copy_x<<<pb, PROJ_T, 0, s>>>(dT);
+            SCI_LAUNCHED("k_batch_copy_x");
         }
         return SCI_OK;
     }

@@ -14,12 +14,14 @@ constexpr int QP_T = 128;    // pixels per projection task of the work queue (on
 
 struct Item {
     tv::Pass tv;      // per-phase launches: f = xp (projected stack), u = x
-    tv::Pass tvq[2];  // work queue: the same pass with the energies of even / odd
-                      // iterations and the item's stop decisions
+    tv::Pass tvq[2];  // work queue, iterations of even / odd k: the lean pass with
+                      // the projection applied on load from the residual map c,
+                      // the stack ping-ponging x -> xp (even k) and xp -> x (odd
+                      // k), the energies of even / odd k, the item's stop decisions
     const float *y;
     const uint32_t *bits;
     const float *phisum;
-    float *x, *xp, *y1;
+    float *x, *xp, *y1, *c;  // c: the work queue's residual map (H W)
     int B;
     int64_t hw;
     float lam;

@@ -1,9 +1,11 @@
 // Batched uneven GAP-TV as persistent launches over a device work queue.
 //
 // One launch runs iterations [k0, k1) of every item of a batch.  Its tasks
-// are numbered in a fixed order -- per iteration the projection tasks of all
-// items (128-pixel tiles), then their TV tasks (one (frame, row chunk,
-// column band) work item of the register-lean pipeline each), then their
+// are numbered in a fixed order -- per iteration the residual tasks of all
+// items (128-pixel tiles: the GAP residual map c, as the single-measurement
+// solver's fused iteration forms it), then their TV tasks (one (frame, row
+// chunk, column band) work item of the register-lean pipeline each, which
+// applies the projection x + lam (c phi_b) as it loads x), then their
 // stop-test tasks (the same work items) -- and the resident warps take the
 // next number from an atomic counter until the launch's tasks are used up.
 // A task waits only for tasks of its own item with smaller numbers:
@@ -44,16 +46,16 @@ __device__ __forceinline__ void finish(Queue *Q, int phase, int item, int lane) 
 
 __device__ __forceinline__ float bitf(uint32_t w, int b) { return ((w >> b) & 1u) ? 1.0f : 0.0f; }
 
-// GAP projection of one 128-pixel tile of item I (4 pixels per lane), the
-// arithmetic of k_proj_gap_tma: yb = sum_b phi_b x_b in frame order, ACC:
-// y1 += y - yb, r = (y1 - yb) / Phi_sum, else r = (y - yb) / Phi_sum;
-// xp_b = x_b + lam (r phi_b).  Tile 0 also clears the energy sums the
+// GAP residual map of one 128-pixel tile of item I (4 pixels per lane), the
+// arithmetic of k_gap_resid_vec: yb = sum_b phi_b x_b in frame order, ACC:
+// y1 += y - yb, c = (y1 - yb) / Phi_sum, else c = (y - yb) / Phi_sum, with
+// x the iteration's TV input P.f.  Tile 0 also clears the energy sums the
 // item's TV pass of this iteration adds to.
 // x and y1 were written earlier in this launch by warps on other SMs: they
 // are read at L2 (ld.global.cg), never through the non-coherent or L1
 // caches, which may still hold the lines of an earlier iteration.
 template <bool ACC>
-__device__ __forceinline__ void proj_task(const Item &I, const tv::Pass &P, int tile, int lane) {
+__device__ __forceinline__ void resid_task(const Item &I, const tv::Pass &P, int tile, int lane) {
     if (tile == 0) {
         const int ne = P.nf * P.K * 2;
         for (int e = lane; e < ne; e += 32) P.energy[e] = 0.0;
@@ -66,7 +68,7 @@ __device__ __forceinline__ void proj_task(const Item &I, const tv::Pass &P, int 
     float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll 8
     for (int b = 0; b < B; ++b) {
-        const float4 v = __ldcg(reinterpret_cast<const float4 *>(I.x + b * hw + p));
+        const float4 v = __ldcg(reinterpret_cast<const float4 *>(P.f + b * hw + p));
         s.x = fmaf(v.x, bitf(w.x, b), s.x);
         s.y = fmaf(v.y, bitf(w.y, b), s.y);
         s.z = fmaf(v.z, bitf(w.z, b), s.z);
@@ -87,17 +89,7 @@ __device__ __forceinline__ void proj_task(const Item &I, const tv::Pass &P, int 
         r = make_float4(__fdiv_rn(yv.x - s.x, ps.x), __fdiv_rn(yv.y - s.y, ps.y),
                         __fdiv_rn(yv.z - s.z, ps.z), __fdiv_rn(yv.w - s.w, ps.w));
     }
-    const float lam = I.lam;
-#pragma unroll 8
-    for (int b = 0; b < B; ++b) {
-        const float4 v = __ldcg(reinterpret_cast<const float4 *>(I.x + b * hw + p));
-        float4 o;
-        o.x = fmaf(lam, r.x * bitf(w.x, b), v.x);
-        o.y = fmaf(lam, r.y * bitf(w.y, b), v.y);
-        o.z = fmaf(lam, r.z * bitf(w.z, b), v.z);
-        o.w = fmaf(lam, r.w * bitf(w.w, b), v.w);
-        st4_cs(I.xp + b * hw + p, o);
-    }
+    st4(I.c + p, r);
 }
 
 // The TV pass with S dual updates of one work item, or (FIX) its re-run with
@@ -108,27 +100,27 @@ __device__ __forceinline__ void tv_task(const tv::Pass &P, int frame, int chunk,
                                         const tv::slim::Rings &G2) {
     using namespace tv::slim;
     if (!FIX) {
-        if (P.cpl == 2) srun_mode<S, 2, true, 0, 1, 1>(P, frame, chunk, band, lane, G2);
-        else srun_mode<S, 4, true, 0, 1, 1>(P, frame, chunk, band, lane, G4);
+        if (P.cpl == 2) srun_mode<S, 2, true, 1, 1, 1>(P, frame, chunk, band, lane, G2);
+        else srun_mode<S, 4, true, 1, 1, 1>(P, frame, chunk, band, lane, G4);
         return;
     }
     const int j = __ldcg(P.stopj + frame);  // decided by another warp of this launch
     if (j < 1 || j >= S) return;
     switch (j) {
         case 1:
-            if (P.cpl == 2) srun_mode<1, 2, false, 0, 1, 1>(P, frame, chunk, band, lane, G2);
-            else srun_mode<1, 4, false, 0, 1, 1>(P, frame, chunk, band, lane, G4);
+            if (P.cpl == 2) srun_mode<1, 2, false, 1, 1, 1>(P, frame, chunk, band, lane, G2);
+            else srun_mode<1, 4, false, 1, 1, 1>(P, frame, chunk, band, lane, G4);
             break;
         case 2:
             if constexpr (S > 2) {
-                if (P.cpl == 2) srun_mode<2, 2, false, 0, 1, 1>(P, frame, chunk, band, lane, G2);
-                else srun_mode<2, 4, false, 0, 1, 1>(P, frame, chunk, band, lane, G4);
+                if (P.cpl == 2) srun_mode<2, 2, false, 1, 1, 1>(P, frame, chunk, band, lane, G2);
+                else srun_mode<2, 4, false, 1, 1, 1>(P, frame, chunk, band, lane, G4);
             }
             break;
         default:
             if constexpr (S > 3) {
-                if (P.cpl == 2) srun_mode<3, 2, false, 0, 1, 1>(P, frame, chunk, band, lane, G2);
-                else srun_mode<3, 4, false, 0, 1, 1>(P, frame, chunk, band, lane, G4);
+                if (P.cpl == 2) srun_mode<3, 2, false, 1, 1, 1>(P, frame, chunk, band, lane, G2);
+                else srun_mode<3, 4, false, 1, 1, 1>(P, frame, chunk, band, lane, G4);
             }
             break;
     }
@@ -138,13 +130,13 @@ __device__ __forceinline__ void tv_task(const tv::Pass &P, int frame, int chunk,
 template <int S, bool ACC>
 __global__ void __launch_bounds__(tv::WPB * 32, QMINB)
     k_batch_queue(const Table *__restrict__ T, Queue *__restrict__ Q, int k0, int k1) {
-    __shared__ __align__(16) unsigned char smem[tv::slim::Smem<4, 0>::bytes];
+    __shared__ __align__(16) unsigned char smem[tv::slim::Smem<4, 1>::bytes];
     const int lane = threadIdx.x & 31;
-    // each warp's share holds its 4-column ring; a 2-column ring uses the
-    // first half of the same share
-    constexpr int share = tv::slim::Smem<4, 0>::bytes / tv::WPB;
-    const tv::slim::Rings G4 = tv::slim::lane_rings<4, 0>(smem, lane, share);
-    const tv::slim::Rings G2 = tv::slim::lane_rings<2, 0>(smem, lane, share);
+    // each warp's share holds its three 4-column rings (x, map, mask); the
+    // 2-column rings use the first half of the same share
+    constexpr int share = tv::slim::Smem<4, 1>::bytes / tv::WPB;
+    const tv::slim::Rings G4 = tv::slim::lane_rings<4, 1>(smem, lane, share);
+    const tv::slim::Rings G2 = tv::slim::lane_rings<2, 1>(smem, lane, share);
     const int n = T->n;
     const unsigned np = (unsigned)T->qp_prefix[n], nt = (unsigned)T->tq_prefix[n];
     const unsigned span = np + 2u * nt;
@@ -161,7 +153,7 @@ __global__ void __launch_bounds__(tv::WPB * 32, QMINB)
             const int i = find_item(T->qp_prefix, n, (int)rem);
             const unsigned ntv = (unsigned)(T->tq_prefix[i + 1] - T->tq_prefix[i]);
             if (j > 0 && !wait_count(Q, &Q->done[PH_FIX][i], j * ntv, lane)) return;
-            proj_task<ACC>(T->it[i], T->it[i].tvq[k & 1], (int)rem - T->qp_prefix[i], lane);
+            resid_task<ACC>(T->it[i], T->it[i].tvq[k & 1], (int)rem - T->qp_prefix[i], lane);
             finish(Q, PH_PROJ, i, lane);
             continue;
         }
