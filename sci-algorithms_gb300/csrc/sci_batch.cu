@@ -405,10 +405,12 @@ int enqueue(const Table &T, Table *dT, const Layout &L, char *ws, int n, int ite
         Queue *dQ = reinterpret_cast<Queue *>(ws + L.queue);
         const int m = per_launch > 0 ? per_launch : std::max(1, iters);
         const int blocks = queue_blocks();
+        bool narrow = false;
+        for (int i = 0; i < n; ++i) narrow = narrow || T.it[i].tvq[0].cpl == 2;
         for (int k0 = 0; k0 < iters; k0 += m) {
             SCI_CUDA(cudaMemsetAsync(dQ, 0, sizeof(Queue), s));
             if (int e = queue_launch(dT, dQ, k0, std::min(iters, k0 + m), accelerate != 0, K - 1,
-                                     blocks, s))
+                                     blocks, narrow, s))
                 return e;
             k_batch_fold<<<1, 32, 0, s>>>(dQ);
             SCI_LAUNCHED("k_batch_fold");

@@ -91,7 +91,7 @@ __device__ __forceinline__ int find_item(const int *prefix, int n, int g) {
 // launch over a device work queue.  Returns a negative status on a launch
 // error.
 int queue_launch(const Table *dT, Queue *dQ, int k0, int k1, bool accelerate, int S, int blocks,
-                 cudaStream_t s);
+                 bool narrow, cudaStream_t s);  // narrow: some item runs 2 columns per lane
 int queue_blocks();  // resident blocks of the persistent kernel (whole GPU)
 
 }  // namespace batch

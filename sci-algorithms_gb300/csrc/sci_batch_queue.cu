@@ -94,13 +94,15 @@ __device__ __forceinline__ void resid_task(const Item &I, const tv::Pass &P, int
 
 // The TV pass with S dual updates of one work item, or (FIX) its re-run with
 // the stop index j the pass decided.
-template <int S, bool FIX>
+// N2: some item runs 2 columns per lane (otherwise that code is not built,
+// which leaves the 4-column pipeline more registers).
+template <int S, bool FIX, bool N2>
 __device__ __forceinline__ void tv_task(const tv::Pass &P, int frame, int chunk, int band,
                                         int lane, const tv::slim::Rings &G4,
                                         const tv::slim::Rings &G2) {
     using namespace tv::slim;
     if (!FIX) {
-        if (P.cpl == 2) srun_mode<S, 2, true, 1, 1, 1>(P, frame, chunk, band, lane, G2);
+        if (N2 && P.cpl == 2) srun_mode<S, 2, true, 1, 1, 1>(P, frame, chunk, band, lane, G2);
         else srun_mode<S, 4, true, 1, 1, 1>(P, frame, chunk, band, lane, G4);
         return;
     }
@@ -108,18 +110,18 @@ __device__ __forceinline__ void tv_task(const tv::Pass &P, int frame, int chunk,
     if (j < 1 || j >= S) return;
     switch (j) {
         case 1:
-            if (P.cpl == 2) srun_mode<1, 2, false, 1, 1, 1>(P, frame, chunk, band, lane, G2);
+            if (N2 && P.cpl == 2) srun_mode<1, 2, false, 1, 1, 1>(P, frame, chunk, band, lane, G2);
             else srun_mode<1, 4, false, 1, 1, 1>(P, frame, chunk, band, lane, G4);
             break;
         case 2:
             if constexpr (S > 2) {
-                if (P.cpl == 2) srun_mode<2, 2, false, 1, 1, 1>(P, frame, chunk, band, lane, G2);
+                if (N2 && P.cpl == 2) srun_mode<2, 2, false, 1, 1, 1>(P, frame, chunk, band, lane, G2);
                 else srun_mode<2, 4, false, 1, 1, 1>(P, frame, chunk, band, lane, G4);
             }
             break;
         default:
             if constexpr (S > 3) {
-                if (P.cpl == 2) srun_mode<3, 2, false, 1, 1, 1>(P, frame, chunk, band, lane, G2);
+                if (N2 && P.cpl == 2) srun_mode<3, 2, false, 1, 1, 1>(P, frame, chunk, band, lane, G2);
                 else srun_mode<3, 4, false, 1, 1, 1>(P, frame, chunk, band, lane, G4);
             }
             break;
@@ -127,7 +129,7 @@ __device__ __forceinline__ void tv_task(const tv::Pass &P, int frame, int chunk,
 }
 
 // The persistent worker loop: S = tv_iter_max - 1 dual updates per TV pass.
-template <int S, bool ACC>
+template <int S, bool ACC, bool N2 = true>
 __global__ void __launch_bounds__(tv::WPB * 32, QMINB)
     k_batch_queue(const Table *__restrict__ T, Queue *__restrict__ Q, int k0, int k1) {
     __shared__ __align__(16) unsigned char smem[tv::slim::Smem<4, 1>::bytes];
@@ -168,10 +170,10 @@ __global__ void __launch_bounds__(tv::WPB * 32, QMINB)
         int frame, chunk, band;
         tv::decode_index(P, g - T->tq_prefix[i], frame, chunk, band);
         if (!fix) {
-            tv_task<S, false>(P, frame, chunk, band, lane, G4, G2);
+            tv_task<S, false, N2>(P, frame, chunk, band, lane, G4, G2);
             tv::decide_stops(P, lane);
         } else {
-            tv_task<S, true>(P, frame, chunk, band, lane, G4, G2);
+            tv_task<S, true, N2>(P, frame, chunk, band, lane, G4, G2);
         }
         finish(Q, fix ? PH_FIX : PH_TV, i, lane);
     }
@@ -200,7 +202,7 @@ int queue_blocks() {
 }
 
 int queue_launch(const Table *dT, Queue *dQ, int k0, int k1, bool accelerate, int S, int blocks,
-                 cudaStream_t s) {
+                 bool narrow, cudaStream_t s) {
 #define SCI_QUEUE_CASE(SV)                                                                 \
     case SV:                                                                               \
         if (accelerate) k_batch_queue<SV, true><<<blocks, tv::WPB * 32, 0, s>>>(dT, dQ, k0, k1); \
@@ -210,9 +212,16 @@ int queue_launch(const Table *dT, Queue *dQ, int k0, int k1, bool accelerate, in
         SCI_QUEUE_CASE(1)
         SCI_QUEUE_CASE(2)
         SCI_QUEUE_CASE(3)
-        default:
-            if (accelerate) k_batch_queue<4, true><<<blocks, tv::WPB * 32, 0, s>>>(dT, dQ, k0, k1);
-            else k_batch_queue<4, false><<<blocks, tv::WPB * 32, 0, s>>>(dT, dQ, k0, k1);
+        default:  // n_iter_max 5: without the 2-column code when no item needs it
+            if (narrow) {
+                if (accelerate) k_batch_queue<4, true><<<blocks, tv::WPB * 32, 0, s>>>(dT, dQ, k0, k1);
+                else k_batch_queue<4, false><<<blocks, tv::WPB * 32, 0, s>>>(dT, dQ, k0, k1);
+            } else {
+                if (accelerate)
+                    k_batch_queue<4, true, false><<<blocks, tv::WPB * 32, 0, s>>>(dT, dQ, k0, k1);
+                else
+                    k_batch_queue<4, false, false><<<blocks, tv::WPB * 32, 0, s>>>(dT, dQ, k0, k1);
+            }
             break;
     }
 #undef SCI_QUEUE_CASE
