@@ -193,6 +193,15 @@ __device__ __forceinline__ void store_row(float *rowp, int col, const Row<CPL> &
     }
 }
 
+// One pixel of the GAP projection x + lam (c phi_b) with phi_b = bit
+// `frame` of the packed mask word w (fbit = 1 << frame): fma(lam, c, x)
+// where the bit is set, x where it is not -- the value of
+// fmaf(lam, c * phi_b, x) (up to the sign of a zero x), in three
+// instructions instead of five.
+__device__ __forceinline__ float proj_px(float lam, float c, float x, uint32_t w, uint32_t fbit) {
+    return (w & fbit) ? fmaf(lam, c, x) : x;
+}
+
 // Input row of frame `frame`: the stored row, or with the GAP projection
 // applied on the fly (same arithmetic as k_proj_gap: x + lam * (c * phi_b)).
 template <int CPL, int MODE, int PROJ>
@@ -204,13 +213,11 @@ __device__ __forceinline__ Row<CPL> load_f(const Pass &P, const float *fb, int f
     const Row<CPL> wb =
         load_row<CPL, MODE>(reinterpret_cast<const float *>(P.bits) + row * W, col, W, vec);
     Row<CPL> f;
+    const uint32_t fbit = 1u << frame;
 #pragma unroll
-    for (int j = 0; j < CPL / 2; ++j) {
-        const float m0 = ((__float_as_uint(lo(wb.q[j])) >> frame) & 1u) ? 1.f : 0.f;
-        const float m1 = ((__float_as_uint(hi(wb.q[j])) >> frame) & 1u) ? 1.f : 0.f;
-        f.q[j] = mk2(fmaf(P.lam, lo(c.q[j]) * m0, lo(x.q[j])),
-                     fmaf(P.lam, hi(c.q[j]) * m1, hi(x.q[j])));
-    }
+    for (int j = 0; j < CPL / 2; ++j)
+        f.q[j] = mk2(proj_px(P.lam, lo(c.q[j]), lo(x.q[j]), __float_as_uint(lo(wb.q[j])), fbit),
+                     proj_px(P.lam, hi(c.q[j]), hi(x.q[j]), __float_as_uint(hi(wb.q[j])), fbit));
     return f;
 }
 

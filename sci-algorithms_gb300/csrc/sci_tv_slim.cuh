@@ -175,13 +175,11 @@ __device__ __forceinline__ Row<CPL> stage0(const Pass &P, const Rings &G, int r,
     if (PROJ) {  // f = x + lam (c phi_b), as the GAP projection rounds it
         const Row<CPL> c = lds<CPL>(G.c, r);
         const Row<CPL> wb = lds<CPL>(G.m, r);
+        const uint32_t fbit = 1u << frame;
 #pragma unroll
-        for (int j = 0; j < NQ; ++j) {
-            const float m0 = ((__float_as_uint(lo(wb.q[j])) >> frame) & 1u) ? 1.f : 0.f;
-            const float m1 = ((__float_as_uint(hi(wb.q[j])) >> frame) & 1u) ? 1.f : 0.f;
-            u.q[j] = mk2(fmaf(P.lam, lo(c.q[j]) * m0, lo(u.q[j])),
-                         fmaf(P.lam, hi(c.q[j]) * m1, hi(u.q[j])));
-        }
+        for (int j = 0; j < NQ; ++j)
+            u.q[j] = mk2(proj_px(P.lam, lo(c.q[j]), lo(u.q[j]), __float_as_uint(lo(wb.q[j])), fbit),
+                         proj_px(P.lam, hi(c.q[j]), hi(u.q[j]), __float_as_uint(hi(wb.q[j])), fbit));
         sts<CPL>(G.x, r, u);
     }
     return u;
