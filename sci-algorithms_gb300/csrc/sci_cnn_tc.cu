@@ -451,6 +451,202 @@ __global__ void __launch_bounds__(kThr, 3)
                      : "memory");
 }
 
+// Row-segment tiles read by the tensor cores in place (k_conv_thin_rd, the
+// default): the staged input rows are [row dy][pixel][8 channels], 16 bytes
+// per pixel, which is the K-major core-matrix layout of an A operand whose
+// rows are consecutive pixels (8 rows of 16 bytes = 128 contiguous bytes,
+// 8-row groups 128 bytes apart).  Tap (dy, dx) of output pixel m is staged
+// pixel m + dx of row dy, so a pair of taps is one descriptor: start at the
+// first tap's pixel 0, leading byte offset = the second tap's distance
+// (16 bytes within a row, or a row minus 32 bytes from dx = 2 to the next
+// row's dx = 0).  The five MMAs take taps (0,1), (2,3), (4,5), (6,7) and
+// (7,8), the weights of the last pair being (zero, tap 8), so no read
+// leaves the tile's three rows and no im2col copy is built.  Pixels outside
+// the frame are zeroed in the staged rows before the MMAs (the bulk copies
+// skip them); a buffer is refilled, two tiles ahead, once its MMAs are done.
+constexpr int kRowStride = kRowPx * 16;   // bytes of one staged row
+constexpr int kSmemRd = 56 * 1024;        // 4 blocks per SM
+
+template <int N>
+struct alignas(1024) RdSmem {
+    uint8_t b[(N / 8) * kSBO];  // weights, K chunks (tap 0..7, zero, tap 8)
+    uint8_t stage[kM * N * 2];
+    uint8_t rows[2][kRowBuf];
+    float bias[N];
+    uint64_t rbar[2];
+    uint64_t bar;
+    uint32_t tmem;
+};
+
+// Descriptor with explicit leading / stride byte offsets (no swizzle).
+__device__ __forceinline__ uint64_t smem_desc_lbo(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+
+template <int N>
+__global__ void __launch_bounds__(kThr, 4)
+    k_conv_thin_rd(const uint4 *__restrict__ in, const uint4 *__restrict__ wts,
+                   const float *__restrict__ bias, uint4 *__restrict__ out, int64_t F,
+                   int64_t H, int64_t W, int relu) {
+    static_assert(N % 32 == 0 && N >= 32 && N <= 256, "N: multiple of 32 up to 256");
+    static_assert(sizeof(RdSmem<N>) + 1024 <= kSmemRd, "shared memory layout too large");
+    extern __shared__ uint8_t smem_raw[];
+    RdSmem<N> &s = *reinterpret_cast<RdSmem<N> *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
+    // weights: chunk 8 (zeros) and chunk 9 (tap 8) change places
+    for (int i = tid; i < N * kKC; i += kThr) {
+        const int n = i / kKC, kc = i % kKC;
+        const int dkc = kc == 8 ? 9 : (kc == 9 ? 8 : kc);
+        *reinterpret_cast<uint4 *>(s.b + (n >> 3) * kSBO + dkc * kCore + (n & 7) * 16) = wts[i];
+    }
+    for (int i = tid; i < N; i += kThr) s.bias[i] = bias[i];
+    const int64_t nseg = (W + kM - 1) / kM, ntiles = F * H * nseg;
+    const int64_t G = gridDim.x;
+    if (tid == 0) {
+        mbar_init(&s.bar, 1);
+        mbar_init(s.rbar + 0, 1);
+        mbar_init(s.rbar + 1, 1);
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        const int64_t t0 = blockIdx.x;
+        if (t0 < ntiles) issue_rows(in, s.rows[0], s.rbar + 0, t0, H, W, nseg);
+        if (t0 + G < ntiles) issue_rows(in, s.rows[1], s.rbar + 1, t0 + G, H, W, nseg);
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(&s.tmem)),
+                     "r"(kTmemCols)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = s.tmem;
+    const uint32_t b_addr = smem_u32(s.b);
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+    // (first tap's byte offset in the staged rows, leading byte offset) of the five MMAs
+    constexpr uint32_t a_off[5] = {0u, 32u, (uint32_t)kRowStride + 16u, 2u * kRowStride,
+                                   2u * kRowStride + 16u};
+    constexpr uint32_t a_lbo[5] = {16u, (uint32_t)kRowStride - 32u, 16u, 16u, 16u};
+    unsigned phase = 0;
+    int i = 0;
+    for (int64_t t = blockIdx.x; t < ntiles; t += G, ++i) {
+        const int buf = i & 1;
+        const RowTile r = row_tile(t, H, W, nseg);
+        const bool rows_ok = mbar_wait(s.rbar + buf, (unsigned)(i >> 1) & 1u);
+        if (__syncthreads_or(!rows_ok)) {
+            if (tid == 0) {
+                atomicOr(&g_cnn_status, 1u);
+                mbar_wait(s.rbar + buf, (unsigned)(i >> 1) & 1u);
+                if (t + G < ntiles) mbar_wait(s.rbar + (buf ^ 1), (unsigned)((i + 1) >> 1) & 1u);
+            }
+            break;
+        }
+        // zeros for the staged pixels outside the frame: whole rows above or
+        // below it, column x0 - 1 of the first segment, columns >= W of the last
+        {
+            uint4 *rw = reinterpret_cast<uint4 *>(s.rows[buf]);
+            const int px_hi = (int)((W - (r.x0 - 1)) < kRowPx ? (W - (r.x0 - 1)) : kRowPx);
+#pragma unroll
+            for (int dy = 0; dy < 3; ++dy) {
+                const int64_t yy = r.y + dy - 1;
+                if (yy < 0 || yy >= H) {
+                    for (int px = tid; px < kRowPx; px += kThr) rw[dy * kRowPx + px] = zero;
+                } else {
+                    if (r.x0 == 0 && tid == 0) rw[dy * kRowPx] = zero;
+                    for (int px = px_hi + tid; px < kRowPx; px += kThr) rw[dy * kRowPx + px] = zero;
+                }
+            }
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        tc_fence_before();  // the previous tile's tcgen05.ld before the barrier
+        __syncthreads();
+        tc_fence_after();
+        if (tid == 0) {
+            const uint32_t rows_addr = smem_u32(s.rows[buf]);
+#pragma unroll
+            for (int kk = 0; kk < kKC / 2; ++kk)
+                tc_mma(tmem, smem_desc_lbo(rows_addr + a_off[kk], a_lbo[kk], 128u),
+                       smem_desc(b_addr + kk * 2 * kCore), instr_desc<N>(), kk > 0 ? 1u : 0u);
+            tc_commit(&s.bar);
+        }
+        const bool ok = mbar_wait(&s.bar, phase);
+        if (tid == 0) {
+            asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+            // this buffer's MMAs are done: refill it two tiles ahead
+            if (ok && t + 2 * G < ntiles)
+                issue_rows(in, s.rows[buf], s.rbar + buf, t + 2 * G, H, W, nseg);
+        }
+        if (__syncthreads_or(!ok)) {
+            if (tid == 0) {
+                atomicOr(&g_cnn_status, 1u);
+                mbar_wait(&s.bar, phase);
+                if (t + G < ntiles) mbar_wait(s.rbar + (buf ^ 1), (unsigned)((i + 1) >> 1) & 1u);
+            }
+            break;
+        }
+        phase ^= 1u;
+        tc_fence_after();
+        uint4 *srow = reinterpret_cast<uint4 *>(s.stage) + tid * (N / 8);
+#pragma unroll
+        for (int c0 = 0; c0 < N; c0 += 32) {
+            uint32_t rr[32];
+            tc_ld32(lane_base + (uint32_t)c0, rr);
+            uint4 *o = srow + c0 / 8;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                uint32_t w4[4];
+#pragma unroll
+                for (int e = 0; e < 4; ++e) {
+                    const int j = q * 8 + e * 2;
+                    float v0 = __uint_as_float(rr[j]) + s.bias[c0 + j];
+                    float v1 = __uint_as_float(rr[j + 1]) + s.bias[c0 + j + 1];
+                    if (relu) {
+                        v0 = fmaxf(v0, 0.f);
+                        v1 = fmaxf(v1, 0.f);
+                    }
+                    const __nv_bfloat162 h = __floats2bfloat162_rn(v0, v1);
+                    w4[e] = *reinterpret_cast<const uint32_t *>(&h);
+                }
+                o[q] = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+            }
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncthreads();
+        if (tid == 0) {
+            const int64_t p0 = (r.f * H + r.y) * W + r.x0;
+            bulk_s2g(out + p0 * (N / 8), s.stage, (unsigned)(r.nv * N * 2));
+        }
+    }
+    if (tid == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                     "r"(kTmemCols)
+                     : "memory");
+}
+
+template <int N>
+int launch_rd(const void *in, const void *wts, const float *bias, void *out, int64_t F,
+              int64_t H, int64_t W, int relu, cudaStream_t st) {
+    const int64_t ntiles = F * H * ((W + kM - 1) / kM);
+    const int64_t cap = int64_t(kSMs) * 4;
+    const int grid = int(ntiles < cap ? ntiles : cap);
+    SCI_CUDA(cudaFuncSetAttribute(k_conv_thin_rd<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  kSmemRd));
+    k_conv_thin_rd<N><<<grid, kThr, kSmemRd, st>>>(
+        reinterpret_cast<const uint4 *>(in), reinterpret_cast<const uint4 *>(wts), bias,
+        reinterpret_cast<uint4 *>(out), F, H, W, relu);
+    SCI_LAUNCHED("k_conv_thin_rd");
+    return SCI_OK;
+}
+
 template <int N>
 int launch_rows(const void *in, const void *wts, const float *bias, void *out, int64_t F,
                 int64_t H, int64_t W, int relu, cudaStream_t st) {
@@ -485,14 +681,18 @@ int launch_thin(const void *in, const void *wts, const float *bias, void *out, i
 // for 8 x 2048 x 2048 -> 96 channels against 1.99 ms for the per-pixel
 // gather (SCI_THIN_ROWS=0); the gather with a second A buffer and the next
 // tile's copies in flight (2 blocks per SM) measured 2.37 ms.
+// SCI_THIN_ROWS: 2 (the default) the staged rows read in place by the
+// MMAs, 1 the im2col rows built from the staged rows, 0 the per-pixel
+// gather.
 template <int N>
 int launch_thin_n(const void *in, const void *wts, const float *bias, void *out, int64_t F,
                   int64_t H, int64_t W, int relu, cudaStream_t st) {
-    static const bool rows = [] {
+    static const int form = [] {
         const char *e = getenv("SCI_THIN_ROWS");
-        return !(e && e[0] == '0');
+        return e ? atoi(e) : 2;
     }();
-    if (rows) return launch_rows<N>(in, wts, bias, out, F, H, W, relu, st);
+    if (form >= 2) return launch_rd<N>(in, wts, bias, out, F, H, W, relu, st);
+    if (form == 1) return launch_rows<N>(in, wts, bias, out, F, H, W, relu, st);
     return launch_thin<N>(in, wts, bias, out, F, H, W, relu, st);
 }
 
