@@ -37,6 +37,19 @@ bool pdl_enabled() {
     return !(e && atoi(e) == 0);
 }
 
+// Sweep direction of the residual passes of the fused iterations.  The TV
+// pass walks its row chunks top to bottom, so the last rows it wrote are
+// the ones still in L2 when the residual pass starts; a residual pass that
+// walks bottom to top reads them there, and ends on the top rows, which
+// the next TV pass reads first.  SCI_RESID_REV=0 keeps top to bottom.
+static int resid_rev() {
+    static const int v = [] {
+        const char *e = getenv("SCI_RESID_REV");
+        return (e && atoi(e) == 0) ? 0 : 1;
+    }();
+    return v;
+}
+
 int launch_proj_gap_tma(const float *x, const uint32_t *bits, const float *y, float *y1,
                         const float *phisum, float *xo, float lam, bool acc, int B, int64_t hw,
                         cudaStream_t s, double *rn);
@@ -350,7 +363,7 @@ template <int MODE, bool ACC>
 __global__ void __launch_bounds__(256) k_gap_resid_vec(
     const float *__restrict__ x, Mask<MODE> M, const float *__restrict__ y,
     float *__restrict__ y1, const float *__restrict__ phisum, float *__restrict__ c, int B,
-    int64_t hw, double *__restrict__ rn, double *__restrict__ zero, int nzero) {
+    int64_t hw, double *__restrict__ rn, double *__restrict__ zero, int nzero, int rev) {
     grid_dep_wait();
     if (blockIdx.x == 0)  // the next TV pass's stop-test sums
         for (int i = threadIdx.x; i < nzero; i += blockDim.x) zero[i] = 0.0;
@@ -358,7 +371,7 @@ __global__ void __launch_bounds__(256) k_gap_resid_vec(
     double racc = 0.0;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n4;
          q += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t p = q << 2;
+        const int64_t p = (rev ? n4 - 1 - q : q) << 2;  // rev: bottom rows first
         const uint4 w = M.word4(p);
         float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll 4
@@ -404,7 +417,7 @@ __global__ void __launch_bounds__(256) k_admm_resid_vec(
     const float *__restrict__ tp, Mask<1> M, const float *__restrict__ y,
     const float *__restrict__ phisum, float *__restrict__ rnew, float *__restrict__ xo, float lam,
     float gamma, int B, int64_t hw, double *__restrict__ rn, double *__restrict__ zero,
-    int nzero) {
+    int nzero, int rev) {
     grid_dep_wait();
     if (blockIdx.x == 0)  // the next TV pass's stop-test sums
         for (int i = threadIdx.x; i < nzero; i += blockDim.x) zero[i] = 0.0;
@@ -416,7 +429,7 @@ __global__ void __launch_bounds__(256) k_admm_resid_vec(
     double racc = 0.0;
     for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < n4;
          q += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t p = q << 2;
+        const int64_t p = (rev ? n4 - 1 - q : q) << 2;
         const uint4 w = M.word4(p);
         float4 s = make_float4(0.f, 0.f, 0.f, 0.f);
 #pragma unroll 4
@@ -627,15 +640,15 @@ int gap_residual_rn(const float *x, const float *phi, const uint32_t *mask_bits,
     if (mask_bits) {
         Mask<1> M{mask_bits, hw};
         if (accelerate) SCI_CUDA(launch_dep(k_gap_resid_vec<1, true>, g, dim3(256), 0, s, x, M, y, y1,
-                                        phisum, c, (int)B, hw, rn, zero, nzero));
+                                        phisum, c, (int)B, hw, rn, zero, nzero, resid_rev()));
         else SCI_CUDA(launch_dep(k_gap_resid_vec<1, false>, g, dim3(256), 0, s, x, M, y, y1,
-                                        phisum, c, (int)B, hw, rn, zero, nzero));
+                                        phisum, c, (int)B, hw, rn, zero, nzero, resid_rev()));
     } else {
         Mask<0> M{phi, hw};
         if (accelerate) SCI_CUDA(launch_dep(k_gap_resid_vec<0, true>, g, dim3(256), 0, s, x, M, y, y1,
-                                        phisum, c, (int)B, hw, rn, zero, nzero));
+                                        phisum, c, (int)B, hw, rn, zero, nzero, resid_rev()));
         else SCI_CUDA(launch_dep(k_gap_resid_vec<0, false>, g, dim3(256), 0, s, x, M, y, y1,
-                                        phisum, c, (int)B, hw, rn, zero, nzero));
+                                        phisum, c, (int)B, hw, rn, zero, nzero, resid_rev()));
     }
     SCI_LAUNCHED("k_gap_resid");
     return SCI_OK;
@@ -659,7 +672,7 @@ int admm_residual_rn(const float *t, const uint32_t *mask_bits, const float *y,
     Mask<1> M{mask_bits, hw};
 #define SCI_ADMM_RESID(F, X)                                                                  \
     SCI_CUDA(launch_dep(k_admm_resid_vec<F, X>, g, dim3(256), 0, s, t, M, y, phisum, r_new,   \
-                        x_out, lambda, gamma, (int)B, hw, rn, zero, nzero))
+                        x_out, lambda, gamma, (int)B, hw, rn, zero, nzero, resid_rev()))
     if (first) {
         if (x_out) SCI_ADMM_RESID(true, true);
         else SCI_ADMM_RESID(true, false);
