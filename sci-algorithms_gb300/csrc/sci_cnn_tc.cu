@@ -26,14 +26,21 @@
 // them; k_conv_thin_tc takes any 128 consecutive pixels and gathers each
 // row's nine taps from global memory by cp.async.
 //
+// k_conv_thin_rd (the default) reads the staged rows in place through
+// tap-shifted descriptors and writes its output tile with tensor stores
+// from a swizzled stage (see the comments at the kernel).
+//
 // Persistent blocks of 128 threads; 64 / 74 KiB of shared memory per block
-// caps residency at 3 blocks per SM (3 x 128 of the SM's 512 TMEM columns).
+// caps residency at 3 blocks per SM for the im2col and gather forms, 56 KiB
+// at 4 for k_conv_thin_rd (4 x 128 = the SM's 512 TMEM columns).
 // The wait for each tile's MMAs is bounded: on timeout the block sets bit 0
 // of the CNN status word, waits once more (bounded) for the MMAs in
 // flight, frees its tensor memory and returns.
+#include <cuda.h>  // CUtensorMap; the encoder is fetched through the runtime
 #include <cuda_bf16.h>
 
 #include <cstdlib>
+#include <cstring>
 
 #include "sci_bulk.cuh"
 #include "sci_common.cuh"
@@ -470,13 +477,36 @@ constexpr int kSmemRd = 56 * 1024;        // 4 blocks per SM
 template <int N>
 struct alignas(1024) RdSmem {
     uint8_t b[(N / 8) * kSBO];  // weights, K chunks (tap 0..7, zero, tap 8)
-    uint8_t stage[kM * N * 2];
+    alignas(1024) uint8_t stage[kM * N * 2];
     uint8_t rows[2][kRowBuf];
-    float bias[N];
+    alignas(16) float bias[N];
     uint64_t rbar[2];
     uint64_t bar;
     uint32_t tmem;
 };
+
+// Output tile staged for tensor stores (TM): boxes of 64 channels (128-byte
+// pixel rows, 128-byte swizzle: 16-byte chunk k of pixel t at chunk
+// k ^ (t & 7)) and, when N % 64 == 32, one box of 32 channels (64-byte
+// rows, 64-byte swizzle: chunk k ^ ((t >> 1) & 3)).  Either way the eight
+// pixels of a quarter warp write eight different 16-byte bank groups; the
+// plain pixel-major stage (N * 2 bytes per pixel) puts them on two.
+template <int N>
+__device__ __forceinline__ uint32_t stage_off(int kc, int t) {
+    constexpr int nA = N / 64;
+    if (kc < 8 * nA)
+        return (uint32_t)((kc >> 3) * 16384 + t * 128 + (((kc & 7) ^ (t & 7)) << 4));
+    return (uint32_t)(nA * 16384 + t * 64 + (((kc - 8 * nA) ^ ((t >> 1) & 3)) << 4));
+}
+
+__device__ __forceinline__ void tma_store3(const CUtensorMap *m, const void *src, int c, int x,
+                                           int row) {
+    asm volatile(
+        "cp.async.bulk.tensor.3d.global.shared::cta.bulk_group [%0, {%1, %2, %3}], [%4];" ::"l"(
+            reinterpret_cast<uint64_t>(m)),
+        "r"(c), "r"(x), "r"(row), "r"(smem_u32(src))
+        : "memory");
+}
 
 // Descriptor with explicit leading / stride byte offsets (no swizzle).
 __device__ __forceinline__ uint64_t smem_desc_lbo(uint32_t addr, uint32_t lbo, uint32_t sbo) {
@@ -484,11 +514,12 @@ __device__ __forceinline__ uint64_t smem_desc_lbo(uint32_t addr, uint32_t lbo, u
            ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
 }
 
-template <int N>
+template <int N, bool TM>
 __global__ void __launch_bounds__(kThr, 4)
     k_conv_thin_rd(const uint4 *__restrict__ in, const uint4 *__restrict__ wts,
                    const float *__restrict__ bias, uint4 *__restrict__ out, int64_t F,
-                   int64_t H, int64_t W, int relu) {
+                   int64_t H, int64_t W, int relu, const __grid_constant__ CUtensorMap tm64,
+                   const __grid_constant__ CUtensorMap tm32) {
     static_assert(N % 32 == 0 && N >= 32 && N <= 256, "N: multiple of 32 up to 256");
     static_assert(sizeof(RdSmem<N>) + 1024 <= kSmemRd, "shared memory layout too large");
     extern __shared__ uint8_t smem_raw[];
@@ -592,20 +623,21 @@ __global__ void __launch_bounds__(kThr, 4)
         }
         phase ^= 1u;
         tc_fence_after();
-        uint4 *srow = reinterpret_cast<uint4 *>(s.stage) + tid * (N / 8);
 #pragma unroll
         for (int c0 = 0; c0 < N; c0 += 32) {
             uint32_t rr[32];
             tc_ld32(lane_base + (uint32_t)c0, rr);
-            uint4 *o = srow + c0 / 8;
 #pragma unroll
             for (int q = 0; q < 4; ++q) {
+                const float4 *b4 = reinterpret_cast<const float4 *>(s.bias + c0 + q * 8);
+                const float4 ba = b4[0], bb = b4[1];
+                const float bv[8] = {ba.x, ba.y, ba.z, ba.w, bb.x, bb.y, bb.z, bb.w};
                 uint32_t w4[4];
 #pragma unroll
                 for (int e = 0; e < 4; ++e) {
                     const int j = q * 8 + e * 2;
-                    float v0 = __uint_as_float(rr[j]) + s.bias[c0 + j];
-                    float v1 = __uint_as_float(rr[j + 1]) + s.bias[c0 + j + 1];
+                    float v0 = __uint_as_float(rr[j]) + bv[2 * e];
+                    float v1 = __uint_as_float(rr[j + 1]) + bv[2 * e + 1];
                     if (relu) {
                         v0 = fmaxf(v0, 0.f);
                         v1 = fmaxf(v1, 0.f);
@@ -613,14 +645,24 @@ __global__ void __launch_bounds__(kThr, 4)
                     const __nv_bfloat162 h = __floats2bfloat162_rn(v0, v1);
                     w4[e] = *reinterpret_cast<const uint32_t *>(&h);
                 }
-                o[q] = make_uint4(w4[0], w4[1], w4[2], w4[3]);
+                const int kc = c0 / 8 + q;
+                const uint32_t off = TM ? stage_off<N>(kc, tid) : (uint32_t)(tid * N * 2 + kc * 16);
+                *reinterpret_cast<uint4 *>(s.stage + off) = make_uint4(w4[0], w4[1], w4[2], w4[3]);
             }
         }
         asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         __syncthreads();
         if (tid == 0) {
-            const int64_t p0 = (r.f * H + r.y) * W + r.x0;
-            bulk_s2g(out + p0 * (N / 8), s.stage, (unsigned)(r.nv * N * 2));
+            if (TM) {
+                const int row = (int)(r.f * H + r.y), x = (int)r.x0;
+#pragma unroll
+                for (int i = 0; i < N / 64; ++i) tma_store3(&tm64, s.stage + i * 16384, i * 64, x, row);
+                if (N % 64) tma_store3(&tm32, s.stage + (N / 64) * 16384, (N / 64) * 64, x, row);
+                asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+            } else {
+                const int64_t p0 = (r.f * H + r.y) * W + r.x0;
+                bulk_s2g(out + p0 * (N / 8), s.stage, (unsigned)(r.nv * N * 2));
+            }
         }
     }
     if (tid == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
@@ -632,17 +674,70 @@ __global__ void __launch_bounds__(kThr, 4)
                      : "memory");
 }
 
+using EncodeTiledFn = CUresult (*)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                   const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                   const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                   CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+static EncodeTiledFn tensor_map_encoder() {
+    static const EncodeTiledFn fn = [] {
+        void *p = nullptr;
+        cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000,
+                                             cudaEnableDefault, &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<EncodeTiledFn>(p);
+    }();
+    return fn;
+}
+
+// Tensor map of the NHWC bf16 output: dims (N channels, W, F H rows), box
+// (bc channels, 128 pixels, 1 row), swizzle matching stage_off; pixels past
+// the row end of a tile are clipped by the store.
+static bool out_map(CUtensorMap *m, void *out, int64_t F, int64_t H, int64_t W, int N, int bc) {
+    const EncodeTiledFn enc = tensor_map_encoder();
+    if (!enc || F * H > INT32_MAX || W > INT32_MAX) return false;
+    const cuuint64_t dims[3] = {(cuuint64_t)N, (cuuint64_t)W, (cuuint64_t)(F * H)};
+    const cuuint64_t strides[2] = {(cuuint64_t)N * 2, (cuuint64_t)W * (cuuint64_t)N * 2};
+    const cuuint32_t box[3] = {(cuuint32_t)bc, (cuuint32_t)kM, 1u};
+    const cuuint32_t es[3] = {1u, 1u, 1u};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, out, dims, strides, box, es,
+               CU_TENSOR_MAP_INTERLEAVE_NONE,
+               bc == 64 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B,
+               CU_TENSOR_MAP_L2_PROMOTION_NONE, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// SCI_THIN_TMA=0: the staged tile written by one plain bulk copy (pixel-major
+// stage) instead of swizzled tensor stores.
+static bool thin_tma() {
+    static const bool v = [] {
+        const char *e = getenv("SCI_THIN_TMA");
+        return !(e && atoi(e) == 0);
+    }();
+    return v;
+}
+
 template <int N>
 int launch_rd(const void *in, const void *wts, const float *bias, void *out, int64_t F,
               int64_t H, int64_t W, int relu, cudaStream_t st) {
     const int64_t ntiles = F * H * ((W + kM - 1) / kM);
     const int64_t cap = int64_t(kSMs) * 4;
     const int grid = int(ntiles < cap ? ntiles : cap);
-    SCI_CUDA(cudaFuncSetAttribute(k_conv_thin_rd<N>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                  kSmemRd));
-    k_conv_thin_rd<N><<<grid, kThr, kSmemRd, st>>>(
-        reinterpret_cast<const uint4 *>(in), reinterpret_cast<const uint4 *>(wts), bias,
-        reinterpret_cast<uint4 *>(out), F, H, W, relu);
+    CUtensorMap m64, m32;
+    memset(&m64, 0, sizeof(m64));
+    memset(&m32, 0, sizeof(m32));
+    bool tm = thin_tma() && out_map(&m64, out, F, H, W, N, 64);
+    if (tm && N % 64) tm = out_map(&m32, out, F, H, W, N, 32);
+    auto go = [&](auto kern) -> int {
+        SCI_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, kSmemRd));
+        kern<<<grid, kThr, kSmemRd, st>>>(reinterpret_cast<const uint4 *>(in),
+                                          reinterpret_cast<const uint4 *>(wts), bias,
+                                          reinterpret_cast<uint4 *>(out), F, H, W, relu, m64, m32);
+        return SCI_OK;
+    };
+    const int rc = tm ? go(k_conv_thin_rd<N, true>) : go(k_conv_thin_rd<N, false>);
+    if (rc != SCI_OK) return rc;
     SCI_LAUNCHED("k_conv_thin_rd");
     return SCI_OK;
 }
