@@ -448,6 +448,26 @@ int sci_cnn_conv_thin(const void *in, const void *weights, const float *bias,
                       void *out, int64_t nframes, int64_t H, int64_t W, int N,
                       int relu, void *stream);
 
+/* FastDVDnet's DenBlock tail in one pass on the tensor cores, bfloat16
+ * operands, float32 accumulation:
+ *   h = x0 + PixelShuffle(2)(u1), o0 = ReLU(conv3x3(h, w0) + b0) (bfloat16),
+ *   e = conv3x3(o0, w1) + b1 (float32), out[k] = src[first + k] - e,
+ * src reflect-padded to Hp x Wp as in sci_cnn_center_sub, out cropped to
+ * Ho x Wo and clipped to [0, 1] when clip != 0 (count x Ho x Wo float32).
+ * x0: count x Hp x Wp x 32 bfloat16 (NHWC); u1: count x Hp/2 x Wp/2 x 128
+ * bfloat16 with the upsampling convolution's channels sub-pixel-major (as
+ * sci_cnn_shuffle_add); w0: 32 x 288 bfloat16 (k = (3 dy + dx) * 32 + c),
+ * b0: 32 float32; w1: 288 bfloat16 (the one output filter), b1: one
+ * float32 or NULL (zero).  Both convolutions zero-pad by 1.  Hp, Wp even.
+ * A timed-out device-side wait sets bit 0 of the status word of
+ * sci_device_status.  Replaces DenBlock.forward's x0 + x1, OutputCvBlock
+ * and in1 - x (packages/fastdvdnet/models.py:86-100, :203-205) and the
+ * crop of fastdvdnet.py:136-140. */
+int sci_cnn_den_tail(const void *x0, const void *u1, const void *w0, const float *b0,
+                     const void *w1, const float *b1, const float *src, int64_t nframes,
+                     int64_t Hs, int64_t Ws, int64_t first, int64_t count, int64_t Hp,
+                     int64_t Wp, int64_t Ho, int64_t Wo, int clip, float *out, void *stream);
+
 /* Per-frame image-quality sums of x against orig (planar nframes x H x W,
  * H, W >= 7): sqerr[f] = sum (orig - x)^2 over frame f, and ssim_sum[f] =
  * the sum of the SSIM map (7 x 7 uniform windows, sample covariance, K1 =

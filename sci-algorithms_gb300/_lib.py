@@ -110,6 +110,8 @@ _SIGS = {
     "sci_cnn_shuffle_add_f32": [c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_i64, c_vp],
     "sci_cnn_conv_thin": [c_vp, c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, ctypes.c_int,
                           ctypes.c_int, c_vp],
+    "sci_cnn_den_tail": [c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_i64,
+                         c_i64, c_i64, c_i64, c_i64, c_i64, ctypes.c_int, c_vp, c_vp],
     "sci_unrolled_workspace_bytes": [c_i64, c_i64, c_i64, c_i64, ctypes.c_int, ctypes.c_int,
                                      ctypes.POINTER(c_sz)],
     "sci_unrolled_fwd": [c_vp, c_vp, c_vp, c_i64, c_i64, c_i64, c_i64, ctypes.c_int,

@@ -401,6 +401,11 @@ class CnnEngine:
         # first layer on the tensor cores by this library's tcgen05 kernel
         # (bf16 only; SCI_CNN_TC=0 leaves it to cuDNN)
         self.tc = self.bf16 and os.environ.get("SCI_CNN_TC", "1") != "0"
+        # FastDVDnet's DenBlock tail (full-resolution shuffle + add, the two
+        # output convolutions, centre - output) in one tcgen05 kernel
+        # (bf16 only; SCI_CNN_TAIL=0 runs it as shuffle-add, two cuDNN
+        # convolutions and the centre subtraction)
+        self.tail = self.tc and os.environ.get("SCI_CNN_TAIL", "1") != "0"
         self.graphs = graphs
         self.chunk_bytes = chunk_bytes
         self.dev = _dev.device()
@@ -453,12 +458,19 @@ class CnnEngine:
                         p[name] = _fold(conv, bn, dt, cin_pad=96, cl=True)
                     elif name == "o1":
                         p[name] = _fold(conv, bn, dt, cout_pad=8, cl=True)
+                        if self.tail:
+                            w1 = p[name][0][0].permute(1, 2, 0).reshape(-1).contiguous()
+                            p["tail_o1"] = (w1, None)
                     elif name in ("u2c", "u1c"):
                         w, b = _fold(conv, bn, dt)
                         p[name] = (_subpixel_major(w).contiguous(
                             memory_format=torch.channels_last), b)
                     else:
                         p[name] = _fold(conv, bn, dt, cl=True)
+                        if name == "o0" and self.tail:
+                            w0, b0 = p[name]
+                            p["tail_o0"] = (w0.permute(0, 2, 3, 1).reshape(32, 288).contiguous(),
+                                            b0.float().contiguous())
                 self.blocks.append(p)
         self._versions = self._param_versions()
         self._graphs.clear()
@@ -494,9 +506,9 @@ class CnnEngine:
              noise.shape[-1], int(clip), out.data_ptr(), s)
 
     # -- FastDVDnet ----------------------------------------------------------
-    def _denblock(self, p, win):
-        """DenBlock body on a prepared window tensor; returns the network
-        output r (before `centre - r`)."""
+    def _denblock(self, p, win, src, Hs, Ws, first, count, Hp, Wp, Ho, Wo, clip, out):
+        """DenBlock on a prepared window tensor, then out = centre - DenBlock
+        (cropped to Ho x Wo, clipped when `clip`)."""
         tf = self.precision == "tf32"
 
         def c(x, name, stride=1, relu=True):
@@ -509,7 +521,15 @@ class CnnEngine:
         u2 = c(c(c(x2, "u2a"), "u2b"), "u2c", relu=False)
         x1 = self._shuffle_add(x1, u2)
         u1 = c(c(c(x1, "u1a"), "u1b"), "u1c", relu=False)
-        return c(c(self._shuffle_add(x0, u1), "o0"), "o1", relu=False)
+        if self.tail:
+            x0n, u1n = self._dense(x0), self._dense(u1)
+            (w0, b0), (w1, _) = p["tail_o0"], p["tail_o1"]
+            call("sci_cnn_den_tail", x0n.data_ptr(), u1n.data_ptr(), w0.data_ptr(),
+                 b0.data_ptr(), w1.data_ptr(), None, src.data_ptr(), src.shape[0], Hs, Ws, first,
+                 count, Hp, Wp, Ho, Wo, int(clip), out.data_ptr(), _dev.stream_handle())
+            return
+        r = c(c(self._shuffle_add(x0, u1), "o0"), "o1", relu=False)
+        self._center_sub(src, Hs, Ws, first, count, r, Hp, Wp, Ho, Wo, clip, out)
 
     def _shuffle_add(self, a, u):
         """a + PixelShuffle(2)(u) on NHWC tensors (u's channels in
@@ -548,13 +568,13 @@ class CnnEngine:
         T = torch.empty((Fn, Hp, Wp), device=x.device)
         for a in range(0, Fn, step):
             n = min(step, Fn - a)
-            r = self._denblock(self.blocks[0], self._window(x, H, W, Hp, Wp, a, n))
-            self._center_sub(x, H, W, a, n, r, Hp, Wp, Hp, Wp, False, T[a:a + n])
+            self._denblock(self.blocks[0], self._window(x, H, W, Hp, Wp, a, n), x, H, W, a, n,
+                           Hp, Wp, Hp, Wp, False, T[a:a + n])
         # second stage over the windows of T, cropped back to H x W
         for a in range(0, Fn, step):
             n = min(step, Fn - a)
-            r = self._denblock(self.blocks[1], self._window(T, Hp, Wp, Hp, Wp, a, n))
-            self._center_sub(T, Hp, Wp, a, n, r, Hp, Wp, H, W, clip, out[a:a + n])
+            self._denblock(self.blocks[1], self._window(T, Hp, Wp, Hp, Wp, a, n), T, Hp, Wp, a,
+                           n, Hp, Wp, H, W, clip, out[a:a + n])
 
     def _bytes_per_frame(self, Hp, Wp):
         # live activations of one DenBlock call at full resolution (~4

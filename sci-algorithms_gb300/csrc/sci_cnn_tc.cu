@@ -772,6 +772,377 @@ int launch_thin(const void *in, const void *wts, const float *bias, void *out, i
     return SCI_OK;
 }
 
+// ------------------------------------------------------- DenBlock tail
+// FastDVDnet's DenBlock after its last upsampling convolution, one pass per
+// column strip of a frame (packages/fastdvdnet/models.py:86-100, :203-205):
+//   h  = x0 + PixelShuffle(2)(u1)                    32 channels, bfloat16
+//   o0 = ReLU(conv3x3(h, w0) + b0)                   32 -> 32, bfloat16
+//   e  = conv3x3(o0, w1) + b1                        32 -> 1, float32
+//   out = centre frame - e  (cropped, clipped)       float32 planes
+// Rows stream through shared memory top to bottom: per row step the x0
+// row and the u1 half row are loaded by TMA (one step ahead) and summed
+// into an h row, and one batch of MMAs computes an o0 row and the output
+// row two rows above it (implicit GEMMs, M = 128 pixels, K = 9 taps x 32
+// channels = 18 MMAs of K 16 each, float32 accumulators in TMEM), reading
+// rings of three h rows and four o0 rows in place through tap-shifted
+// descriptors, as k_conv_thin_rd does; the centre pixels are loaded while
+// the batch runs.  A staged row holds 130
+// pixels as four 8-channel planes (pixel p of plane j at j * 2080 + 16 p:
+// the K-major core-matrix layout, K-adjacent chunks one plane apart).  o0
+// is computed for the strip's 126 output columns plus one on each side
+// (128 = one MMA tile); o0 values outside the frame are zero (the zero
+// padding of the second convolution).  Waits are bounded as in the thin
+// convolution.
+constexpr int kTailSeg = 126;                    // output columns per strip
+constexpr int kTailPx = 130;                     // staged h pixels per row
+constexpr int kTailPlane = kTailPx * 16;         // one 8-channel plane of a row
+constexpr int kTailRow = 4 * kTailPlane;         // 32 channels
+constexpr int kTailKC = 36;                      // 16-byte K chunks of a 3 x 3 x 32 filter
+constexpr int kTailSBO = kTailKC * kCore;        // 8-row groups of a weight operand
+constexpr int kTailTmem = 128;  // o0 accumulators at columns 0-31, 32-63; e at 64-79, 96-111
+constexpr unsigned kTailLoad = kTailPx * 64 + 65 * 128;  // bytes of one row's two TMA boxes
+
+struct alignas(1024) TailSmem {
+    uint8_t sx[kTailPx * 64];              // x0 row: 130 px x 32 ch, 64-byte swizzle
+    alignas(1024) uint8_t su[65 * 128];    // u1 half row: 65 px x 64 ch, 128-byte swizzle
+    alignas(16) uint8_t h[4][kTailRow];
+    alignas(16) uint8_t o[4][kTailRow];
+    alignas(16) uint8_t w0[4 * kTailSBO];  // 32 filters
+    // the output filter per row dy as 16 x 32 operands: filter n = 3 dy + dx
+    // holds tap (dy, dx), the others zero, so the three rows' MMAs
+    // accumulate D[m, 3 dy + dx] = sum_c o0(dy)[m, c] w1(dy, dx)[c]
+    alignas(16) uint8_t w1[3][2 * 4 * kCore];
+    float esum[3][kTailPx + 2];  // per dx: sum_dy D[m, 3 dy + dx]
+    alignas(16) float b0[32];
+    float b1;
+    uint64_t lbar, abar[2], bbar[2];
+    uint32_t tmem;
+};
+constexpr int kSmemTail = (int)sizeof(TailSmem) + 1024;
+static_assert(kSmemTail <= 112 * 1024, "k_den_tail: two blocks per SM");
+
+
+__device__ __forceinline__ void tma_load4(void *dst, const CUtensorMap *m, int c0, int c1, int c2,
+                                          int c3, uint64_t *bar) {
+    asm volatile(
+        "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, "
+        "{%2, %3, %4, %5}], [%6];" ::"r"(smem_u32(dst)),
+        "l"(reinterpret_cast<uint64_t>(m)), "r"(c0), "r"(c1), "r"(c2), "r"(c3),
+        "r"(smem_u32(bar))
+        : "memory");
+}
+
+struct TailGeo {
+    int64_t count, Hp, Wp, Ho, Wo, Hs, Ws, first;
+    int nseg, nchunk, R;
+};
+
+struct TailUnit {
+    int f, xs, ya, yb;
+};
+
+__device__ __forceinline__ TailUnit tail_unit(const TailGeo &g, int64_t u) {
+    TailUnit t;
+    const int64_t per_f = (int64_t)g.nseg * g.nchunk;
+    t.f = (int)(u / per_f);
+    const int rem = (int)(u - (int64_t)t.f * per_f);
+    const int c = rem / g.nseg, sg = rem - c * g.nseg;
+    t.xs = sg * kTailSeg;
+    t.ya = c * g.R;
+    t.yb = (int)((int64_t)(t.ya + g.R) < g.Ho ? (t.ya + g.R) : g.Ho);
+    return t;
+}
+
+// thread 0: the TMA boxes of h row `hrow` of strip `t` (rows and columns
+// outside the tensors read as zeros)
+__device__ __forceinline__ void tail_issue(TailSmem &s, const CUtensorMap *mx,
+                                           const CUtensorMap *mu, const TailUnit &t, int hrow) {
+    mbar_expect_tx(&s.lbar, kTailLoad);
+    tma_load4(s.sx, mx, 0, t.xs - 2, hrow, t.f, &s.lbar);
+    tma_load4(s.su, mu, 64 * (hrow & 1), (t.xs - 2) >> 1, hrow >> 1, t.f, &s.lbar);
+}
+
+__device__ __forceinline__ uint4 add8_bf16(uint4 x, uint4 y) {
+    uint4 r;
+    const uint32_t *px = reinterpret_cast<const uint32_t *>(&x);
+    const uint32_t *py = reinterpret_cast<const uint32_t *>(&y);
+    uint32_t *pr = reinterpret_cast<uint32_t *>(&r);
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+        const __nv_bfloat162 a = *reinterpret_cast<const __nv_bfloat162 *>(px + q);
+        const __nv_bfloat162 b = *reinterpret_cast<const __nv_bfloat162 *>(py + q);
+        const __nv_bfloat162 c = __floats2bfloat162_rn(__low2float(a) + __low2float(b),
+                                                       __high2float(a) + __high2float(b));
+        pr[q] = *reinterpret_cast<const uint32_t *>(&c);
+    }
+    return r;
+}
+
+// One 3 x 3 x 32 convolution row: 18 MMAs over the ring rows r0, r1, r2
+// (dy = 0, 1, 2), accumulator at TMEM column `col`.
+template <int N>
+__device__ __forceinline__ void tail_mma(uint32_t tmem, const uint8_t *r0, const uint8_t *r1,
+                                         const uint8_t *r2, const uint8_t *w, uint32_t wsbo) {
+    const uint8_t *rows[3] = {r0, r1, r2};
+    const uint32_t wb = smem_u32(w);
+#pragma unroll
+    for (int dy = 0; dy < 3; ++dy) {
+        const uint32_t ra = smem_u32(rows[dy]);
+#pragma unroll
+        for (int dx = 0; dx < 3; ++dx)
+#pragma unroll
+            for (int q = 0; q < 2; ++q) {
+                const int tap = 3 * dy + dx;
+                const uint64_t a = smem_desc_lbo(ra + (uint32_t)(2 * q * kTailPlane + dx * 16),
+                                                 (uint32_t)kTailPlane, 128u);
+                const uint64_t b = smem_desc_lbo(wb + (uint32_t)((tap * 4 + 2 * q) * kCore),
+                                                 (uint32_t)kCore, wsbo);
+                tc_mma(tmem, a, b, instr_desc<N>(), (tap | q) ? 1u : 0u);
+            }
+    }
+}
+
+constexpr int kTailThr = kThr + 32;  // 4 worker warps (TMEM lanes 0-127) + the issuing warp
+
+// The output convolution with its taps folded into N: per row dy two MMAs
+// (K = 32 channels) of the unshifted o0 row against the row's three taps;
+// the column shifts are applied in the epilogue.
+__device__ __forceinline__ void tail_mma_fold(uint32_t tmem, const uint8_t *r0, const uint8_t *r1,
+                                              const uint8_t *r2, const uint8_t (*w)[2 * 4 * kCore]) {
+    const uint8_t *rows[3] = {r0, r1, r2};
+#pragma unroll
+    for (int dy = 0; dy < 3; ++dy)
+#pragma unroll
+        for (int q = 0; q < 2; ++q) {
+            const uint64_t a = smem_desc_lbo(smem_u32(rows[dy]) + (uint32_t)(2 * q * kTailPlane),
+                                             (uint32_t)kTailPlane, 128u);
+            const uint64_t b = smem_desc_lbo(smem_u32(w[dy]) + (uint32_t)(2 * q * kCore),
+                                             (uint32_t)kCore, (uint32_t)(4 * kCore));
+            tc_mma(tmem, a, b, instr_desc<16>(), (dy | q) ? 1u : 0u);
+        }
+}
+
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, uint32_t (&r)[16]) {
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+        "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+          "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+          "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+        : "r"(taddr));
+    asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+}
+
+__global__ void __launch_bounds__(kTailThr, 2)
+    k_den_tail(const __grid_constant__ CUtensorMap mx, const __grid_constant__ CUtensorMap mu,
+               const uint4 *__restrict__ w0, const float *__restrict__ b0,
+               const uint4 *__restrict__ w1, const float *__restrict__ b1,
+               const float *__restrict__ src, float *__restrict__ out, TailGeo g, int clip) {
+    extern __shared__ uint8_t smem_raw[];
+    TailSmem &s = *reinterpret_cast<TailSmem *>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const bool worker = warp < 4, issuer = tid == kThr;  // issuer: lane 0 of warp 4
+    const uint4 zero = make_uint4(0u, 0u, 0u, 0u);
+    // filters as K-major core matrices: filter n, K chunk kc (tap * 4 + j)
+    for (int i = tid; i < 32 * kTailKC; i += kTailThr) {
+        const int n = i / kTailKC, kc = i % kTailKC;
+        *reinterpret_cast<uint4 *>(s.w0 + (n >> 3) * kTailSBO + kc * kCore + (n & 7) * 16) = w0[i];
+    }
+    for (int i = tid; i < 3 * 16 * 4; i += kTailThr) {
+        const int dy = i / 64, n = (i / 4) % 16, kc = i % 4;
+        *reinterpret_cast<uint4 *>(s.w1[dy] + (n >> 3) * 4 * kCore + kc * kCore + (n & 7) * 16) =
+            (n < 9 && n / 3 == dy) ? w1[n * 4 + kc] : zero;
+    }
+    for (int i = tid; i < 3 * 4; i += kTailThr) s.esum[i / 4][kTailPx - 2 + i % 4] = 0.f;
+    for (int i = tid; i < 32; i += kTailThr) s.b0[i] = b0[i];
+    if (tid == 0) s.b1 = b1 ? b1[0] : 0.f;
+    // o0 ring pixels 128, 129 are read only by the strip's two unused MMA rows
+    for (int i = tid; i < 4 * 4 * 2; i += kTailThr)
+        *reinterpret_cast<uint4 *>(s.o[i / 8] + ((i / 2) % 4) * kTailPlane + (128 + i % 2) * 16) =
+            zero;
+    const int64_t nunits = g.count * g.nseg * g.nchunk, G = gridDim.x;
+    if (tid == 0) {
+        mbar_init(&s.lbar, 1);
+        for (int i = 0; i < 2; ++i) {
+            mbar_init(s.abar + i, 1);
+            mbar_init(s.bbar + i, 1);
+        }
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        if ((int64_t)blockIdx.x < nunits) {
+            const TailUnit t0 = tail_unit(g, blockIdx.x);
+            tail_issue(s, &mx, &mu, t0, t0.ya - 2);
+        }
+    }
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                         smem_u32(&s.tmem)),
+                     "r"(kTailTmem)
+                     : "memory");
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+    }
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tc_fence_before();
+    __syncthreads();
+    tc_fence_after();
+    const uint32_t tmem = s.tmem;
+    const uint32_t lane = (uint32_t)(warp * 32) << 16;
+    // phase bits of the two o0 / e barriers, and their commits not yet waited for
+    unsigned lphase = 0, aph = 0, bph = 0, apend = 0, bpend = 0;
+    bool failed = false;
+    for (int64_t u = blockIdx.x; u < nunits && !failed; u += G) {
+        const TailUnit t = tail_unit(g, u);
+        // Step k (KH = yb - ya + 3):
+        //   A  (0 <= k <= KH)      h row ya - 2 + k from the staged rows
+        //   B  (2 <= k <= KH)      MMAs of o0 row ya - 3 + k into o0 buffer k & 1
+        //   C  (3 <= k <= KH + 1)  epilogue of o0 row ya - 4 + k (buffer (k - 1) & 1)
+        //      (6 <= k <= KH + 2)  epilogue of output row ya + k - 6 (buffer (k - 1) & 1)
+        //   D  (5 <= k <= KH + 1)  MMAs of output row ya + k - 5 into e buffer k & 1
+        // so each batch of MMAs runs while the block forms the next h row and
+        // the epilogue of the previous batch.
+        const int KH = (t.yb - t.ya) + 3;
+        for (int k = 0; k <= KH + 2; ++k) {
+            const int x = t.xs + tid, y = t.ya + k - 6;
+            const bool store = k >= 6 && tid < kTailSeg && x < g.Wo;
+            float cen = 0.f;
+            if (store) {  // the centre pixel, loaded while the step runs
+                const int64_t gi = g.first + t.f;
+                const int64_t yi = y < g.Hs ? y : 2 * (g.Hs - 1) - y;
+                const int64_t xi = x < g.Ws ? x : 2 * (g.Ws - 1) - x;
+                cen = __ldg(src + (gi * g.Hs + (yi < 0 ? 0 : yi)) * g.Ws + (xi < 0 ? 0 : xi));
+            }
+            // A (workers; the issuer is meanwhile issuing the previous step's D)
+            bool ok = true;
+            if (k <= KH) {
+                if (worker) {
+                    ok = mbar_wait(&s.lbar, lphase);
+                    uint8_t *hr = s.h[k & 3];
+                    for (int p = tid; p < kTailPx; p += kThr) {
+                        const int q = p >> 1, b = p & 1;
+#pragma unroll
+                        for (int j = 0; j < 4; ++j) {
+                            const uint4 xv = *reinterpret_cast<const uint4 *>(
+                                s.sx + p * 64 + ((j ^ ((p >> 1) & 3)) << 4));
+                            const uint4 uv = *reinterpret_cast<const uint4 *>(
+                                s.su + q * 128 + (((4 * b + j) ^ (q & 7)) << 4));
+                            *reinterpret_cast<uint4 *>(hr + j * kTailPlane + p * 16) =
+                                add8_bf16(xv, uv);
+                        }
+                    }
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                }
+                lphase ^= 1u;
+            }
+            tc_fence_before();
+            if (__syncthreads_or(!ok)) {
+                failed = true;
+                break;
+            }
+            tc_fence_after();
+            if (k >= 2 && k <= KH) apend |= 1u << (k & 1);
+            if (issuer && k <= KH) {  // the next row's boxes, into the stage just consumed; B
+                if (k + 1 <= KH) {
+                    tail_issue(s, &mx, &mu, t, t.ya - 1 + k);
+                } else if (u + G < nunits) {
+                    const TailUnit tn = tail_unit(g, u + G);
+                    tail_issue(s, &mx, &mu, tn, tn.ya - 2);
+                }
+                if (k >= 2) {
+                    tail_mma<32>(tmem + 32u * (k & 1), s.h[(k - 2) & 3], s.h[(k - 1) & 3],
+                                 s.h[k & 3], s.w0, (uint32_t)kTailSBO);
+                    tc_commit(s.abar + (k & 1));
+                }
+            }
+            // C (workers)
+            if (k >= 3 && k <= KH + 1) {
+                const int bi = (k - 1) & 1;
+                if (worker) {
+                    ok = mbar_wait(s.abar + bi, (aph >> bi) & 1u);
+                    tc_fence_after();
+                    uint32_t rr[32];
+                    tc_ld32(tmem + lane + 32u * bi, rr);
+                    const int orow = t.ya + k - 4, xo = t.xs - 1 + tid;  // this thread's o0 column
+                    const bool inside = orow >= 0 && orow < g.Hp && xo >= 0 && xo < g.Wp;
+                    uint8_t *orw = s.o[(k - 1) & 3];
+#pragma unroll
+                    for (int j = 0; j < 4; ++j) {
+                        const float4 *b4 = reinterpret_cast<const float4 *>(s.b0 + j * 8);
+                        const float4 ba = b4[0], bb = b4[1];
+                        const float bv[8] = {ba.x, ba.y, ba.z, ba.w, bb.x, bb.y, bb.z, bb.w};
+                        uint32_t w4[4];
+#pragma unroll
+                        for (int e = 0; e < 4; ++e) {
+                            const int c = j * 8 + 2 * e;
+                            float v0 = fmaxf(__uint_as_float(rr[c]) + bv[2 * e], 0.f);
+                            float v1 = fmaxf(__uint_as_float(rr[c + 1]) + bv[2 * e + 1], 0.f);
+                            if (!inside) v0 = v1 = 0.f;
+                            const __nv_bfloat162 hb = __floats2bfloat162_rn(v0, v1);
+                            w4[e] = *reinterpret_cast<const uint32_t *>(&hb);
+                        }
+                        *reinterpret_cast<uint4 *>(orw + j * kTailPlane + tid * 16) =
+                            make_uint4(w4[0], w4[1], w4[2], w4[3]);
+                    }
+                    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+                }
+                aph ^= 1u << bi;
+                apend &= ~(1u << bi);
+            }
+            if (k >= 6) {
+                const int bi = (k - 1) & 1;
+                if (worker) {
+                    ok = mbar_wait(s.bbar + bi, (bph >> bi) & 1u) && ok;
+                    tc_fence_after();
+                    uint32_t d[16];
+                    tc_ld16(tmem + lane + 64u + 32u * bi, d);
+#pragma unroll
+                    for (int dx = 0; dx < 3; ++dx)
+                        s.esum[dx][tid] = __uint_as_float(d[dx]) + __uint_as_float(d[3 + dx]) +
+                                          __uint_as_float(d[6 + dx]);
+                    asm volatile("bar.sync 1, 128;" ::: "memory");  // the four worker warps
+                    const float ev = s.esum[0][tid] + s.esum[1][tid + 1] + s.esum[2][tid + 2];
+                    if (store) {
+                        float v = cen - (ev + s.b1);
+                        if (clip) v = fminf(fmaxf(v, 0.f), 1.f);
+                        out[((int64_t)t.f * g.Ho + y) * g.Wo + x] = v;
+                    }
+                }
+                bph ^= 1u << bi;
+                bpend &= ~(1u << bi);
+            }
+            tc_fence_before();
+            if (__syncthreads_or(!ok)) {
+                failed = true;
+                break;
+            }
+            tc_fence_after();
+            if (k >= 5 && k <= KH + 1) {  // D: output row ya + k - 5 from o0 rows ya + k - 6 ..
+                if (issuer) {
+                    tail_mma_fold(tmem + 64u + 32u * (k & 1), s.o[(k - 3) & 3], s.o[(k - 2) & 3],
+                                  s.o[(k - 1) & 3], s.w1);
+                    tc_commit(s.bbar + (k & 1));
+                }
+                bpend |= 1u << (k & 1);
+            }
+        }
+    }
+    if (failed && tid == 0) {
+        atomicOr(&g_cnn_status, 1u);
+        // let the copies and MMAs in flight land before the block ends
+        mbar_wait(&s.lbar, lphase);
+        for (int i = 0; i < 2; ++i) {
+            if ((apend >> i) & 1u) mbar_wait(s.abar + i, (aph >> i) & 1u);
+            if ((bpend >> i) & 1u) mbar_wait(s.bbar + i, (bph >> i) & 1u);
+        }
+    }
+    tc_fence_before();
+    __syncthreads();
+    if (warp == 0)
+        asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                     "r"(kTailTmem)
+                     : "memory");
+}
+
 // Row-segment tiles with bulk-copied input rows (k_conv_thin_rows): 1.84 ms
 // for 8 x 2048 x 2048 -> 96 channels against 1.99 ms for the per-pixel
 // gather (SCI_THIN_ROWS=0); the gather with a second A buffer and the next
@@ -789,6 +1160,82 @@ int launch_thin_n(const void *in, const void *wts, const float *bias, void *out,
     if (form >= 2) return launch_rd<N>(in, wts, bias, out, F, H, W, relu, st);
     if (form == 1) return launch_rows<N>(in, wts, bias, out, F, H, W, relu, st);
     return launch_thin<N>(in, wts, bias, out, F, H, W, relu, st);
+}
+
+// Tensor map over a bfloat16 tensor of `rank` dims (innermost first; byte
+// strides of dims 1..rank-1), the box `box`, 64- or 128-byte swizzle.
+static bool encode_map(CUtensorMap *m, const void *base, int rank, const cuuint64_t *dims,
+                       const cuuint64_t *strides, const cuuint32_t *box, int swizzle_bytes) {
+    const EncodeTiledFn enc = tensor_map_encoder();
+    if (!enc) return false;
+    const cuuint32_t es[5] = {1u, 1u, 1u, 1u, 1u};
+    const CUtensorMapSwizzle sw =
+        swizzle_bytes == 128 ? CU_TENSOR_MAP_SWIZZLE_128B : CU_TENSOR_MAP_SWIZZLE_64B;
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, (cuuint32_t)rank, const_cast<void *>(base),
+               dims, strides, box, es, CU_TENSOR_MAP_INTERLEAVE_NONE, sw,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_128B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) ==
+           CUDA_SUCCESS;
+}
+
+// Rows per strip of k_den_tail: the fewest whole waves of strips times the
+// row steps each strip takes (its rows plus 6).  SCI_TAIL_ROWS overrides.
+static int tail_rows(int64_t count, int nseg, int64_t Ho, int slots) {
+    if (const char *e = getenv("SCI_TAIL_ROWS")) {
+        const int v = atoi(e);
+        if (v >= 8) return v;
+    }
+    int best = 64;
+    int64_t best_cost = INT64_MAX;
+    for (int R = 32; R <= 256; R += 8) {
+        const int64_t units = count * nseg * ((Ho + R - 1) / R);
+        const int64_t waves = (units + slots - 1) / slots;
+        const int64_t cost = waves * (int64_t)(R + 6);
+        if (cost < best_cost) best_cost = cost, best = R;
+    }
+    return best;
+}
+
+int launch_den_tail(const void *x0, const void *u1, const void *w0, const float *b0,
+                    const void *w1, const float *b1, const float *src, int64_t Hs, int64_t Ws,
+                    int64_t first, int64_t count, int64_t Hp, int64_t Wp, int64_t Ho, int64_t Wo,
+                    int clip, float *out, cudaStream_t st) {
+    CUtensorMap mx, mu;
+    {
+        const cuuint64_t dims[4] = {32, (cuuint64_t)Wp, (cuuint64_t)Hp, (cuuint64_t)count};
+        const cuuint64_t str[3] = {64, (cuuint64_t)Wp * 64, (cuuint64_t)(Hp * Wp * 64)};
+        const cuuint32_t box[4] = {32, (cuuint32_t)kTailPx, 1, 1};
+        if (!encode_map(&mx, x0, 4, dims, str, box, 64)) {
+            set_error("sci_cnn_den_tail: tensor map of x0 refused");
+            return SCI_ERR_CUDA;
+        }
+    }
+    {
+        const int64_t h2 = Hp / 2, w2 = Wp / 2;
+        const cuuint64_t dims[4] = {128, (cuuint64_t)w2, (cuuint64_t)h2, (cuuint64_t)count};
+        const cuuint64_t str[3] = {256, (cuuint64_t)w2 * 256, (cuuint64_t)(h2 * w2 * 256)};
+        const cuuint32_t box[4] = {64, 65, 1, 1};
+        if (!encode_map(&mu, u1, 4, dims, str, box, 128)) {
+            set_error("sci_cnn_den_tail: tensor map of u1 refused");
+            return SCI_ERR_CUDA;
+        }
+    }
+    TailGeo g;
+    g.count = count, g.Hp = Hp, g.Wp = Wp, g.Ho = Ho, g.Wo = Wo, g.Hs = Hs, g.Ws = Ws;
+    g.first = first;
+    g.nseg = (int)((Wo + kTailSeg - 1) / kTailSeg);
+    const int slots = kSMs * 2;
+    g.R = tail_rows(count, g.nseg, Ho, slots);
+    g.nchunk = (int)((Ho + g.R - 1) / g.R);
+    const int64_t units = count * g.nseg * g.nchunk;
+    const int grid = (int)(units < slots ? units : slots);
+    SCI_CUDA(cudaFuncSetAttribute(k_den_tail, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  kSmemTail));
+    k_den_tail<<<grid, kTailThr, kSmemTail, st>>>(mx, mu, reinterpret_cast<const uint4 *>(w0), b0,
+                                              reinterpret_cast<const uint4 *>(w1), b1, src, out,
+                                              g, clip);
+    SCI_CUDA(cudaGetLastError());
+    SCI_LAUNCHED("k_den_tail");
+    return SCI_OK;
 }
 
 }  // namespace
@@ -824,4 +1271,26 @@ extern "C" int sci_cnn_conv_thin(const void *in, const void *weights, const floa
             set_error("sci_cnn_conv_thin: N = %d (64 or 96)", N);
             return SCI_ERR_UNSUPPORTED;
     }
+}
+
+extern "C" int sci_cnn_den_tail(const void *x0, const void *u1, const void *w0, const float *b0,
+                                const void *w1, const float *b1, const float *src,
+                                int64_t nframes, int64_t Hs, int64_t Ws, int64_t first,
+                                int64_t count, int64_t Hp, int64_t Wp, int64_t Ho, int64_t Wo,
+                                int clip, float *out, void *stream) {
+    SCI_CHECK_ARG(x0 && u1 && w0 && b0 && w1 && src && out, "sci_cnn_den_tail: null pointer");
+    SCI_CHECK_ARG(count >= 1 && first >= 0 && first + count <= nframes,
+                  "sci_cnn_den_tail: frames [first, first + count) outside the source");
+    SCI_CHECK_ARG(Hp >= 4 && Wp >= 4 && Hp % 2 == 0 && Wp % 2 == 0,
+                  "sci_cnn_den_tail: Hp, Wp must be even and >= 4");
+    SCI_CHECK_ARG(Hs >= 1 && Ws >= 1 && Hs <= Hp && Ws <= Wp && Hp - Hs < Hs && Wp - Ws < Ws,
+                  "sci_cnn_den_tail: the padding must be less than the source size");
+    SCI_CHECK_ARG(Ho >= 1 && Wo >= 1 && Ho <= Hp && Wo <= Wp,
+                  "sci_cnn_den_tail: the crop must lie inside Hp x Wp");
+    SCI_CHECK_ARG(count * Hp <= INT32_MAX && Wp <= INT32_MAX / 2,
+                  "sci_cnn_den_tail: too large for the tensor coordinates");
+    SCI_CHECK_ARG(aligned16(x0) && aligned16(u1) && aligned16(w0) && aligned16(w1),
+                  "sci_cnn_den_tail: x0, u1, w0, w1 must be 16-byte aligned");
+    return sci::launch_den_tail(x0, u1, w0, b0, w1, b1, src, Hs, Ws, first, count, Hp, Wp, Ho,
+                                Wo, clip, out, as_stream(stream));
 }

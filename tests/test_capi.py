@@ -145,6 +145,19 @@ def test_argument_checks_of_the_wider_entry_points(L):
     # CNN first layer: null input
     assert L.sci_cnn_conv_thin(None, 16, 32, 48, 8, 64, 64, 96, 1, s) == -1
     assert "null" in _lib.last_error()
+    # DenBlock tail: null input, odd padded size, padding as large as the source
+    assert L.sci_cnn_den_tail(None, 16, 32, 48, 64, 0, 80, 4, 64, 64, 0, 2, 64, 64, 64, 64, 0,
+                              96, s) == -1
+    assert "null" in _lib.last_error()
+    assert L.sci_cnn_den_tail(16, 32, 48, 64, 80, 0, 96, 4, 63, 63, 0, 2, 63, 64, 63, 63, 0,
+                              112, s) == -1
+    assert "even" in _lib.last_error()
+    assert L.sci_cnn_den_tail(16, 32, 48, 64, 80, 0, 96, 4, 32, 32, 0, 2, 64, 64, 64, 64, 0,
+                              112, s) == -1
+    assert "padding" in _lib.last_error()
+    assert L.sci_cnn_den_tail(16, 32, 48, 64, 80, 0, 96, 4, 64, 64, 3, 2, 64, 64, 64, 64, 0,
+                              112, s) == -1
+    assert "frames" in _lib.last_error()
 
 
 def test_noalloc_scratch_limit_is_as_documented(L):

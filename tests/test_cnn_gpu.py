@@ -267,3 +267,86 @@ def test_bf16_tensor_core_path_on_odd_sizes(golden, kind):
         ref = ocnn.fastdvdnet_denoiser(v, 0.1, p)
     assert x.shape == v.shape
     assert noise_rel(x, v, ref) < NOISE_TOL["bf16"]
+
+
+def den_tail_ref(x0, u1, w0, b0, w1, src, first, Hs, Ws, Ho, Wo, clip):
+    """DenBlock tail in float64 from the same bfloat16 operands, rounding h
+    and o0 to bfloat16 where the kernel stores them."""
+    import torch.nn.functional as F
+    n, Hp, Wp, _ = x0.shape
+    u = u1.double().reshape(n, Hp // 2, Wp // 2, 2, 2, 32).permute(0, 1, 3, 2, 4, 5)
+    h = (x0.float() + u.reshape(n, Hp, Wp, 32).float()).to(torch.bfloat16).double()
+    h = h.permute(0, 3, 1, 2)
+    o0 = F.relu(F.conv2d(h, w0.double().reshape(32, 3, 3, 32).permute(0, 3, 1, 2), b0.double(),
+                         padding=1))
+    o0 = o0.to(torch.bfloat16).double()
+    e = F.conv2d(o0, w1.double().reshape(1, 3, 3, 32).permute(0, 3, 1, 2), padding=1)[:, 0]
+    cen = src[first:first + n].double()
+    cen = F.pad(cen[:, None], (0, Wp - Ws, 0, Hp - Hs), mode="reflect")[:, 0]
+    out = (cen - e)[:, :Ho, :Wo]
+    return out.clamp(0, 1) if clip else out
+
+
+@pytest.mark.parametrize("count,Hs,Ws,Hp,Wp,Ho,Wo,clip", [
+    (2, 10, 258, 12, 260, 12, 260, 0),   # three strips, the last one partial; reflect rows / cols
+    (1, 7, 130, 8, 132, 7, 130, 1),      # cropped and clipped
+    (3, 24, 32, 24, 32, 24, 32, 0),      # narrower than one strip
+    (2, 200, 300, 200, 300, 197, 299, 0),
+])
+def test_den_tail_matches_reference(count, Hs, Ws, Hp, Wp, Ho, Wo, clip):
+    """sci_cnn_den_tail (shuffle + add, two tcgen05 convolutions, centre -
+    output) against the float64 restatement of the same bfloat16 operands."""
+    torch.manual_seed(Hp * 1000 + Wp)
+    dev = torch.device("cuda")
+    x0 = torch.randn(count, Hp, Wp, 32, device=dev).to(torch.bfloat16)
+    u1 = torch.randn(count, Hp // 2, Wp // 2, 128, device=dev).to(torch.bfloat16)
+    w0 = (torch.randn(32, 288, device=dev) / 12).to(torch.bfloat16).contiguous()
+    b0 = torch.randn(32, device=dev) * 0.1
+    w1 = (torch.randn(288, device=dev) / 12).to(torch.bfloat16).contiguous()
+    first = 1
+    src = torch.rand(first + count + 1, Hs, Ws, device=dev)
+    out = torch.full((count, Ho, Wo), float("nan"), device=dev)
+    call("sci_cnn_den_tail", x0.data_ptr(), u1.data_ptr(), w0.data_ptr(), b0.data_ptr(),
+         w1.data_ptr(), None, src.data_ptr(), src.shape[0], Hs, Ws, first, count, Hp, Wp, Ho, Wo,
+         clip, out.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    ref = den_tail_ref(x0.cpu(), u1.cpu(), w0.cpu(), b0.cpu(), w1.cpu(), src.cpu(), first, Hs,
+                       Ws, Ho, Wo, clip)
+    got = out.cpu().double()
+    assert not torch.isnan(got).any()
+    err = (got - ref).abs()
+    # an o0 value that rounds to the neighbouring bfloat16 (float32 sums in
+    # another order) moves e by about 2^-8 of one product
+    assert float(err.max()) < 5e-3
+    assert float(err.mean()) < 2e-4
+    v = ctypes.c_uint(0)
+    call("sci_device_status", ctypes.byref(v), 1)
+    assert v.value == 0
+
+
+def test_fused_tail_and_unfused_agree(golden, monkeypatch):
+    """The bf16 FastDVDnet engine with the fused DenBlock tail against the
+    same engine running it as shuffle-add, two cuDNN convolutions and the
+    centre subtraction, on frames that need padding and three strips; both
+    against the float64 oracle."""
+    g = golden("cnn_fastdvdnet")
+    net = fastdvdnet(golden)
+    rng = np.random.default_rng(5)
+    v = rng.random((38, 259, 5)).astype(np.float32)  # padded to 40 x 260: three strips
+    a = cnn.CnnEngine(net, "fastdvdnet", "bf16", graphs=False)
+    assert a.tail
+    monkeypatch.setenv("SCI_CNN_TAIL", "0")
+    b = cnn.CnnEngine(net, "fastdvdnet", "bf16", graphs=False)
+    assert not b.tail
+    x = torch.from_numpy(np.moveaxis(v, -1, 0).copy()).cuda()
+    ra, rb = a(x, 0.1), b(x, 0.1)
+    d = (ra - rb).abs()
+    # bf16 networks: the unfused path rounds the output filter's result to
+    # bfloat16 before the subtraction, and the first stage's difference
+    # moves roundings of the second stage's inputs
+    assert float(d.max()) < 2e-2 and float(d.mean()) < 3e-3
+    p = ocnn.as_float64(ocnn.seeded_state_dict(ocnn.fastdvdnet_layout(1), int(g["seed"])))
+    ref = ocnn.fastdvdnet_denoiser(v, 0.1, p)
+    na = noise_rel(np.moveaxis(ra.cpu().numpy(), 0, -1), v, ref)
+    nb = noise_rel(np.moveaxis(rb.cpu().numpy(), 0, -1), v, ref)
+    assert na < NOISE_TOL["bf16"] and na < 1.1 * nb
