@@ -878,11 +878,10 @@ __device__ __forceinline__ uint4 add8_bf16(uint4 x, uint4 y) {
     return r;
 }
 
-// One 3 x 3 x 32 convolution row: 18 MMAs over the ring rows r0, r1, r2
-// (dy = 0, 1, 2), accumulator at TMEM column `col`.
-template <int N>
+// One row of the 3 x 3, 32 -> 32 convolution: 18 MMAs over the ring rows
+// r0, r1, r2 (dy = 0, 1, 2), accumulator at TMEM address `tmem`.
 __device__ __forceinline__ void tail_mma(uint32_t tmem, const uint8_t *r0, const uint8_t *r1,
-                                         const uint8_t *r2, const uint8_t *w, uint32_t wsbo) {
+                                         const uint8_t *r2, const uint8_t *w) {
     const uint8_t *rows[3] = {r0, r1, r2};
     const uint32_t wb = smem_u32(w);
 #pragma unroll
@@ -896,8 +895,8 @@ __device__ __forceinline__ void tail_mma(uint32_t tmem, const uint8_t *r0, const
                 const uint64_t a = smem_desc_lbo(ra + (uint32_t)(2 * q * kTailPlane + dx * 16),
                                                  (uint32_t)kTailPlane, 128u);
                 const uint64_t b = smem_desc_lbo(wb + (uint32_t)((tap * 4 + 2 * q) * kCore),
-                                                 (uint32_t)kCore, wsbo);
-                tc_mma(tmem, a, b, instr_desc<N>(), (tap | q) ? 1u : 0u);
+                                                 (uint32_t)kCore, (uint32_t)kTailSBO);
+                tc_mma(tmem, a, b, instr_desc<32>(), (tap | q) ? 1u : 0u);
             }
     }
 }
@@ -1049,8 +1048,8 @@ __global__ void __launch_bounds__(kTailThr, 2)
                     tail_issue(s, &mx, &mu, tn, tn.ya - 2);
                 }
                 if (k >= 2) {
-                    tail_mma<32>(tmem + 32u * (k & 1), s.h[(k - 2) & 3], s.h[(k - 1) & 3],
-                                 s.h[k & 3], s.w0, (uint32_t)kTailSBO);
+                    tail_mma(tmem + 32u * (k & 1), s.h[(k - 2) & 3], s.h[(k - 1) & 3],
+                             s.h[k & 3], s.w0);
                     tc_commit(s.abar + (k & 1));
                 }
             }
@@ -1233,7 +1232,6 @@ int launch_den_tail(const void *x0, const void *u1, const void *w0, const float 
     k_den_tail<<<grid, kTailThr, kSmemTail, st>>>(mx, mu, reinterpret_cast<const uint4 *>(w0), b0,
                                               reinterpret_cast<const uint4 *>(w1), b1, src, out,
                                               g, clip);
-    SCI_CUDA(cudaGetLastError());
     SCI_LAUNCHED("k_den_tail");
     return SCI_OK;
 }
