@@ -123,12 +123,13 @@ class Solver:
 
     def run_host_many(self, y_hosts, x_hosts):
         """End to end over a sequence of measurements (the frame-block loop of
-        ``admmdenoise_cacti``): each pinned host measurement (H, W) is copied
-        in and solved on the current stream while the previous result is
-        copied back into its pinned ``x_hosts[k]`` (B, H, W) on a second
-        stream.  Two device result slots alternate; a slot is reused only
-        after its copy-out has finished.  Returns when every result is on
-        the host."""
+        ``admmdenoise_cacti``): each pinned host measurement (H, W) is solved
+        on the current stream while, on a second stream, the previous result
+        is copied back into its pinned ``x_hosts[k]`` (B, H, W) and the
+        measurement after next is copied in.  Two device result slots and two
+        measurement slots alternate; a result slot is reused only after its
+        copy-out has finished, a measurement slot only after the solve that
+        read it.  Returns when every result is on the host."""
         if len(y_hosts) != len(x_hosts):
             raise ValueError("one host result buffer per measurement")
         dev = self.op.dev
@@ -140,21 +141,40 @@ class Solver:
             self._copy_stream = torch.cuda.Stream(device=dev)
         main = torch.cuda.current_stream()
         copy = self._copy_stream
-        freed = [None, None]  # events: copy-out of each slot finished
-        for k, (yh, xh) in enumerate(zip(y_hosts, x_hosts)):
+        n = len(y_hosts)
+        freed = [None, None]  # events: copy-out of each result slot finished
+        ready = [None, None]  # events: copy-in of each measurement slot finished
+        read = [None, None]   # events: the solve reading each measurement slot finished
+        copy.wait_stream(main)  # the slots may still be in use by earlier work
+
+        def copy_in(k):
+            s = k % 2
+            with torch.cuda.stream(copy):
+                if read[s] is not None:
+                    copy.wait_event(read[s])
+                self._y_slots[s].copy_(y_hosts[k], non_blocking=True)
+                ready[s] = torch.cuda.Event()
+                ready[s].record(copy)
+
+        for k in range(min(n, 2)):
+            copy_in(k)
+        x = None
+        for k in range(n):
             s = k % 2
             if freed[s] is not None:
                 main.wait_event(freed[s])
-            y = self._y_slots[s]
-            y.copy_(yh, non_blocking=True)
-            x = self.run(y, out=self._slots[s])
+            main.wait_event(ready[s])
+            x = self.run(self._y_slots[s], out=self._slots[s])
             solved = torch.cuda.Event()
             solved.record(main)
+            read[s] = solved
             copy.wait_event(solved)
             with torch.cuda.stream(copy):
-                xh.copy_(x, non_blocking=True)
+                x_hosts[k].copy_(x, non_blocking=True)
             freed[s] = torch.cuda.Event()
             freed[s].record(copy)
+            if k + 2 < n:
+                copy_in(k + 2)
         copy.synchronize()
         main.synchronize()
         return x_hosts
