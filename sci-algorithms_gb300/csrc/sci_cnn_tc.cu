@@ -987,8 +987,12 @@ __global__ void __launch_bounds__(kTailThr, 2)
     tc_fence_after();
     const uint32_t tmem = s.tmem;
     const uint32_t lane = (uint32_t)(warp * 32) << 16;
-    // phase bits of the two o0 / e barriers, and their commits not yet waited for
+    // phase bits of the load barrier and of the two o0 / e barriers, and the
+    // loads / commits not yet waited for (flipped and cleared only once a
+    // step's barrier shows every wait succeeded, so that a block giving up
+    // drains exactly what is still in flight)
     unsigned lphase = 0, aph = 0, bph = 0, apend = 0, bpend = 0;
+    bool lpend = (int64_t)blockIdx.x < nunits;  // the prologue's load
     bool failed = false;
     for (int64_t u = blockIdx.x; u < nunits && !failed; u += G) {
         const TailUnit t = tail_unit(g, u);
@@ -1031,7 +1035,6 @@ __global__ void __launch_bounds__(kTailThr, 2)
                     }
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 }
-                lphase ^= 1u;
             }
             tc_fence_before();
             if (__syncthreads_or(!ok)) {
@@ -1039,8 +1042,13 @@ __global__ void __launch_bounds__(kTailThr, 2)
                 break;
             }
             tc_fence_after();
+            if (k <= KH) {
+                lphase ^= 1u;
+                // the next row's boxes, into the stage just consumed
+                lpend = k + 1 <= KH || u + G < nunits;
+            }
             if (k >= 2 && k <= KH) apend |= 1u << (k & 1);
-            if (issuer && k <= KH) {  // the next row's boxes, into the stage just consumed; B
+            if (issuer && k <= KH) {  // the next row's boxes; B
                 if (k + 1 <= KH) {
                     tail_issue(s, &mx, &mu, t, t.ya - 1 + k);
                 } else if (u + G < nunits) {
@@ -1084,8 +1092,6 @@ __global__ void __launch_bounds__(kTailThr, 2)
                     }
                     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
                 }
-                aph ^= 1u << bi;
-                apend &= ~(1u << bi);
             }
             if (k >= 6) {
                 const int bi = (k - 1) & 1;
@@ -1106,8 +1112,6 @@ __global__ void __launch_bounds__(kTailThr, 2)
                         out[((int64_t)t.f * g.Ho + y) * g.Wo + x] = v;
                     }
                 }
-                bph ^= 1u << bi;
-                bpend &= ~(1u << bi);
             }
             tc_fence_before();
             if (__syncthreads_or(!ok)) {
@@ -1115,6 +1119,14 @@ __global__ void __launch_bounds__(kTailThr, 2)
                 break;
             }
             tc_fence_after();
+            if (k >= 3 && k <= KH + 1) {  // C's o0 batch waited for
+                aph ^= 1u << ((k - 1) & 1);
+                apend &= ~(1u << ((k - 1) & 1));
+            }
+            if (k >= 6) {  // and the e batch
+                bph ^= 1u << ((k - 1) & 1);
+                bpend &= ~(1u << ((k - 1) & 1));
+            }
             if (k >= 5 && k <= KH + 1) {  // D: output row ya + k - 5 from o0 rows ya + k - 6 ..
                 if (issuer) {
                     tail_mma_fold(tmem + 64u + 32u * (k & 1), s.o[(k - 3) & 3], s.o[(k - 2) & 3],
@@ -1128,7 +1140,7 @@ __global__ void __launch_bounds__(kTailThr, 2)
     if (failed && tid == 0) {
         atomicOr(&g_cnn_status, 1u);
         // let the copies and MMAs in flight land before the block ends
-        mbar_wait(&s.lbar, lphase);
+        if (lpend) mbar_wait(&s.lbar, lphase);
         for (int i = 0; i < 2; ++i) {
             if ((apend >> i) & 1u) mbar_wait(s.abar + i, (aph >> i) & 1u);
             if ((bpend >> i) & 1u) mbar_wait(s.bbar + i, (bph >> i) & 1u);
