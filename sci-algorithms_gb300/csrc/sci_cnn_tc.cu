@@ -1,40 +1,41 @@
-// Thin-input 3 x 3 convolution on the 5th-generation tensor cores
-// (tcgen05.mma, accumulator in tensor memory): the first layer of
-// FastDVDnet's denoising block (6 input channels -> 90 features, padded to
-// 8 -> 96; packages/fastdvdnet/models.py:29-43) and of FFDNet (5 -> 64,
+// Convolutions on the 5th-generation tensor cores (tcgen05.mma, accumulator
+// in tensor memory).
+//
+// 1. The thin-input 3 x 3 convolution: the first layer of FastDVDnet's
+// denoising block (6 input channels -> 90 features, padded to 8 -> 96;
+// packages/fastdvdnet/models.py:29-43) and of FFDNet (5 -> 64,
 // packages/ffdnet/models.py:37-42), where cuDNN falls back to slow kernels
-// because each filter tap has only 8 input channels.
-//
-// Implicit GEMM per tile of kM = 128 consecutive output pixels (flattened
-// frame, row, column order; TMEM lane m = pixel m of the tile):
+// because each filter tap has only 8 input channels.  Implicit GEMM per
+// tile of kM = 128 output pixels (TMEM lane m = pixel m of the tile):
 //   D[m, n] = sum_k A[m, k] * B[n, k],  k = tap * 8 + c  (tap = 3 dy + dx),
-// A = the tile's im2col rows (9 taps x 8 bf16 channels = 9 x 16 bytes, plus
-// one zero chunk: K = 80 = 5 MMAs of K = 16), gathered from the NHWC8 input
-// by cp.async (zero outside the frame); B = the N x 80 weights, staged once
-// per block.  Both operands are K-major without swizzle: an 8-row x 16-byte
-// core matrix is 128 contiguous bytes, K-adjacent core matrices are 128 B
-// apart (LBO), 8-row groups kSBO = 10 x 128 B apart (SBO).  The epilogue
-// reads D with tcgen05.ld (warp w owns lanes 32w..32w+31, i.e. thread t owns
-// pixel t), adds the bias, applies ReLU, stages the tile's N bf16 channels
-// per pixel in shared memory and writes them with one bulk copy (the
-// tile's pixels are contiguous in the NHWC output), which drains while the
-// block gathers its next tile.
+// K = 9 taps x 8 bf16 channels plus one zero chunk = 80 = 5 MMAs of K 16;
+// B = the N x 80 weights, staged once per block.  Both operands are K-major
+// without swizzle: an 8-row x 16-byte core matrix is 128 contiguous bytes,
+// with explicit byte offsets between K-adjacent core matrices (LBO) and
+// between 8-row groups (SBO).  The epilogue reads D with tcgen05.ld (warp w
+// owns lanes 32w..32w+31, i.e. thread t owns pixel t), adds the bias,
+// applies ReLU, stages the tile's N bf16 channels in shared memory and
+// writes them with bulk copies that drain while the block starts its next
+// tile.  Three forms:
+//   k_conv_thin_rd (the default): 128-pixel segments of a frame row; the
+//     three input row segments a tile needs are bulk-copied into shared
+//     memory two tiles ahead and read by the MMAs in place through
+//     tap-shifted descriptors; the output stage is swizzled and written by
+//     tensor stores (conflict-free 16-byte stage stores);
+//   k_conv_thin_rows: the same row segments, with the im2col rows built in
+//     shared memory and a pixel-major stage written by one bulk copy;
+//   k_conv_thin_tc: any 128 consecutive pixels, each row's nine taps
+//     gathered from global memory by cp.async.
+// 56 KiB of shared memory per block gives k_conv_thin_rd 4 blocks per SM
+// (4 x 128 = the SM's 512 TMEM columns); 64 / 74 KiB cap the other two
+// forms at 3.
 //
-// Two tilings: k_conv_thin_rows (the default) takes 128-pixel segments of a
-// frame row, stages the three input row segments a tile needs in shared
-// memory by bulk copies two tiles ahead, and builds the im2col rows from
-// them; k_conv_thin_tc takes any 128 consecutive pixels and gathers each
-// row's nine taps from global memory by cp.async.
+// 2. k_den_tail: FastDVDnet's DenBlock tail (shuffle + add, the 32 -> 32 and
+// 32 -> 1 convolutions, centre - output) in one warp-specialised kernel;
+// see the comments at the kernel.
 //
-// k_conv_thin_rd (the default) reads the staged rows in place through
-// tap-shifted descriptors and writes its output tile with tensor stores
-// from a swizzled stage (see the comments at the kernel).
-//
-// Persistent blocks of 128 threads; 64 / 74 KiB of shared memory per block
-// caps residency at 3 blocks per SM for the im2col and gather forms, 56 KiB
-// at 4 for k_conv_thin_rd (4 x 128 = the SM's 512 TMEM columns).
-// The wait for each tile's MMAs is bounded: on timeout the block sets bit 0
-// of the CNN status word, waits once more (bounded) for the MMAs in
+// Every wait on an mbarrier is bounded: on timeout the block sets bit 0 of
+// the CNN status word, waits once more (bounded) for the copies and MMAs in
 // flight, frees its tensor memory and returns.
 #include <cuda.h>  // CUtensorMap; the encoder is fetched through the runtime
 #include <cuda_bf16.h>
