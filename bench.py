@@ -611,6 +611,11 @@ def run_gpu(args):
         for k in ("cassi", "batched", "unrolled"):
             if k in extras:
                 line[k] = extras[k]
+        # the denoiser calls' bf16 times once more, short, at the very end
+        cnn_ms = {k: v["bf16"]["ms"] for k, v in extras.get("cnn", {}).items()
+                  if isinstance(v, dict) and "bf16" in v}
+        if cnn_ms:
+            line["cnn_bf16_ms_2048x2048x24"] = cnn_ms
         print(json.dumps(rounded(line)))
     if world > 1:
         torch.distributed.destroy_process_group()
